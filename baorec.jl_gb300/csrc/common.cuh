@@ -1,0 +1,162 @@
+// Internal declarations shared by the translation units of libbaorec_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "baorec_gb300.h"
+
+namespace baorec {
+
+constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
+
+// Device-side error word bits (set by kernels, read after a sync).
+enum : unsigned {
+  kErrOOB = 1u,        // particle index outside the mesh
+};
+
+struct Level {                        // one multigrid level
+  int n[3];
+  size_t N;
+  float* f;                            // right-hand side
+  float* v;                            // solution / correction
+  float* r;                            // residual / scratch
+  float* ax[3];                        // x_vec axes of this level (device, FP32)
+};
+
+struct DevBuf {                       // a growable device buffer
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace baorec
+
+struct baorec_ctx {
+  baorec_config cfg;
+  int n1, n2, n3, n1h;
+  size_t N, Nk;                        // real cells, complex (halved) cells
+  cudaStream_t stream;
+  cufftHandle plan_r2c = 0, plan_c2r = 0, plan_r2c2 = 0, plan_c2r2 = 0, plan_c2r3 = 0, plan_c2r6 = 0;
+  void* fft_work = nullptr;            // one work area shared by all plans
+  // persistent meshes: mesh3 = three adjacent meshes A | B | C
+  float* mesh3 = nullptr;
+  float* result = nullptr;             // recon.result_cache (= A)
+  bool has_result = false;
+  float* psi = nullptr;                // 6 real meshes (displacements / iterative parts)
+  bool psi_valid = false;              // psi[0..2] hold the displacement of `result`
+  cufftComplex* ck = nullptr;          // complex work: 6 spectra
+  float* xvec[3] = {nullptr, nullptr, nullptr};   // x_vec of the mesh (device)
+  float* phi_lo = nullptr;             // low part of the double-float solution
+  float* phi_lo2 = nullptr;            // ping-pong partners of the solution pair
+  float* phi_hi2 = nullptr;
+  // multigrid levels (level 0 = finest)
+  int nlev = 0;
+  baorec::Level lev[16];
+  // reductions
+  double* dred = nullptr;              // device FP64 partial sums
+  double* hred = nullptr;              // pinned host mirror
+  unsigned* derr = nullptr;            // device error word
+  unsigned* herr = nullptr;            // pinned host copy
+  // particle staging (host inputs)
+  baorec::DevBuf stage[8];
+  // statistics
+  int64_t launches = 0;
+  baorec_solve_stats last_stats;
+  char msg[512];
+};
+
+namespace baorec {
+
+int set_error(baorec_ctx* c, int code, const char* fmt, ...);
+int cuda_fail(baorec_ctx* c, cudaError_t e, const char* what);
+int cufft_fail(baorec_ctx* c, cufftResult e, const char* what);
+int ensure(baorec_ctx* c, DevBuf& b, size_t bytes);
+int finish(baorec_ctx* c, uint32_t flags);   // sync unless async; check device error word
+
+// Stage host particle arrays to the device (slot s..s+k-1); device pointers pass through.
+int stage_in(baorec_ctx* c, int slot, const float* p, int64_t n, uint32_t flags, const float** out);
+int stage_out_alloc(baorec_ctx* c, int slot, int64_t n, uint32_t flags, float* user, float** dev);
+int stage_out_copy(baorec_ctx* c, float* user, const float* dev, int64_t n, uint32_t flags);
+
+inline unsigned grid_for(size_t n, int block) {
+  size_t g = (n + block - 1) / block;
+  return (unsigned)(g > 0x7fffffffu ? 0x7fffffffu : (g == 0 ? 1 : g));
+}
+
+#define BAOREC_LAUNCHED(c) ((c)->launches++)
+
+#define CK(call)                                                         \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) return ::baorec::cuda_fail(ctx, _e, #call);   \
+  } while (0)
+
+#define CKLAUNCH()                                                       \
+  do {                                                                   \
+    ctx->launches++;                                                     \
+    cudaError_t _e = cudaGetLastError();                                 \
+    if (_e != cudaSuccess) return ::baorec::cuda_fail(ctx, _e, "kernel launch"); \
+  } while (0)
+
+#define CKFFT(call)                                                      \
+  do {                                                                   \
+    cufftResult _r = (call);                                             \
+    if (_r != CUFFT_SUCCESS) return ::baorec::cufft_fail(ctx, _r, #call); \
+  } while (0)
+
+#define CKS(call)                                                        \
+  do {                                                                   \
+    int _s = (call);                                                     \
+    if (_s != BAOREC_OK) return _s;                                      \
+  } while (0)
+
+// ---- geometry helpers shared by kernels ---------------------------------
+
+// Mesh geometry passed by value to kernels.
+struct Geom {
+  int n1, n2, n3;
+  float L[3];
+  float bmin[3];
+};
+
+inline Geom geom_of(const baorec_ctx* c) {
+  Geom g;
+  g.n1 = c->n1; g.n2 = c->n2; g.n3 = c->n3;
+  for (int a = 0; a < 3; ++a) { g.L[a] = c->cfg.box_size[a]; g.bmin[a] = c->cfg.box_min[a]; }
+  return g;
+}
+
+// ---- entry points implemented per translation unit ------------------------
+// paint.cu
+int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w,
+          int64_t n, int wrap, int mas, uint32_t flags);
+int minmax3(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
+            float mn[3], float mx[3]);
+// fft.cu
+int smooth(baorec_ctx* ctx, float* mesh);
+int normalize_data(baorec_ctx* ctx, float* delta);
+int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr);
+int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
+int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
+int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
+int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
+int smooth_pair(baorec_ctx* ctx, float* a, float* b);   // b == a + N uses one batched transform pair
+// mg.cu
+int mg_setup(baorec_ctx* ctx);
+int mg_update_tables(baorec_ctx* ctx);
+int xvec_update(baorec_ctx* ctx);
+int mg_jacobi(baorec_ctx* ctx, float* v, const float* f, const int nl[3], int niter, float* tmp);
+int mg_residual(baorec_ctx* ctx, float* r, const float* v, const float* f, const int nl[3]);
+int mg_reduce(baorec_ctx* ctx, float* coarse, const float* fine, const int nl[3]);
+int mg_prolong(baorec_ctx* ctx, float* fine, const float* coarse, const int nl[3], int add);
+int mg_vcycle_ref(baorec_ctx* ctx, int lvl, float* v, const float* f);
+int mg_fmg(baorec_ctx* ctx, const float* f, float* phi);
+int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st);
+// readout.cu
+int readout(baorec_ctx* ctx, const float* psi3, const float* x, const float* y, const float* z,
+            int64_t n, int field, int mode, float* o0, float* o1, float* o2);
+
+}  // namespace baorec

@@ -1,0 +1,356 @@
+// k-space operators around cuFFT: Gaussian smoothing, overdensity
+// normalisation (FP64 reductions), the iterative-FFT step and the
+// displacement / gradient meshes.
+//
+// Spectra are the halved R2C layout of an x-fastest mesh: element (i, j, k)
+// with i < n1/2+1 at i + (n1/2+1)*(j + n2*k); the halved axis is x as in
+// rfftfreq(dims[1]) (src/utils.jl:6).  The 1/N of the inverse transform is
+// folded into the k-space multiply that precedes every C2R.
+#include "common.cuh"
+
+namespace baorec {
+namespace {
+
+struct KGeom {
+  int n1h, n2, n3;
+  float mult[3];   // T(fs/n), fs = T(2π n / L) — the k-axis step of k_vec (src/utils.jl:3-10)
+  float invN;
+};
+
+KGeom kgeom_of(const baorec_ctx* c) {
+  KGeom g;
+  g.n1h = c->n1h; g.n2 = c->n2; g.n3 = c->n3;
+  const int n[3] = {c->n1, c->n2, c->n3};
+  for (int a = 0; a < 3; ++a) {
+    float fs = (float)(2.0 * 3.14159265358979323846 * (double)n[a] / (double)c->cfg.box_size[a]);
+    g.mult[a] = fs / (float)n[a];
+  }
+  g.invN = (float)(1.0 / (double)c->N);
+  return g;
+}
+
+// k axes of k_vec: rfftfreq for x, fftfreq (negative half from -n/2) for y, z.
+__device__ __forceinline__ void kvals(const KGeom& g, int i, int j, int k, float& kx, float& ky, float& kz) {
+  int jj = j < (g.n2 + 1) / 2 ? j : j - g.n2;
+  int kk = k < (g.n3 + 1) / 2 ? k : k - g.n3;
+  kx = __fmul_rn((float)i, g.mult[0]);
+  ky = __fmul_rn((float)jj, g.mult[1]);
+  kz = __fmul_rn((float)kk, g.mult[2]);
+}
+
+__device__ __forceinline__ float ksq(float kx, float ky, float kz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+}
+
+__device__ __forceinline__ void decompose(size_t e, const KGeom& g, int& i, int& j, int& k) {
+  i = (int)(e % g.n1h);
+  size_t r = e / g.n1h;
+  j = (int)(r % g.n2);
+  k = (int)(r / g.n2);
+}
+
+// smooth!: δ_k *= exp(-0.5 R² k²) (src/utils.jl:50-53), times 1/N.
+__global__ void gauss_kernel(cufftComplex* __restrict__ a, size_t nk, int batch, size_t stride,
+                             KGeom g, float R2) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nk; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; decompose(e, g, i, j, k);
+    float kx, ky, kz; kvals(g, i, j, k, kx, ky, kz);
+    float fac = expf(-0.5f * R2 * ksq(kx, ky, kz)) * g.invN;
+    for (int b = 0; b < batch; ++b) {
+      cufftComplex v = a[e + b * stride];
+      v.x *= fac; v.y *= fac;
+      a[e + b * stride] = v;
+    }
+  }
+}
+
+// iterate!, first half (src/iterative.jl:8-14, 26-28, 52-54): δ_k/k² (DC → 0)
+// and the products handed to the inverse transforms.
+//  local LOS: out[m] = k_i k_j δ_k/k² for (i,j) in (11,12,13,22,23,33)
+//  global LOS: out[m] = k_i² r̂_i δ_k/k² for each axis with r̂_i != 0.
+__global__ void hessian_kernel(const cufftComplex* __restrict__ dk, cufftComplex* __restrict__ out,
+                               size_t nk, KGeom g, int local, float3 los, int nprod, int axes_mask) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nk; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; decompose(e, g, i, j, k);
+    float kv[3]; kvals(g, i, j, k, kv[0], kv[1], kv[2]);
+    float k2 = ksq(kv[0], kv[1], kv[2]);
+    cufftComplex d = dk[e];
+    if (k2 == 0.0f) { d.x = 0.0f; d.y = 0.0f; }
+    else { d.x = __fdiv_rn(d.x, k2); d.y = __fdiv_rn(d.y, k2); }
+    d.x *= g.invN; d.y *= g.invN;
+    if (local) {
+      int m = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = a; b < 3; ++b) {
+          float s = __fmul_rn(kv[a], kv[b]);
+          out[e + (size_t)m * nk] = make_float2(__fmul_rn(s, d.x), __fmul_rn(s, d.y));
+          ++m;
+        }
+    } else {
+      const float r[3] = {los.x, los.y, los.z};
+      int m = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (!((axes_mask >> a) & 1)) continue;
+        float s = __fmul_rn(__fmul_rn(kv[a], kv[a]), r[a]);
+        out[e + (size_t)m * nk] = make_float2(__fmul_rn(s, d.x), __fmul_rn(s, d.y));
+        ++m;
+      }
+    }
+  }
+}
+
+// iterate!, second half (src/iterative.jl:17, 32-35, 58-60): δ_r = δ_s then
+// the terms subtracted in the reference's (i, j) order.
+__global__ void iterate_update_kernel(float* __restrict__ dr, const float* __restrict__ ds,
+                                      const float* __restrict__ parts, size_t N, int n1, int n2,
+                                      const float* __restrict__ ax, const float* __restrict__ ay,
+                                      const float* __restrict__ az, int local, int nprod,
+                                      float fac_diag, float fac_off) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    float v = ds[e];
+    if (local) {
+      int i = (int)(e % n1);
+      size_t r = e / n1;
+      int j = (int)(r % n2);
+      int k = (int)(r / n2);
+      float xv[3] = {ax[i], ay[j], az[k]};
+      float x2 = __fadd_rn(__fadd_rn(__fmul_rn(xv[0], xv[0]), __fmul_rn(xv[1], xv[1])), __fmul_rn(xv[2], xv[2]));
+      int m = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = a; b < 3; ++b) {
+          float fac = (a == b) ? fac_diag : fac_off;
+          float t = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(fac, parts[e + (size_t)m * N]), xv[a]), xv[b]), x2);
+          v = x2 > 0.0f ? __fsub_rn(v, t) : 0.0f;
+          ++m;
+        }
+    } else {
+      for (int m = 0; m < nprod; ++m) v = __fsub_rn(v, __fmul_rn(fac_diag, parts[e + (size_t)m * N]));
+    }
+    dr[e] = v;
+  }
+}
+
+// compute_displacements, iterative (src/iterative.jl:265-270): Ψ_i = i k_i δ_k / k²
+// (mode == 0); multigrid (src/multigrid.jl:765-768): ∂_i φ = i k_i φ_k (mode == 1).
+__global__ void grad_kernel(const cufftComplex* __restrict__ src, cufftComplex* __restrict__ out,
+                            size_t nk, KGeom g, int inv_lap) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nk; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; decompose(e, g, i, j, k);
+    float kv[3]; kvals(g, i, j, k, kv[0], kv[1], kv[2]);
+    float k2 = ksq(kv[0], kv[1], kv[2]);
+    cufftComplex d = src[e];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      // (i k) * (re + i im) = (-k im, k re)
+      float re = -__fmul_rn(kv[a], d.y), im = __fmul_rn(kv[a], d.x);
+      if (inv_lap) {
+        if (k2 > 0.0f) { re = __fdiv_rn(re, k2); im = __fdiv_rn(im, k2); }
+        else { re = 0.0f; im = 0.0f; }
+      }
+      out[e + (size_t)a * nk] = make_float2(re * g.invN, im * g.invN);
+    }
+  }
+}
+
+// FP64 block partial sums of up to two meshes (deterministic two-stage reduction).
+__global__ void sum2_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, size_t N,
+                                    double* __restrict__ part) {
+  double sa = 0.0, sb = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    sa += (double)a[e];
+    if (b) sb += (double)b[e];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  __shared__ double s[2][32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { s[0][wid] = sa; s[1][wid] = sb; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { ta += s[0][k]; tb += s[1][k]; }
+    part[2 * blockIdx.x] = ta;
+    part[2 * blockIdx.x + 1] = tb;
+  }
+}
+
+__device__ __forceinline__ void total2(const double* part, int nb, double& ta, double& tb) {
+  ta = 0.0; tb = 0.0;
+  for (int k = 0; k < nb; ++k) { ta += part[2 * k]; tb += part[2 * k + 1]; }
+}
+
+// setup_overdensity! data only (src/recon.jl:54-55): δ = (δ/mean - 1)/b.
+__global__ void norm_data_kernel(float* __restrict__ d, size_t N, const double* __restrict__ part, int nb,
+                                 float bias) {
+  __shared__ float mean_s;
+  if (threadIdx.x == 0) {
+    double ta, tb; total2(part, nb, ta, tb);
+    mean_s = (float)(ta / (double)N);
+  }
+  __syncthreads();
+  float mean = mean_s;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    d[e] = __fdiv_rn(__fsub_rn(__fdiv_rn(d[e], mean), 1.0f), bias);
+}
+
+// setup_overdensity! with randoms (src/recon.jl:78-85).
+__global__ void norm_randoms_kernel(float* __restrict__ d, const float* __restrict__ r, size_t N,
+                                    const double* __restrict__ part, int nb, float bias, float ran_min,
+                                    float nrand) {
+  __shared__ float al_s, thr_s;
+  if (threadIdx.x == 0) {
+    double ta, tb; total2(part, nb, ta, tb);
+    al_s = (float)(ta / tb);
+    thr_s = __fdiv_rn(__fmul_rn(ran_min, (float)tb), nrand);
+  }
+  __syncthreads();
+  const float al = al_s, thr = thr_s;
+  const float bal = __fmul_rn(bias, al);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    float rv = r[e];
+    float dv = __fsub_rn(d[e], __fmul_rn(al, rv));
+    d[e] = rv > thr ? __fdiv_rn(dv, __fmul_rn(bal, rv)) : 0.0f;
+  }
+}
+
+constexpr int kRedBlocks = 2 * kNumSMs;
+
+}  // namespace
+
+int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
+  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, nullptr, N, ctx->dred);
+  CKLAUNCH();
+  CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kRedBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double s = 0.0;
+  for (int k = 0; k < kRedBlocks; ++k) s += ctx->hred[2 * k];
+  *out = s;
+  return BAOREC_OK;
+}
+
+__global__ void sumsq_partial_kernel(const float* __restrict__ a, size_t N, double* __restrict__ part) {
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    s += (double)a[e] * (double)a[e];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+    part[blockIdx.x] = t;
+  }
+}
+
+int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
+  sumsq_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, N, ctx->dred);
+  CKLAUNCH();
+  CK(cudaMemcpyAsync(ctx->hred, ctx->dred, kRedBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double s = 0.0;
+  for (int k = 0; k < kRedBlocks; ++k) s += ctx->hred[k];
+  *out = s;
+  return BAOREC_OK;
+}
+
+int smooth(baorec_ctx* ctx, float* mesh) {
+  KGeom g = kgeom_of(ctx);
+  float R = ctx->cfg.smoothing_radius;
+  CKFFT(cufftExecR2C(ctx->plan_r2c, mesh, ctx->ck));
+  gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 1, ctx->Nk, g, R * R);
+  CKLAUNCH();
+  CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, mesh));
+  return BAOREC_OK;
+}
+
+// Smooth the data and randoms meshes with one batched transform pair.
+int smooth_pair(baorec_ctx* ctx, float* a, float* b) {
+  if (b != a + ctx->N) {   // batched plans need the two meshes adjacent
+    CKS(smooth(ctx, a));
+    return smooth(ctx, b);
+  }
+  KGeom g = kgeom_of(ctx);
+  float R = ctx->cfg.smoothing_radius;
+  CKFFT(cufftExecR2C(ctx->plan_r2c2, a, ctx->ck));
+  gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 2, ctx->Nk, g, R * R);
+  CKLAUNCH();
+  CKFFT(cufftExecC2R(ctx->plan_c2r2, ctx->ck, a));
+  return BAOREC_OK;
+}
+
+int normalize_data(baorec_ctx* ctx, float* delta) {
+  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, nullptr, ctx->N, ctx->dred);
+  CKLAUNCH();
+  norm_data_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(delta, ctx->N, ctx->dred, kRedBlocks,
+                                                                   ctx->cfg.bias);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr) {
+  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, ran, ctx->N, ctx->dred);
+  CKLAUNCH();
+  norm_randoms_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(
+      delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter) {
+  KGeom g = kgeom_of(ctx);
+  const bool local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL;
+  float beta = ctx->cfg.beta;
+  // factor = (1 + [i != j]) β, divided by (1 + β) on the first iteration
+  float fac_diag = beta, fac_off = 2.0f * beta;
+  if (iter == 1) { fac_diag = fac_diag / (1.0f + beta); fac_off = fac_off / (1.0f + beta); }
+  int mask = 0, nprod = 6;
+  float3 los = make_float3(ctx->cfg.los[0], ctx->cfg.los[1], ctx->cfg.los[2]);
+  if (!local) {
+    nprod = 0;
+    for (int a = 0; a < 3; ++a)
+      if (ctx->cfg.los[a] != 0.0f) { mask |= 1 << a; ++nprod; }
+  }
+  CKFFT(cufftExecR2C(ctx->plan_r2c, delta_r, ctx->ck));
+  hessian_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->ck, ctx->Nk, g, local ? 1 : 0,
+                                                                  los, nprod, mask);
+  CKLAUNCH();
+  if (nprod == 6) {
+    CKFFT(cufftExecC2R(ctx->plan_c2r6, ctx->ck, ctx->psi));
+  } else {
+    for (int m = 0; m < nprod; ++m)
+      CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck + (size_t)m * ctx->Nk, ctx->psi + (size_t)m * ctx->N));
+  }
+  iterate_update_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(
+      delta_r, delta_s, ctx->psi, ctx->N, ctx->n1, ctx->n2, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2],
+      local ? 1 : 0, nprod, fac_diag, fac_off);
+  CKLAUNCH();
+  ctx->psi_valid = false;
+  return BAOREC_OK;
+}
+
+int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3) {
+  KGeom g = kgeom_of(ctx);
+  // cuFFT's R2C reads but does not modify its input
+  CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
+  grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g,
+                                                               ctx->cfg.method == BAOREC_ITERATIVE ? 1 : 0);
+  CKLAUNCH();
+  CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, psi3));
+  return BAOREC_OK;
+}
+
+}  // namespace baorec
+
+extern "C" int baorec_smooth(baorec_ctx* ctx, float* mesh) {
+  if (!ctx || !mesh) return BAOREC_ERR_ARG;
+  CKS(baorec::smooth(ctx, mesh));
+  return baorec::finish(ctx, 0);
+}

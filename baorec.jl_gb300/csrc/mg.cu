@@ -1,0 +1,630 @@
+// Multigrid for the anisotropic reconstruction operator (src/multigrid.jl).
+//
+// Operator on a level with cell sizes c_a and per-axis tables p_a
+// (x_vec / cell for the local line of sight, los / cell for a global one):
+//   g = β / Σ c_a² p_a²,  gp_a = 1/c_a² + g p_a²
+//   (A v)_0 = 2 Σ gp_a v_0 − [ Σ gp_a (v_{+a} + v_{−a})
+//             + g/2 Σ_{a<b} p_a p_b (v_{++} + v_{−−} − v_{−+} − v_{+−})
+//             + (local only) g Σ p_a (v_{+a} − v_{−a}) ]        (periodic)
+// The neighbour coefficients sum to the diagonal, so A annihilates constants:
+// the periodic system is singular.
+//
+// Two solvers:
+//  * reference schedule (src/multigrid.jl:654-752): FMG with damped Jacobi
+//    (ω, ν sweeps), `vcycle_niterations` V-cycles per level, FP32;
+//  * convergent (no reference counterpart): defect correction
+//        r_k = f − α_k − A v_k,  α_{k+1} = α_k + mean(r_k),
+//        v_{k+1} = v_k + V(r_k − mean(r_k))
+//    with v held as a double-float pair (hi + lo) on the finest level and
+//    r_k evaluated in difference form, so the relative residual can reach
+//    1e-6 although every mesh is FP32.  The shift α converges to the value
+//    that makes the singular system consistent.  V is one V-cycle with
+//    red-black Gauss-Seidel smoothing on the operator whose first-derivative
+//    coefficients are clamped to |g p_a| <= κ gp_a (only cells next to the
+//    observer change), an FP64 shared-memory solve on the coarsest level.
+#include <math.h>
+#include <vector>
+
+#include "common.cuh"
+
+namespace baorec {
+namespace {
+
+constexpr float kClamp = 0.5f;       // κ for the V-cycle operators
+constexpr int kCoarseSweeps = 200;   // FP64 red-black sweeps on the coarsest level
+constexpr int kCoarseMaxCells = 2048;
+
+struct LG {                           // level geometry passed to kernels
+  int n[3];
+  float cell2[3], icell2[3];
+  const float* P[3];                  // p_a tables (local) — n[a] entries each
+  float pg[3];                        // los / cell (global)
+  float beta;
+  int local;
+  float clamp;                        // > 0: clamp derivative coefficients
+};
+
+struct Coef {
+  float gpx, gpy, gpz, g, pxy, pxz, pyz, dx, dy, dz;
+};
+
+__device__ __forceinline__ Coef coef_at(const LG& G, int i, int j, int k) {
+  float px, py, pz;
+  if (G.local) { px = G.P[0][i]; py = G.P[1][j]; pz = G.P[2][k]; }
+  else { px = G.pg[0]; py = G.pg[1]; pz = G.pg[2]; }
+  Coef c;
+  float px2 = px * px, py2 = py * py, pz2 = pz * pz;
+  c.g = G.beta / (G.cell2[0] * px2 + G.cell2[1] * py2 + G.cell2[2] * pz2);
+  c.gpx = G.icell2[0] + c.g * px2;
+  c.gpy = G.icell2[1] + c.g * py2;
+  c.gpz = G.icell2[2] + c.g * pz2;
+  c.pxy = px * py; c.pxz = px * pz; c.pyz = py * pz;
+  if (G.local) {
+    c.dx = c.g * px; c.dy = c.g * py; c.dz = c.g * pz;
+    if (G.clamp > 0.0f) {
+      c.dx = fminf(fmaxf(c.dx, -G.clamp * c.gpx), G.clamp * c.gpx);
+      c.dy = fminf(fmaxf(c.dy, -G.clamp * c.gpy), G.clamp * c.gpy);
+      c.dz = fminf(fmaxf(c.dz, -G.clamp * c.gpz), G.clamp * c.gpz);
+    }
+  } else {
+    c.dx = c.dy = c.dz = 0.0f;
+  }
+  return c;
+}
+
+struct Nb {                           // the 18 neighbours
+  float xp, xm, yp, ym, zp, zm;
+  float pp0, mm0, mp0, pm0;           // xy plane: (+,+), (−,−), (−,+), (+,−)
+  float p0p, m0m, m0p, p0m;           // xz
+  float _pp, _mm, _mp, _pm;           // yz
+};
+
+__device__ __forceinline__ void cell_ijk(size_t e, const int n[3], int& i, int& j, int& k) {
+  i = (int)(e % (unsigned)n[0]);
+  size_t r = e / (unsigned)n[0];
+  j = (int)(r % (unsigned)n[1]);
+  k = (int)(r / (unsigned)n[1]);
+}
+
+template <typename F>
+__device__ __forceinline__ Nb gather(F get, const int n[3], int i, int j, int k) {
+  int ip = i + 1 == n[0] ? 0 : i + 1, im = i == 0 ? n[0] - 1 : i - 1;
+  int jp = j + 1 == n[1] ? 0 : j + 1, jm = j == 0 ? n[1] - 1 : j - 1;
+  int kp = k + 1 == n[2] ? 0 : k + 1, km = k == 0 ? n[2] - 1 : k - 1;
+  Nb b;
+  b.xp = get(ip, j, k); b.xm = get(im, j, k);
+  b.yp = get(i, jp, k); b.ym = get(i, jm, k);
+  b.zp = get(i, j, kp); b.zm = get(i, j, km);
+  b.pp0 = get(ip, jp, k); b.mm0 = get(im, jm, k); b.mp0 = get(im, jp, k); b.pm0 = get(ip, jm, k);
+  b.p0p = get(ip, j, kp); b.m0m = get(im, j, km); b.m0p = get(im, j, kp); b.p0m = get(ip, j, km);
+  b._pp = get(i, jp, kp); b._mm = get(i, jm, km); b._mp = get(i, jm, kp); b._pm = get(i, jp, km);
+  return b;
+}
+
+// The bracket of src/multigrid.jl:64-79 (neighbour part), reference order.
+__device__ __forceinline__ float offdiag(const Coef& c, const Nb& b, int local) {
+  float s = c.gpx * (b.xp + b.xm) + c.gpy * (b.yp + b.ym) + c.gpz * (b.zp + b.zm) +
+            c.g / 2.0f * (c.pxy * (b.pp0 + b.mm0 - b.mp0 - b.pm0) + c.pxz * (b.p0p + b.m0m - b.m0p - b.p0m) +
+                          c.pyz * (b._pp + b._mm - b._mp - b._pm));
+  if (local) s += c.dx * (b.xp - b.xm) + c.dy * (b.yp - b.ym) + c.dz * (b.zp - b.zm);
+  return s;
+}
+
+__device__ __forceinline__ size_t at(const int n[3], int i, int j, int k) {
+  return (size_t)i + (size_t)n[0] * ((size_t)j + (size_t)n[1] * (size_t)k);
+}
+
+// ---- reference-schedule kernels -------------------------------------------
+
+// One damped-Jacobi sweep (src/multigrid.jl:137-191, 207): out = (1-ω)v + ω jac.
+__global__ void jacobi_kernel(const float* __restrict__ v, const float* __restrict__ f, float* __restrict__ out,
+                              LG G, float omega, size_t N) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, G.n, i, j, k);
+    Coef c = coef_at(G, i, j, k);
+    Nb b = gather([&](int a, int bb, int cc) { return v[at(G.n, a, bb, cc)]; }, G.n, i, j, k);
+    float jac = f[e] + offdiag(c, b, G.local);
+    jac /= 2.0f * (c.gpx + c.gpy + c.gpz);
+    out[e] = (1.0f - omega) * v[e] + omega * jac;
+  }
+}
+
+// r = f - A v (src/multigrid.jl:328-376, 393).
+__global__ void residual_kernel(const float* __restrict__ v, const float* __restrict__ f, float* __restrict__ r,
+                                LG G, size_t N, float shift) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, G.n, i, j, k);
+    Coef c = coef_at(G, i, j, k);
+    Nb b = gather([&](int a, int bb, int cc) { return v[at(G.n, a, bb, cc)]; }, G.n, i, j, k);
+    float av = 2.0f * (c.gpx + c.gpy + c.gpz) * v[e] - offdiag(c, b, G.local);
+    r[e] = (f[e] - shift) - av;
+  }
+}
+
+// Full-weighting restriction (src/multigrid.jl:586-640): coarse c centred on fine 2c+1.
+__global__ void reduce_kernel(const float* __restrict__ fine, float* __restrict__ coarse, int3 nf, int3 nc,
+                              size_t Nc) {
+  const int nfa[3] = {nf.x, nf.y, nf.z};
+  const int nca[3] = {nc.x, nc.y, nc.z};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < Nc; e += (size_t)gridDim.x * blockDim.x) {
+    int ci, cj, ck; cell_ijk(e, nca, ci, cj, ck);
+    int i = 2 * ci + 1, j = 2 * cj + 1, k = 2 * ck + 1;
+    int ip = i + 1 == nf.x ? 0 : i + 1, im = i - 1;
+    int jp = j + 1 == nf.y ? 0 : j + 1, jm = j - 1;
+    int kp = k + 1 == nf.z ? 0 : k + 1, km = k - 1;
+    auto F = [&](int a, int b, int c) { return fine[at(nfa, a, b, c)]; };
+    float s = 8.0f * F(i, j, k) +
+              4.0f * (F(ip, j, k) + F(im, j, k) + F(i, jp, k) + F(i, jm, k) + F(i, j, kp) + F(i, j, km)) +
+              2.0f * (F(ip, jp, k) + F(im, jp, k) + F(ip, jm, k) + F(im, jm, k) + F(ip, j, kp) + F(im, j, kp) +
+                      F(ip, j, km) + F(im, j, km) + F(i, jp, kp) + F(i, jm, kp) + F(i, jp, km) + F(i, jm, km)) +
+              F(ip, jp, kp) + F(im, jp, kp) + F(ip, jm, kp) + F(im, jm, kp) + F(ip, jp, km) + F(im, jp, km) +
+              F(ip, jm, km) + F(im, jm, km);
+    coarse[e] = s / 64.0f;
+  }
+}
+
+// Trilinear prolongation (src/multigrid.jl:456-509): coarse c → fine 2c+1,
+// midpoints 2c+2 (periodic).  add != 0 adds into fine (v += prolong(v2h)).
+__global__ void prolong_kernel(const float* __restrict__ coarse, float* __restrict__ fine, int3 nc, int3 nf,
+                               size_t Nc, int add) {
+  const int nfa[3] = {nf.x, nf.y, nf.z};
+  const int nca[3] = {nc.x, nc.y, nc.z};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < Nc; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, nca, i, j, k);
+    int ip = i + 1 == nc.x ? 0 : i + 1, jp = j + 1 == nc.y ? 0 : j + 1, kp = k + 1 == nc.z ? 0 : k + 1;
+    auto C = [&](int a, int b, int c) { return coarse[at(nca, a, b, c)]; };
+    float c000 = C(i, j, k), c100 = C(ip, j, k), c010 = C(i, jp, k), c001 = C(i, j, kp);
+    float c110 = C(ip, jp, k), c011 = C(i, jp, kp), c101 = C(ip, j, kp), c111 = C(ip, jp, kp);
+    int x0 = 2 * i + 1, y0 = 2 * j + 1, z0 = 2 * k + 1;
+    int x1 = x0 + 1 == nf.x ? 0 : x0 + 1, y1 = y0 + 1 == nf.y ? 0 : y0 + 1, z1 = z0 + 1 == nf.z ? 0 : z0 + 1;
+    float v[8] = {c000,
+                  (c000 + c100) / 2.0f,
+                  (c000 + c010) / 2.0f,
+                  (c000 + c001) / 2.0f,
+                  (c000 + c100 + c010 + c110) / 4.0f,
+                  (c000 + c010 + c001 + c011) / 4.0f,
+                  (c000 + c100 + c001 + c101) / 4.0f,
+                  (c000 + c100 + c010 + c001 + c110 + c101 + c011 + c111) / 8.0f};
+    size_t o[8] = {at(nfa, x0, y0, z0), at(nfa, x1, y0, z0), at(nfa, x0, y1, z0), at(nfa, x0, y0, z1),
+                   at(nfa, x1, y1, z0), at(nfa, x0, y1, z1), at(nfa, x1, y0, z1), at(nfa, x1, y1, z1)};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) fine[o[q]] = add ? fine[o[q]] + v[q] : v[q];
+  }
+}
+
+// ---- convergent-solver kernels --------------------------------------------
+
+// Half of a red-black Gauss-Seidel sweep, out of place: cells of `colour`
+// ((i+j+k) mod 2) get (rhs - shift + neighbours(in)) / diag, the others copy.
+__global__ void rb_half_kernel(const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ rhs,
+                               LG G, size_t N, int colour, float shift) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, G.n, i, j, k);
+    if (((i + j + k) & 1) != colour) { out[e] = in[e]; continue; }
+    Coef c = coef_at(G, i, j, k);
+    Nb b = gather([&](int a, int bb, int cc) { return in[at(G.n, a, bb, cc)]; }, G.n, i, j, k);
+    out[e] = (rhs[e] - shift + offdiag(c, b, G.local)) / (2.0f * (c.gpx + c.gpy + c.gpz));
+  }
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// v' = (hi + lo) + e as a renormalised double-float pair.
+__device__ __forceinline__ void df_add(float hi, float lo, float e, float& ohi, float& olo) {
+  float s, err;
+  two_sum(hi, e, s, err);
+  float t = __fadd_rn(lo, err);
+  ohi = __fadd_rn(s, t);
+  olo = __fsub_rn(t, __fsub_rn(ohi, s));
+}
+
+// Accurate residual with the exact (unclamped) operator, fused with the
+// solution update v' = v + e:  r = (f - α) + [neighbour bracket in differences
+// D = v_nb - v_0].  Writes hi', lo', r and FP64 block partials (Σr, Σr²).
+__global__ void resid_acc_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
+                                 const float* __restrict__ e_corr, const float* __restrict__ f,
+                                 float* __restrict__ ohi, float* __restrict__ olo, float* __restrict__ r,
+                                 LG G, size_t N, float alpha, double* __restrict__ part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, G.n, i, j, k);
+    Coef c = coef_at(G, i, j, k);
+    auto V = [&](int a, int bb, int cc, float& h, float& l) {
+      size_t q = at(G.n, a, bb, cc);
+      h = hi[q]; l = lo[q];
+      if (e_corr) df_add(h, l, e_corr[q], h, l);
+    };
+    float h0, l0;
+    V(i, j, k, h0, l0);
+    auto D = [&](int a, int bb, int cc) {
+      float h, l; V(a, bb, cc, h, l);
+      return __fadd_rn(__fsub_rn(h, h0), __fsub_rn(l, l0));
+    };
+    Nb b = gather(D, G.n, i, j, k);
+    // −A v expressed with differences (the constant terms cancel)
+    float br = c.gpx * (b.xp + b.xm) + c.gpy * (b.yp + b.ym) + c.gpz * (b.zp + b.zm) +
+               c.g / 2.0f * (c.pxy * ((b.pp0 + b.mm0) - (b.mp0 + b.pm0)) + c.pxz * ((b.p0p + b.m0m) - (b.m0p + b.p0m)) +
+                             c.pyz * ((b._pp + b._mm) - (b._mp + b._pm)));
+    if (G.local) br += c.dx * (b.xp - b.xm) + c.dy * (b.yp - b.ym) + c.dz * (b.zp - b.zm);
+    float rv = (f[e] - alpha) + br;
+    ohi[e] = h0;
+    olo[e] = l0;
+    r[e] = rv;
+    s1 += (double)rv;
+    s2 += (double)rv * (double)rv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double sh[2][32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][wid] = s1; sh[1][wid] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b2 = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += sh[0][q]; b2 += sh[1][q]; }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b2;
+  }
+}
+
+// FP64 red-black solve of the coarsest level in one block (shared memory):
+// mean-free right-hand side, kCoarseSweeps sweeps, mean-free solution.
+__global__ void coarse_solve_kernel(const float* __restrict__ rhs, float* __restrict__ v, LG G, int sweeps) {
+  extern __shared__ double sm[];
+  const int N = G.n[0] * G.n[1] * G.n[2];
+  double* sv = sm;
+  double* sf = sm + N;
+  __shared__ double red[32];
+  // mean of rhs
+  double loc = 0.0;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) { sf[e] = rhs[e]; loc += sf[e]; sv[e] = 0.0; }
+  for (int o = 16; o > 0; o >>= 1) loc += __shfl_xor_sync(0xffffffffu, loc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    red[0] = t / N;
+  }
+  __syncthreads();
+  const double mean = red[0];
+  for (int e = threadIdx.x; e < N; e += blockDim.x) sf[e] -= mean;
+  __syncthreads();
+  // each thread owns at most kCoarseMaxCells / blockDim cells; new values are
+  // staged in registers so same-colour (edge) neighbours read pre-update values
+  constexpr int kPer = kCoarseMaxCells / 256;
+  for (int s = 0; s < sweeps; ++s) {
+    for (int colour = 0; colour < 2; ++colour) {
+      double nv[kPer];
+      int q = 0;
+      for (int e = threadIdx.x; e < N; e += blockDim.x, ++q) {
+        int i, j, k; cell_ijk((size_t)e, G.n, i, j, k);
+        nv[q] = sv[e];
+        if (((i + j + k) & 1) != colour) continue;
+        Coef c = coef_at(G, i, j, k);
+        int ip = i + 1 == G.n[0] ? 0 : i + 1, im = i == 0 ? G.n[0] - 1 : i - 1;
+        int jp = j + 1 == G.n[1] ? 0 : j + 1, jm = j == 0 ? G.n[1] - 1 : j - 1;
+        int kp = k + 1 == G.n[2] ? 0 : k + 1, km = k == 0 ? G.n[2] - 1 : k - 1;
+        auto S = [&](int a, int bb, int cc) { return sv[at(G.n, a, bb, cc)]; };
+        double o = (double)c.gpx * (S(ip, j, k) + S(im, j, k)) + (double)c.gpy * (S(i, jp, k) + S(i, jm, k)) +
+                   (double)c.gpz * (S(i, j, kp) + S(i, j, km)) +
+                   (double)c.g / 2.0 *
+                       ((double)c.pxy * (S(ip, jp, k) + S(im, jm, k) - S(im, jp, k) - S(ip, jm, k)) +
+                        (double)c.pxz * (S(ip, j, kp) + S(im, j, km) - S(im, j, kp) - S(ip, j, km)) +
+                        (double)c.pyz * (S(i, jp, kp) + S(i, jm, km) - S(i, jm, kp) - S(i, jp, km)));
+        if (G.local)
+          o += (double)c.dx * (S(ip, j, k) - S(im, j, k)) + (double)c.dy * (S(i, jp, k) - S(i, jm, k)) +
+               (double)c.dz * (S(i, j, kp) - S(i, j, km));
+        nv[q] = (sf[e] + o) / (2.0 * ((double)c.gpx + (double)c.gpy + (double)c.gpz));
+      }
+      __syncthreads();
+      q = 0;
+      for (int e = threadIdx.x; e < N; e += blockDim.x, ++q) sv[e] = nv[q];
+      __syncthreads();
+    }
+  }
+  loc = 0.0;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) loc += sv[e];
+  for (int o = 16; o > 0; o >>= 1) loc += __shfl_xor_sync(0xffffffffu, loc, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    red[0] = t / N;
+  }
+  __syncthreads();
+  const double vm = red[0];
+  for (int e = threadIdx.x; e < N; e += blockDim.x) v[e] = (float)(sv[e] - vm);
+}
+
+LG level_geom(const baorec_ctx* ctx, int l, float clamp) {
+  const baorec::Level& L = ctx->lev[l];
+  LG G;
+  for (int a = 0; a < 3; ++a) {
+    G.n[a] = L.n[a];
+    float cell = ctx->cfg.box_size[a] / (float)L.n[a];
+    G.cell2[a] = cell * cell;
+    G.icell2[a] = 1.0f / G.cell2[a];
+    G.P[a] = L.ax[a];   // the level's p tables (x_vec / cell)
+    G.pg[a] = ctx->cfg.los[a] / cell;
+  }
+  G.beta = ctx->cfg.beta;
+  G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
+  G.clamp = clamp;
+  return G;
+}
+
+int level_of(const baorec_ctx* ctx, const int nl[3]) {
+  for (int l = 0; l < ctx->nlev; ++l)
+    if (ctx->lev[l].n[0] == nl[0] && ctx->lev[l].n[1] == nl[1] && ctx->lev[l].n[2] == nl[2]) return l;
+  return -1;
+}
+
+bool can_recurse(const int n[3]) {
+  for (int a = 0; a < 3; ++a)
+    if (!(n[a] > 4 && n[a] % 2 == 0)) return false;
+  return true;
+}
+
+unsigned blocks_for(size_t N) {
+  unsigned g = grid_for(N, 256);
+  return g > 32u * kNumSMs ? 32u * kNumSMs : g;
+}
+
+constexpr int kResBlocks = 2 * kNumSMs;
+
+}  // namespace
+
+// Allocate the level hierarchy and the per-level p tables (x_vec / cell of
+// src/utils.jl:21-25 with that level's cell size, rounded to FP32).
+int mg_setup(baorec_ctx* ctx) {
+  if (ctx->nlev > 0) return BAOREC_OK;
+  int n[3] = {ctx->n1, ctx->n2, ctx->n3};
+  int l = 0;
+  while (true) {
+    baorec::Level& L = ctx->lev[l];
+    for (int a = 0; a < 3; ++a) L.n[a] = n[a];
+    L.N = (size_t)n[0] * n[1] * n[2];
+    CK(cudaMalloc(&L.f, L.N * 4 * 4));   // f, v, r, t contiguous
+    L.v = L.f + L.N;
+    L.r = L.v + L.N;
+    for (int a = 0; a < 3; ++a) CK(cudaMalloc(&L.ax[a], (size_t)n[a] * 4));
+    ++l;
+    if (!can_recurse(n) || l == 16) break;
+    for (int a = 0; a < 3; ++a) n[a] /= 2;
+  }
+  ctx->nlev = l;
+  const size_t N0 = ctx->lev[0].N;
+  CK(cudaMalloc(&ctx->phi_lo, N0 * 4 * 3));
+  ctx->phi_lo2 = ctx->phi_lo + N0;
+  ctx->phi_hi2 = ctx->phi_lo2 + N0;
+  return mg_update_tables(ctx);
+}
+
+int mg_update_tables(baorec_ctx* ctx) {
+  for (int l = 0; l < ctx->nlev; ++l) {
+    baorec::Level& L = ctx->lev[l];
+    for (int a = 0; a < 3; ++a) {
+      std::vector<float> t(L.n[a]);
+      float cell = ctx->cfg.box_size[a] / (float)L.n[a];
+      for (int i = 0; i < L.n[a]; ++i) {
+        float xv = (float)((double)ctx->cfg.box_min[a] + ((double)i + 0.5) * (double)cell);
+        t[i] = xv / cell;
+      }
+      CK(cudaMemcpy(L.ax[a], t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+    }
+  }
+  return BAOREC_OK;
+}
+
+// x_vec of the mesh (src/utils.jl:21-25) for the iterative update.
+int xvec_update(baorec_ctx* ctx) {
+  const int n[3] = {ctx->n1, ctx->n2, ctx->n3};
+  for (int a = 0; a < 3; ++a) {
+    std::vector<float> t(n[a]);
+    float cell = ctx->cfg.box_size[a] / (float)n[a];
+    for (int i = 0; i < n[a]; ++i) t[i] = (float)((double)ctx->cfg.box_min[a] + ((double)i + 0.5) * (double)cell);
+    CK(cudaMemcpy(ctx->xvec[a], t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+  }
+  return BAOREC_OK;
+}
+
+int mg_jacobi(baorec_ctx* ctx, float* v, const float* f, const int nl[3], int niter, float* tmp) {
+  int l = level_of(ctx, nl);
+  if (l < 0) return set_error(ctx, BAOREC_ERR_ARG, "jacobi: %dx%dx%d is not a level of this mesh", nl[0], nl[1], nl[2]);
+  LG G = level_geom(ctx, l, 0.0f);
+  size_t N = ctx->lev[l].N;
+  float* a = v;
+  float* b = tmp;
+  for (int s = 0; s < niter; ++s) {
+    jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, f, b, G, ctx->cfg.jacobi_damping_factor, N);
+    CKLAUNCH();
+    float* t = a; a = b; b = t;
+  }
+  if (a != v) CK(cudaMemcpyAsync(v, a, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  return BAOREC_OK;
+}
+
+int mg_residual(baorec_ctx* ctx, float* r, const float* v, const float* f, const int nl[3]) {
+  int l = level_of(ctx, nl);
+  if (l < 0) return set_error(ctx, BAOREC_ERR_ARG, "residual: %dx%dx%d is not a level of this mesh", nl[0], nl[1], nl[2]);
+  LG G = level_geom(ctx, l, 0.0f);
+  residual_kernel<<<blocks_for(ctx->lev[l].N), 256, 0, ctx->stream>>>(v, f, r, G, ctx->lev[l].N, 0.0f);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+int mg_reduce(baorec_ctx* ctx, float* coarse, const float* fine, const int nl[3]) {
+  if (!can_recurse(nl)) return set_error(ctx, BAOREC_ERR_ARG, "reduce: level %dx%dx%d cannot be coarsened", nl[0], nl[1], nl[2]);
+  int3 nf = make_int3(nl[0], nl[1], nl[2]);
+  int3 nc = make_int3(nl[0] / 2, nl[1] / 2, nl[2] / 2);
+  size_t Nc = (size_t)nc.x * nc.y * nc.z;
+  reduce_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(fine, coarse, nf, nc, Nc);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+int mg_prolong(baorec_ctx* ctx, float* fine, const float* coarse, const int nl[3], int add) {
+  if (!can_recurse(nl)) return set_error(ctx, BAOREC_ERR_ARG, "prolong: level %dx%dx%d has no coarse level", nl[0], nl[1], nl[2]);
+  int3 nf = make_int3(nl[0], nl[1], nl[2]);
+  int3 nc = make_int3(nl[0] / 2, nl[1] / 2, nl[2] / 2);
+  size_t Nc = (size_t)nc.x * nc.y * nc.z;
+  prolong_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(coarse, fine, nc, nf, Nc, add);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+// vcycle! (src/multigrid.jl:689-719) on level lvl; level lvl+1 buffers are scratch.
+int mg_vcycle_ref(baorec_ctx* ctx, int lvl, float* v, const float* f) {
+  baorec::Level& L = ctx->lev[lvl];
+  const int nu = ctx->cfg.jacobi_niterations;
+  CKS(mg_jacobi(ctx, v, f, L.n, nu, L.r + L.N));
+  if (lvl + 1 < ctx->nlev) {
+    baorec::Level& C = ctx->lev[lvl + 1];
+    CKS(mg_residual(ctx, L.r, v, f, L.n));
+    CKS(mg_reduce(ctx, C.f, L.r, L.n));
+    CK(cudaMemsetAsync(C.v, 0, C.N * 4, ctx->stream));
+    CKS(mg_vcycle_ref(ctx, lvl + 1, C.v, C.f));
+    CKS(mg_prolong(ctx, v, C.v, L.n, 1));
+  }
+  return mg_jacobi(ctx, v, f, L.n, nu, L.r + L.N);
+}
+
+// fmg (src/multigrid.jl:722-752) starting at level lvl.
+static int fmg_level(baorec_ctx* ctx, int lvl, const float* f, float* v) {
+  baorec::Level& L = ctx->lev[lvl];
+  if (lvl + 1 < ctx->nlev) {
+    baorec::Level& C = ctx->lev[lvl + 1];
+    CKS(mg_reduce(ctx, C.f, f, L.n));
+    // the coarse solution lives in C.v; the coarse V-cycles use level lvl+2 as scratch
+    CKS(fmg_level(ctx, lvl + 1, C.f, C.v));
+    CKS(mg_prolong(ctx, v, C.v, L.n, 0));
+  } else {
+    CK(cudaMemsetAsync(v, 0, L.N * 4, ctx->stream));
+  }
+  for (int c = 0; c < ctx->cfg.vcycle_niterations; ++c) CKS(mg_vcycle_ref(ctx, lvl, v, f));
+  return BAOREC_OK;
+}
+
+int mg_fmg(baorec_ctx* ctx, const float* f, float* phi) {
+  CKS(mg_setup(ctx));
+  // the recursion reads C.f of every coarser level while the V-cycles of the
+  // finer level overwrite it only after that level's FMG stage has finished
+  return fmg_level(ctx, 0, f, phi);
+}
+
+// ---- convergent solve -------------------------------------------------------
+
+// One correction V-cycle on level lvl: lev[lvl].v ← V(rhs), rhs = lev[lvl].f - shift.
+static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
+  baorec::Level& L = ctx->lev[lvl];
+  LG G = level_geom(ctx, lvl, kClamp);
+  const size_t N = L.N;
+  float* v = L.v;
+  float* t = L.r + N;   // ping-pong partner
+  if (lvl + 1 == ctx->nlev) {
+    if (N <= (size_t)kCoarseMaxCells) {
+      // the shift only moves the mean, which the coarse solve removes
+      coarse_solve_kernel<<<1, 256, 2 * N * sizeof(double), ctx->stream>>>(L.f, v, G, kCoarseSweeps);
+      CKLAUNCH();
+      return BAOREC_OK;
+    }
+    CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
+    for (int s = 0; s < 50; ++s) {
+      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
+      CKLAUNCH();
+      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
+      CKLAUNCH();
+    }
+    return BAOREC_OK;
+  }
+  CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
+  for (int s = 0; s < ctx->cfg.nu1; ++s) {
+    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
+    CKLAUNCH();
+    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
+    CKLAUNCH();
+  }
+  baorec::Level& C = ctx->lev[lvl + 1];
+  residual_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, L.f, L.r, G, N, shift);
+  CKLAUNCH();
+  CKS(mg_reduce(ctx, C.f, L.r, L.n));
+  CKS(vcycle_rb(ctx, lvl + 1, 0.0f));
+  CKS(mg_prolong(ctx, v, C.v, L.n, 1));
+  for (int s = 0; s < ctx->cfg.nu2; ++s) {
+    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
+    CKLAUNCH();
+    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
+    CKLAUNCH();
+  }
+  return BAOREC_OK;
+}
+
+int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st) {
+  CKS(mg_setup(ctx));
+  baorec::Level& L0 = ctx->lev[0];
+  const size_t N = L0.N;
+  // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²)
+  double sf = 0.0, sf2 = 0.0;
+  CKS(sum_mesh(ctx, f, N, &sf));
+  CKS(sumsq_mesh(ctx, f, N, &sf2));
+  float* hiA = phi;
+  float* hiB = ctx->phi_hi2;
+  float* loA = ctx->phi_lo;
+  float* loB = ctx->phi_lo2;
+  if (phi0 && phi0 != phi) CK(cudaMemcpyAsync(hiA, phi0, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
+  CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
+  double alpha = sf / (double)N;
+  LG G = level_geom(ctx, 0, 0.0f);
+  bool have_e = false;
+  int cycles = 0;
+  double rho = 0.0, rho0 = 0.0;
+  int status = BAOREC_ERR_NOT_CONVERGED;
+  for (int it = 0;; ++it) {
+    resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
+                                                          G, N, (float)alpha, ctx->dred);
+    CKLAUNCH();
+    CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kResBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double s1 = 0.0, s2 = 0.0;
+    for (int q = 0; q < kResBlocks; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
+    double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;
+    rho = fn2 > 0.0 ? sqrt(s2 / fn2) : 0.0;
+    if (it == 0) rho0 = rho;
+    { float* t = hiA; hiA = hiB; hiB = t; t = loA; loA = loB; loB = t; }
+    if (!(rho == rho)) { status = set_error(ctx, BAOREC_ERR_NOT_CONVERGED, "multigrid solve produced NaN"); break; }
+    if (rho <= (double)ctx->cfg.rtol) { status = BAOREC_OK; break; }
+    if (cycles >= ctx->cfg.max_cycles) {
+      status = set_error(ctx, BAOREC_ERR_NOT_CONVERGED, "multigrid: relative residual %.3e after %d V-cycles (rtol %.1e)",
+                         rho, cycles, (double)ctx->cfg.rtol);
+      break;
+    }
+    double mean_r = s1 / (double)N;
+    alpha += mean_r;
+    // the correction V-cycle solves A e = r - mean(r); r sits in lev[0].f
+    CKS(vcycle_rb(ctx, 0, (float)mean_r));
+    have_e = true;
+    ++cycles;
+  }
+  if (hiA != phi) CK(cudaMemcpyAsync(phi, hiA, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (loA != ctx->phi_lo) CK(cudaMemcpyAsync(ctx->phi_lo, loA, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  baorec_solve_stats s;
+  s.cycles = cycles;
+  s.rel_residual = rho;
+  s.alpha = alpha;
+  s.rel_residual_initial = rho0;
+  ctx->last_stats = s;
+  if (st) *st = s;
+  return status;
+}
+
+}  // namespace baorec

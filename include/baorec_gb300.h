@@ -1,0 +1,240 @@
+/*
+ * baorec_gb300.h — C ABI of the GB300 (sm_103a) BAO reconstruction library.
+ *
+ * Each entry point replaces one function of BAOrec.jl's reconstruction path;
+ * the comment above it names the Julia method (file:line inside the BAOrec.jl
+ * project) whose behaviour it reproduces.  A Julia package binds these with
+ * `ccall`, Python with ctypes.
+ *
+ * Conventions
+ *  - Every function returns a baorec_status (0 = success).  On failure
+ *    baorec_last_error(ctx) returns a message that stays valid until the next
+ *    call on the same context.
+ *  - Meshes are FP32 arrays on the device, x fastest: element (ix, iy, iz) of
+ *    an n1 x n2 x n3 mesh is at ix + n1*(iy + n2*iz) — the memory order of a
+ *    Julia Array{Float32,3}(n1, n2, n3).  Indices are 0-based here; the
+ *    reference's ρ[i, j, k] is element (i-1, j-1, k-1).
+ *  - Particle arrays are FP32 structure-of-arrays (x, y, z, w).  They live on
+ *    the host when BAOREC_HOST is set in `flags`, else on the device.  They
+ *    are borrowed for the call only.
+ *  - A context owns one CUDA stream, its cuFFT plans and all work buffers.
+ *    Calls on one context must not overlap (not thread-safe); separate
+ *    contexts are independent.  Without BAOREC_ASYNC a call returns after its
+ *    work has finished on the GPU, like the reference's `wait(ev)`.
+ */
+#ifndef BAOREC_GB300_H
+#define BAOREC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BAOREC_OK = 0,
+  BAOREC_ERR_ARG = 1,           /* invalid argument (reference: MethodError / AssertionError) */
+  BAOREC_ERR_CUDA = 2,          /* CUDA runtime error */
+  BAOREC_ERR_CUFFT = 3,         /* cuFFT error */
+  BAOREC_ERR_NOT_CONVERGED = 4, /* residual-driven solve hit its cycle cap */
+  BAOREC_ERR_OOB = 5,           /* particle outside the mesh (reference: BoundsError) */
+  BAOREC_ERR_STATE = 6,         /* call order error, e.g. no result yet */
+  BAOREC_ERR_NOMEM = 7          /* device allocation failed */
+} baorec_status;
+
+/* flags */
+#define BAOREC_HOST       0x1u  /* particle pointers are host memory */
+#define BAOREC_ASYNC      0x2u  /* do not wait for the GPU before returning */
+#define BAOREC_WRITEBACK  0x4u  /* paint with wrap writes wrapped positions back (reference mutates its inputs) */
+
+/* method / option enums */
+#define BAOREC_ITERATIVE  0
+#define BAOREC_MULTIGRID  1
+#define BAOREC_LOS_LOCAL  0     /* los = nothing: radial line of sight from the origin */
+#define BAOREC_LOS_GLOBAL 1     /* fixed line-of-sight vector */
+#define BAOREC_MAS_CIC    0
+#define BAOREC_MAS_TSC    1     /* no reference counterpart */
+#define BAOREC_MG_REFERENCE  0  /* FMG, damped Jacobi, fixed cycles (src/multigrid.jl:722-752) */
+#define BAOREC_MG_CONVERGENT 1  /* residual-driven V-cycles to rtol (no reference counterpart) */
+#define BAOREC_FIELD_DISP 0     /* :disp */
+#define BAOREC_FIELD_RSD  1     /* :rsd  */
+#define BAOREC_FIELD_SUM  2     /* :sum  */
+
+/* Reconstruction parameters: the fields of IterativeRecon / MultigridRecon
+ * (src/recon.jl:2-33) plus the options this library adds. */
+typedef struct {
+  int32_t method;            /* BAOREC_ITERATIVE | BAOREC_MULTIGRID */
+  int32_t n[3];              /* mesh size (grid_size of run!) */
+  float box_size[3];         /* recon.box_size */
+  float box_min[3];          /* recon.box_min */
+  int32_t los_mode;          /* BAOREC_LOS_LOCAL (los = nothing) | BAOREC_LOS_GLOBAL */
+  float los[3];              /* recon.los when global */
+  float bias;                /* recon.bias */
+  float f;                   /* recon.f (growth rate) */
+  float smoothing_radius;    /* recon.smoothing_radius */
+  float beta;                /* recon.β; <= 0 means f / bias as the reference default */
+  int32_t n_iter;            /* IterativeRecon.n_iter (default 3) */
+  float jacobi_damping_factor;   /* MultigridRecon (default 0.4) */
+  int32_t jacobi_niterations;    /* MultigridRecon (default 5) */
+  int32_t vcycle_niterations;    /* MultigridRecon (default 6) */
+  float ran_min;             /* setup_overdensity! randoms threshold (default 0.01) */
+  /* additions */
+  int32_t mas;               /* BAOREC_MAS_CIC (default) | BAOREC_MAS_TSC */
+  int32_t mg_mode;           /* BAOREC_MG_REFERENCE (default) | BAOREC_MG_CONVERGENT */
+  int32_t nu1, nu2;          /* convergent mode: pre/post red-black Gauss-Seidel sweeps (2, 2) */
+  float rtol;                /* convergent mode: relative residual target (1e-6) */
+  int32_t max_cycles;        /* convergent mode: V-cycle cap (50) */
+} baorec_config;
+
+/* Solver statistics of the last multigrid solve. */
+typedef struct {
+  int32_t cycles;            /* V-cycles run */
+  double rel_residual;       /* |f - a*1 - A phi| / |f - a*1| after the last cycle (FP64) */
+  double alpha;              /* constant shift a removed from the right-hand side */
+  double rel_residual_initial;
+} baorec_solve_stats;
+
+typedef struct baorec_ctx baorec_ctx;
+
+/* Fill `cfg` with the reference defaults (n_iter 3, damping 0.4, 5 Jacobi
+ * sweeps, 6 V-cycles, ran_min 0.01, CIC, reference MG schedule, 2+2 sweeps,
+ * rtol 1e-6, 50 cycles). */
+void baorec_config_default(baorec_config* cfg);
+
+/* Create a context: allocates the mesh buffers and cuFFT plans for cfg->n on
+ * the current CUDA device.  Replaces setup_fft! (src/recon.jl:35-37), which
+ * plans the FFT on every run!. */
+int baorec_create(const baorec_config* cfg, baorec_ctx** out);
+int baorec_destroy(baorec_ctx* ctx);
+const char* baorec_last_error(const baorec_ctx* ctx);
+/* Update box_size / box_min (run! with randoms overrides them). */
+int baorec_set_box(baorec_ctx* ctx, const float box_size[3], const float box_min[3]);
+int baorec_get_box(const baorec_ctx* ctx, float box_size[3], float box_min[3]);
+/* The CUDA stream the context launches on (cudaStream_t as void*). */
+void* baorec_stream(baorec_ctx* ctx);
+/* Number of kernels this context has launched since creation. */
+int64_t baorec_kernel_launches(const baorec_ctx* ctx);
+/* Device pointer of the context's result field (result_cache), or NULL. */
+float* baorec_result_ptr(baorec_ctx* ctx);
+
+/* setup_box (src/utils.jl:100-109): box_min = min - pad/2, cubic box_size of
+ * the largest extent of max - min + pad.  Device min/max reduction. */
+int baorec_setup_box(baorec_ctx* ctx, const float* x, const float* y, const float* z,
+                     int64_t n, float pad, uint32_t flags,
+                     float box_size_out[3], float box_min_out[3]);
+
+/* cic! (src/mas.jl:1-52 CPU, :53-107 GPU): add the CIC weights of n particles
+ * to `mesh` (device, not cleared).  wrap != 0 applies the reference's
+ * periodic rules; with BAOREC_WRITEBACK the wrapped positions are written back
+ * into x, y, z like the reference mutates its inputs.  Particles whose cell
+ * falls outside the mesh are skipped and reported as BAOREC_ERR_OOB. */
+int baorec_cic(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z,
+               const float* w, int64_t n, int wrap, uint32_t flags);
+
+/* Triangular-shaped-cloud paint (no reference counterpart; same node and wrap
+ * conventions as cic!). */
+int baorec_tsc(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z,
+               const float* w, int64_t n, int wrap, uint32_t flags);
+
+/* The lower CIC cell of every particle (int32 keys ix + n1*(iy + n2*iz)) and
+ * the particle count per cell (int32 mesh, cleared first), computed by the
+ * paint's own binning; integer outputs, bit-exact with src/mas.jl:13-35.
+ * Either output may be NULL. */
+int baorec_cell_bins(baorec_ctx* ctx, const float* x, const float* y, const float* z,
+                     int64_t n, int wrap, uint32_t flags, int32_t* keys_out, int32_t* counts_out);
+
+/* smooth! (src/utils.jl:45-56, :85-96): Gaussian smoothing of a device mesh
+ * in place, exp(-R^2 k^2 / 2) in k space. */
+int baorec_smooth(baorec_ctx* ctx, float* mesh);
+
+/* setup_overdensity!, data only (src/recon.jl:42-57): paint (wrap), smooth,
+ * delta = (delta/mean - 1)/b.  `delta` (device) must be zero on entry. */
+int baorec_setup_overdensity(baorec_ctx* ctx, float* delta, float* x, float* y, float* z,
+                             const float* w, int64_t n, int wrap, uint32_t flags);
+
+/* setup_overdensity!, data + randoms (src/recon.jl:60-91).  `delta` must be
+ * zero on entry. */
+int baorec_setup_overdensity_randoms(baorec_ctx* ctx, float* delta,
+                                     const float* x, const float* y, const float* z,
+                                     const float* w, int64_t n,
+                                     const float* rx, const float* ry, const float* rz,
+                                     const float* rw, int64_t nr, uint32_t flags);
+
+/* iterate! (src/iterative.jl:5-67, :151-211): one iterative-FFT step with the
+ * 1-based counter `iter`; delta_r is updated in place from delta_s. */
+int baorec_iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
+
+/* Multigrid primitives on one level of size nl[3] (src/multigrid.jl). */
+/* jacobi! (:14-135, :193-210): niter damped-Jacobi sweeps on v. */
+int baorec_mg_jacobi(baorec_ctx* ctx, float* v, const float* f, const int32_t nl[3], int niter);
+/* residual! (:213-326, :378-395): r = f - A v. */
+int baorec_mg_residual(baorec_ctx* ctx, float* r, const float* v, const float* f, const int32_t nl[3]);
+/* reduce! (:520-584, :641-651): full-weighting restriction fine -> coarse (nl = fine size). */
+int baorec_mg_reduce(baorec_ctx* ctx, float* coarse, const float* fine, const int32_t nl[3]);
+/* prolong! (:398-453, :511-518): trilinear prolongation coarse -> fine (nl = fine size), overwrites fine. */
+int baorec_mg_prolong(baorec_ctx* ctx, float* fine, const float* coarse, const int32_t nl[3]);
+/* vcycle! (:654-719): one V-cycle on v (level size nl). */
+int baorec_mg_vcycle(baorec_ctx* ctx, float* v, const float* f, const int32_t nl[3]);
+/* fmg (:722-752): full multigrid on the context mesh size; phi is overwritten. */
+int baorec_mg_fmg(baorec_ctx* ctx, const float* f, float* phi);
+/* Residual-driven solve (no reference counterpart): V-cycles with red-black
+ * Gauss-Seidel smoothing until |f - a*1 - A phi| <= rtol |f - a*1|, the shift
+ * `a` making the singular periodic system consistent.  phi0 (device, may be
+ * NULL = zero start) is the initial guess; phi receives the solution.  stats
+ * may be NULL.  Returns BAOREC_ERR_NOT_CONVERGED at the cycle cap (phi holds
+ * the last iterate). */
+int baorec_mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0,
+                    baorec_solve_stats* stats);
+
+/* Statistics of the context's last residual-driven solve. */
+int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats* stats);
+
+/* reconstructed_overdensity! (src/recon.jl:93-132): overdensity then n_iter
+ * iterations into the context result.  rx.. may be NULL (data only). */
+int baorec_reconstructed_overdensity(baorec_ctx* ctx, float* x, float* y, float* z,
+                                     const float* w, int64_t n,
+                                     const float* rx, const float* ry, const float* rz,
+                                     const float* rw, int64_t nr, uint32_t flags);
+/* reconstructed_potential! (src/recon.jl:184-212): overdensity then the
+ * multigrid solve (cfg.mg_mode) into the context result. */
+int baorec_reconstructed_potential(baorec_ctx* ctx, float* x, float* y, float* z,
+                                   const float* w, int64_t n,
+                                   const float* rx, const float* ry, const float* rz,
+                                   const float* rw, int64_t nr, uint32_t flags);
+
+/* run! (src/recon.jl:134-261): with randoms the box is first replaced by
+ * setup_box(randoms, 500); then reconstructed_overdensity! (iterative) or
+ * reconstructed_potential! (multigrid) into the context result. */
+int baorec_run(baorec_ctx* ctx, float* x, float* y, float* z, const float* w, int64_t n,
+               const float* rx, const float* ry, const float* rz, const float* rw, int64_t nr,
+               uint32_t flags);
+
+/* Copy the result field (recon.result_cache) to `out` (host if BAOREC_HOST). */
+int baorec_get_result(baorec_ctx* ctx, float* out, uint32_t flags);
+/* Replace the result field (the 5-argument read_shifts takes a field). */
+int baorec_set_result(baorec_ctx* ctx, const float* in, uint32_t flags);
+
+/* The three displacement meshes of compute_displacements
+ * (src/iterative.jl:253-275 / src/multigrid.jl:755-773) for the result field;
+ * device outputs. */
+int baorec_displacement_meshes(baorec_ctx* ctx, float* psi_x, float* psi_y, float* psi_z);
+
+/* read_cic! (src/mas.jl:218-269): trilinear read of a device mesh at n
+ * particles (wrap = true as the reference's callers use). */
+int baorec_read_cic(baorec_ctx* ctx, const float* mesh, const float* x, const float* y,
+                    const float* z, int64_t n, float* out, uint32_t flags);
+
+/* read_shifts (src/recon.jl:264-364): shifts of kind `field` at n particles
+ * from the context result. */
+int baorec_read_shifts(baorec_ctx* ctx, const float* x, const float* y, const float* z,
+                       int64_t n, int field, float* sx, float* sy, float* sz, uint32_t flags);
+
+/* reconstructed_positions (src/recon.jl:366-388): p - shift(field). */
+int baorec_reconstructed_positions(baorec_ctx* ctx, const float* x, const float* y,
+                                   const float* z, int64_t n, int field,
+                                   float* ox, float* oy, float* oz, uint32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BAOREC_GB300_H */

@@ -1,0 +1,96 @@
+"""Multigrid parity: primitives and the reference FMG schedule against the
+oracle's restatement of src/multigrid.jl, and the residual-driven solver
+against an FP64 evaluation of the residual of the same discrete operator."""
+import numpy as np
+import pytest
+
+import baorec_oracle as O
+from _util import F32, rel_l2, small_lightcone
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(n=32, seed=0, local=True):
+    m = small_lightcone(n_data=30000, rand_factor=5, n_grid=n, seed=seed)
+    bs, bm = O.setup_box(m.rx, m.ry, m.rz, 25.0 * 256 / n)
+    f = O.setup_overdensity_randoms(np.zeros((n, n, n), F32), 2.0, 15.0, bs, bm, m.x, m.y, m.z, m.w,
+                                    m.rx, m.ry, m.rz, m.rw)
+    return f, bs, bm
+
+
+def _recon(bs, bm, los=None, **kw):
+    import baorec
+    return baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=los, **kw)
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.0, 1.0]])
+def test_residual_and_jacobi_match_oracle(los):
+    import baorec
+    f, bs, bm = _problem()
+    rec = _recon(bs, bm, los)
+    rng = np.random.default_rng(1)
+    v = O.smooth(rng.standard_normal(f.shape).astype(F32), 40.0, bs) * F32(100.0)
+    r = baorec.zeros_mesh(f.shape, device=False)
+    baorec.residual_(r, np.asfortranarray(v), np.asfortranarray(f), rec)
+    ro = O.residual(v, f, bs, bm, rec.beta, los=los)
+    assert rel_l2(r, ro) < 1e-4
+    g = np.asfortranarray(v.copy())
+    baorec.jacobi_(g, np.asfortranarray(f), rec, 3)
+    jo = O.jacobi(v.copy(), f, bs, bm, rec.beta, 0.4, 3, los=los)
+    assert rel_l2(g, jo) < 1e-6
+
+
+def test_reduce_prolong_match_oracle():
+    import baorec
+    f, bs, bm = _problem(n=32)
+    rec = _recon(bs, bm)
+    c = baorec.zeros_mesh((16, 16, 16), device=False)
+    baorec.reduce_(c, np.asfortranarray(f), rec, top_shape=f.shape)
+    co = O.reduce(f)
+    assert rel_l2(c, co) < 1e-6
+    fine = baorec.zeros_mesh(f.shape, device=False)
+    baorec.prolong_(fine, np.asfortranarray(co), rec, top_shape=f.shape)
+    np.testing.assert_allclose(fine, O.prolong(co, f.shape), rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.0, 1.0]])
+def test_fmg_reference_schedule_matches_oracle(los):
+    import baorec
+    f, bs, bm = _problem(n=32)
+    rec = _recon(bs, bm, los)
+    phi = baorec.fmg(np.asfortranarray(f), baorec.zeros_mesh(f.shape, device=False), rec)
+    po = O.fmg(f, bs, bm, rec.beta, F32(0.4), 5, 6, los=los)
+    # a long FP32 iteration: compare the potential and its gradient
+    assert rel_l2(phi, po) < 1e-3
+    g = O.gradient_meshes(np.asarray(phi, F32), bs)
+    go = O.gradient_meshes(po, bs)
+    assert max(rel_l2(g[a], go[a]) for a in range(3)) < 1e-3
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.0, 1.0]])
+def test_convergent_solve_reaches_rtol_in_fp64(los):
+    import baorec
+    f, bs, bm = _problem(n=32, seed=3)
+    rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40)
+    phi = baorec.zeros_mesh(f.shape, device=False)
+    st = baorec.solve_(phi, np.asfortranarray(f), rec)
+    assert st["rel_residual"] <= 1e-6 and st["cycles"] <= 20
+    # FP64 residual of the FP32 solution with the same coefficients (FP32 values, FP64 arithmetic)
+    coef = O.coefs_f64(O.stencil_coefficients(f.shape, bs, bm, rec.beta, los, F32))
+    r = (f.astype(np.float64) - st["alpha"]) - O.apply_operator(np.asarray(phi, np.float64), coef, los is None)
+    fn = np.linalg.norm(f.astype(np.float64) - st["alpha"])
+    assert np.linalg.norm(r) / fn < 2e-6
+
+
+def test_convergent_solution_matches_fp64_oracle_gradient():
+    import baorec
+    f, bs, bm = _problem(n=32, seed=5)
+    rec = _recon(bs, bm, None, mg_mode="convergent", rtol=1e-7, max_cycles=40)
+    phi = baorec.zeros_mesh(f.shape, device=False)
+    baorec.solve_(phi, np.asfortranarray(f), rec)
+    v64, hist, _ = O.solve_mg(f.astype(np.float64), bs.astype(np.float64), bm.astype(np.float64), rec.beta,
+                           los=None, rtol=1e-10, max_cycles=40)
+    g = O.gradient_meshes(np.asarray(phi, np.float64), bs.astype(np.float64))
+    go = O.gradient_meshes(v64, bs.astype(np.float64))
+    err = max(rel_l2(g[a], go[a]) for a in range(3))
+    assert err < 1e-5, err

@@ -1,0 +1,122 @@
+"""Paint parity: the CUDA CIC/TSC paint against the oracle's restatement of
+src/mas.jl.  Cell indices and counts are integers and must match bit for bit;
+the mesh is an FP32 sum in a different order, compared with a tolerance."""
+import numpy as np
+import pytest
+
+import baorec_oracle as O
+from _util import F32, uniform_box
+
+pytestmark = pytest.mark.gpu
+
+# FP32 accumulation in a different order: per-cell relative tolerance
+MESH_RTOL = 2e-5
+
+
+@pytest.mark.parametrize("n,npart", [(16, 5000), (32, 50000), (24, 20000)])
+def test_cell_bins_bit_exact(n, npart):
+    import baorec
+    L = F32(1000.0)
+    x, y, z, w = uniform_box(npart, L, seed=n)
+    # put some particles exactly on the upper boundary and on cell edges
+    x[:10] = L
+    y[10:20] = F32(0.0)
+    z[20:30] = F32(L / n * 3)
+    bs, bm = [L] * 3, [0.0] * 3
+    keys, counts = baorec.cell_bins(x, y, z, bs, bm, (n, n, n), wrap=True)
+    *_, okey = O.cell_keys(x, y, z, bs, bm, (n, n, n), wrap=True)
+    np.testing.assert_array_equal(keys.astype(np.int64), okey)
+    ocounts = O.cell_counts(x, y, z, bs, bm, (n, n, n), wrap=True)
+    np.testing.assert_array_equal(counts.astype(np.int64), ocounts)
+    assert counts.sum() == npart
+
+
+@pytest.mark.parametrize("wrap", [True, False])
+def test_cic_matches_oracle(wrap):
+    import baorec
+    n, npart = 32, 40000
+    L = F32(500.0)
+    bmin = (F32(-10.0), F32(5.0), F32(0.0))
+    x, y, z, w = uniform_box(npart, L * F32(0.9), seed=3, bmin=(0, 0, 0))
+    x = (x + bmin[0] + F32(1)).astype(F32)
+    y = (y + bmin[1] + F32(1)).astype(F32)
+    z = (z + bmin[2] + F32(1)).astype(F32)
+    bs = [L] * 3
+    rho = baorec.zeros_mesh((n, n, n), device=False)
+    gx, gy, gz = x.copy(), y.copy(), z.copy()
+    baorec.cic_(rho, gx, gy, gz, w, bs, bmin, wrap=wrap)
+    orho = np.zeros((n, n, n), F32)
+    orho, opos = O.cic(orho, x, y, z, w, bs, bmin, wrap=wrap)
+    np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(np.abs(orho).max()))
+    # mass conservation
+    assert abs(float(rho.sum(dtype=np.float64)) - float(w.sum(dtype=np.float64))) < 1e-4 * float(w.sum())
+
+
+def test_cic_wrap_mutates_positions_like_reference():
+    import baorec
+    n = 16
+    L = F32(100.0)
+    x = np.array([150.0, 50.0, 100.0, 99.999], F32)   # > L wraps, == L does not
+    y = np.array([10.0, 120.0, 0.0, 5.0], F32)
+    z = np.array([1.0, 2.0, 101.0, 3.0], F32)
+    w = np.ones(4, F32)
+    rho = baorec.zeros_mesh((n, n, n), device=False)
+    gx, gy, gz = x.copy(), y.copy(), z.copy()
+    baorec.cic_(rho, gx, gy, gz, w, [L] * 3, [0.0] * 3, wrap=True)
+    _, (ox, oy, oz) = O.cic(np.zeros((n, n, n), F32), x, y, z, w, [L] * 3, [0.0] * 3, wrap=True)
+    np.testing.assert_array_equal(gx, ox)
+    np.testing.assert_array_equal(gy, oy)
+    np.testing.assert_array_equal(gz, oz)
+    assert gx[0] == F32(50.0) and gx[2] == F32(100.0)
+
+
+def test_cic_out_of_bounds_raises_bounds_error():
+    import baorec
+    n = 8
+    rho = baorec.zeros_mesh((n, n, n), device=False)
+    x = np.array([10.0, -5.0], F32)
+    y = np.array([10.0, 10.0], F32)
+    z = np.array([10.0, 10.0], F32)
+    with pytest.raises(IndexError):
+        baorec.cic_(rho, x, y, z, np.ones(2, F32), [100.0] * 3, [0.0] * 3, wrap=True)
+    with pytest.raises(IndexError):
+        O.cic(np.zeros((n, n, n), F32), x, y, z, np.ones(2, F32), [100.0] * 3, [0.0] * 3, wrap=True)
+    # without wrapping a particle in the last cell writes past the mesh
+    x = np.array([99.0], F32)
+    with pytest.raises(IndexError):
+        baorec.cic_(rho, x, y[:1], z[:1], np.ones(1, F32), [100.0] * 3, [0.0] * 3, wrap=False)
+
+
+def test_cic_empty_input():
+    import baorec
+    rho = baorec.zeros_mesh((8, 8, 8), device=False)
+    e = np.zeros(0, F32)
+    baorec.cic_(rho, e, e, e, e, [100.0] * 3, [0.0] * 3)
+    assert not rho.any()
+
+
+def test_cic_device_arrays():
+    import torch
+    import baorec
+    n, npart = 32, 30000
+    L = F32(1000.0)
+    x, y, z, w = uniform_box(npart, L, seed=9)
+    t = [torch.from_numpy(a.copy()).cuda() for a in (x, y, z, w)]
+    rho = baorec.zeros_mesh((n, n, n))
+    baorec.cic_(rho, *t, [L] * 3, [0.0] * 3)
+    orho, _ = O.cic(np.zeros((n, n, n), F32), x, y, z, w, [L] * 3, [0.0] * 3)
+    np.testing.assert_allclose(rho.cpu().numpy(), orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
+
+
+@pytest.mark.parametrize("wrap", [True, False])
+def test_tsc_matches_oracle(wrap):
+    import baorec
+    n, npart = 32, 30000
+    L = F32(800.0)
+    x, y, z, w = uniform_box(npart, L * F32(0.8), seed=5)
+    x, y, z = [(a + F32(80)).astype(F32) for a in (x, y, z)]
+    rho = baorec.zeros_mesh((n, n, n), device=False)
+    baorec.tsc_(rho, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=wrap)
+    orho, _ = O.tsc(np.zeros((n, n, n), F32), x, y, z, w, [L] * 3, [0.0] * 3, wrap=wrap)
+    np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
+    assert abs(float(rho.sum(dtype=np.float64)) - float(w.sum(dtype=np.float64))) < 1e-4 * float(w.sum())
