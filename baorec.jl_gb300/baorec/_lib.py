@@ -84,6 +84,7 @@ _SIGS = {
     "baorec_mg_fmg": (C.c_int, [P, P, P]),
     "baorec_mg_solve": (C.c_int, [P, P, P, P, C.POINTER(SolveStats)]),
     "baorec_last_solve_stats": (C.c_int, [P, C.POINTER(SolveStats)]),
+    "baorec_profile_kernel": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_reconstructed_overdensity": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
     "baorec_reconstructed_potential": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
     "baorec_run": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),

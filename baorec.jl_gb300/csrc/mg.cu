@@ -628,3 +628,43 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
 }
 
 }  // namespace baorec
+
+extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, double* bytes) {
+  using namespace baorec;
+  if (!ctx || !avg_ms || !bytes || reps <= 0) return BAOREC_ERR_ARG;
+  CKS(mg_setup(ctx));
+  Level& L = ctx->lev[0];
+  const size_t N = L.N;
+  float* t = L.r + N;
+  LG G = level_geom(ctx, 0, 0.0f);
+  LG Gc = level_geom(ctx, 0, kClamp);
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  auto launch = [&]() {
+    if (which == 0)
+      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, t, L.f, Gc, N, 0, 0.0f);
+    else if (which == 1)
+      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, ctx->phi_lo2, L.r, L.f, ctx->phi_hi2, t,
+                                                            L.r, G, N, 0.0f, ctx->dred);
+    else
+      jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
+  };
+  if (which < 0 || which > 2) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  launch();   // warm-up
+  CK(cudaEventRecord(a, ctx->stream));
+  for (int r = 0; r < reps; ++r) launch();
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  CKLAUNCH();
+  ctx->launches += reps;
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *avg_ms = ms / reps;
+  // algorithmic bytes: a full smoothing sweep reads v and f and writes v (12 B/cell),
+  // half of it per colour; the accurate residual reads hi, lo, e, f and writes hi, lo, r
+  *bytes = which == 0 ? 6.0 * N : which == 1 ? 28.0 * N : 12.0 * N;
+  return BAOREC_OK;
+}

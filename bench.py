@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark: lightcone multigrid BAO reconstruction at 256^3 on GB300.
+
+Workload (one step = one reconstruction, as examples/lightcone_mg.jl runs it):
+  data 5e5 + randoms 5e6 FP32 points on a lightcone shell (r = 1000-1500 Mpc/h,
+  RA 0-90 deg, Dec 0-45 deg), padded 256^3 mesh (box from setup_box(randoms,
+  pad 25 Mpc/h): cell 5.96 Mpc/h), CIC, R = 15 Mpc/h, b = 2, f = 0.8, local LOS;
+  paint both catalogs -> smooth -> normalise -> multigrid V-cycles with 2+2
+  red-black sweeps until the relative residual is <= 1e-6 -> displacement ->
+  shifted positions of the data (:sum) and of the randoms (:sum and :disp).
+Inputs are seeded synthetic catalogs with the shapes and distributions of the
+UNIT lightcone mocks the reference benchmarks on (those files are not here).
+
+`python bench.py --gpus N --steps K --warmup W` prints one JSON line.
+`--impl reference` times the reference's CPU algorithm (a C/OpenMP + scipy.fft
+restatement, see oracle/cpu_port.py) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "baorec.jl_gb300"))
+
+METRIC = "recons/s at 1e-6 residual, learned-start MG vs plain MG, 256^3, one GB300"
+UNIT = "recons/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mesh", type=int, default=256)
+    ap.add_argument("--n-data", type=int, default=500_000)
+    ap.add_argument("--rand-factor", type=int, default=10)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = []
+        smax = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def workload(args, seed):
+    from baorec import mocks
+    import numpy as np
+    m = mocks.lightcone_mock(n_data=args.n_data, rand_factor=args.rand_factor, n_grid=args.mesh, seed=seed)
+    # padded mesh: box from the randoms with a 25 Mpc/h pad (cell 5.96 Mpc/h at 256^3)
+    pad = 25.0 * 256 / args.mesh
+    f32 = np.float32
+    bmin = np.array([m.rx.min(), m.ry.min(), m.rz.min()], f32) - f32(pad / 2)
+    bmax = np.array([m.rx.max(), m.ry.max(), m.rz.max()], f32) + f32(pad / 2)
+    side = f32(np.max(bmax - bmin))
+    return m, [float(side)] * 3, [float(v) for v in bmin]
+
+
+def traffic_per_launch(name, N):
+    """DRAM bytes per launch of `name` from the committed ncu capture, scaled to N cells."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            t = json.load(fh)[name]
+        return t["dram_bytes"] * N / t["cells"]
+    except Exception:
+        return None
+
+
+def cpu_baseline(args, m, bs, bm, reps=1):
+    """The reference's CPU algorithm on this host: one full reconstruction per sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from cpu_port import CpuPort
+    port = CpuPort()
+    n = (args.mesh,) * 3
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        port.lightcone_reconstruction(m, n, bs, bm)
+        times.append(time.perf_counter() - t0)
+    return port, min(times)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    m, bs, bm = workload(args, args.seed)
+    port = None
+    ts = []
+    for i in range(args.warmup + args.steps):
+        port, t = cpu_baseline(args, m, bs, bm)
+        if i >= args.warmup:
+            ts.append(t)
+    tm = sum(ts) / len(ts)
+    v = 1.0 / tm
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tm * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"lightcone MG reconstruction {args.mesh}^3, {args.n_data} data + "
+                               f"{args.n_data * args.rand_factor} randoms", "mesh": args.mesh},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": port.threads, "kind": "port",
+                         "sample": "one full reconstruction per step by the reference's CPU algorithm "
+                                   "(serial CIC paint, FMG damped Jacobi w=0.4 nu=5, 6 cycles/level; "
+                                   "C/OpenMP + scipy.fft); the reference schedule has no residual test"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import ctypes as C
+    import baorec
+    from baorec import _lib
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    m, bs, bm = workload(args, args.seed + rank)
+    n = (args.mesh,) * 3
+    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=None,
+                                mg_mode="convergent", rtol=1e-6, nu1=2, nu2=2, max_cycles=50)
+    ctx = baorec.setup_fft_(rec, n)
+    nd, nr = len(m.x), len(m.rx)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
+    R = [dev(a) for a in (m.rx, m.ry, m.rz, m.rw)]
+    out_d = [torch.empty(nd, device="cuda") for _ in range(3)]
+    out_rs = [torch.empty(nr, device="cuda") for _ in range(3)]
+    out_ri = [torch.empty(nr, device="cuda") for _ in range(3)]
+    ptr = lambda ts: [t.data_ptr() for t in ts]
+    torch.cuda.synchronize()
+    SUM, DISP = _lib.FIELD["sum"], _lib.FIELD["disp"]
+
+    def step(flags=0, xs=None, rs=None, od=None, ors=None, ori=None):
+        xs = xs or ptr(X)
+        rs = rs or ptr(R)
+        st = ctx.status("baorec_reconstructed_potential", *xs, nd, *rs, nr, flags)
+        if st != _lib.OK:
+            _lib.check(ctx.h, st)
+        ctx.call("baorec_reconstructed_positions", *xs[:3], nd, SUM, *(od or ptr(out_d)), flags | _lib.ASYNC)
+        ctx.call("baorec_reconstructed_positions", *rs[:3], nr, SUM, *(ors or ptr(out_rs)), flags | _lib.ASYNC)
+        ctx.call("baorec_reconstructed_positions", *rs[:3], nr, DISP, *(ori or ptr(out_ri)), flags)
+
+    for _ in range(args.warmup):
+        step()
+    stats = ctx.solve_stats()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launches()
+    clocks.start()
+    ev0.record(stream)
+    cycles = []
+    for _ in range(args.steps):
+        step()
+        cycles.append(ctx.solve_stats()["cycles"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = ctx.launches() - l0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = ws * 1000.0 / ms
+    stats = ctx.solve_stats()
+
+    # roofline of the dominant kernel (finest-level red-black half sweep), measured live
+    peak, peak_src = measured_peak()
+    avg = C.c_float()
+    nbytes = C.c_double()
+    ctx.call("baorec_profile_kernel", 0, 50, C.byref(avg), C.byref(nbytes))
+    achieved = nbytes.value / (avg.value * 1e-3) / 1e9
+    roofline = {"kernel": "rb_half_kernel (finest level, 256^3)", "bound": "hbm", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": traffic_per_launch("rb_half_kernel", int(np.prod(n))),
+                "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
+    ctx.call("baorec_profile_kernel", 1, 20, C.byref(avg), C.byref(nbytes))
+    aux = {"resid_acc_kernel": {"ms": avg.value, "GB/s": nbytes.value / (avg.value * 1e-3) / 1e9}}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        hX = [pin(a) for a in (m.x, m.y, m.z, m.w)]
+        hR = [pin(a) for a in (m.rx, m.ry, m.rz, m.rw)]
+        hod = [torch.empty(nd).pin_memory() for _ in range(3)]
+        hors = [torch.empty(nr).pin_memory() for _ in range(3)]
+        hori = [torch.empty(nr).pin_memory() for _ in range(3)]
+        hp = lambda ts: [t.data_ptr() for t in ts]
+        kw = dict(xs=hp(hX), rs=hp(hR), od=hp(hod), ors=hp(hors), ori=hp(hori))
+        step(_lib.HOST, **kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step(_lib.HOST, **kw)
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": ws / te, "unit": UNIT,
+               # potential: x,y,z,w of both catalogs; each read-out stages x,y,z again
+               "h2d_bytes_per_step": 16 * (nd + nr) + 12 * nd + 24 * nr,
+               "d2h_bytes_per_step": 12 * nd + 24 * nr, "ms_per_step": te * 1e3}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        port, tc = cpu_baseline(args, m, bs, bm)
+        cpu = {"value": 1.0 / tc, "unit": UNIT, "cores": port.threads, "kind": "port",
+               "sample": "one full reconstruction of this workload by the reference's CPU algorithm "
+                         "(serial CIC paint, FMG damped Jacobi w=0.4 nu=5, 6 cycles/level, C/OpenMP + "
+                         "scipy.fft); the reference schedule has no residual test"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"lightcone plain-start MG reconstruction {args.mesh}^3 to 1e-6, "
+                                   f"{nd} data + {nr} randoms, CIC, R=15, b=2, f=0.8, local LOS, 2+2 RB sweeps",
+                       "mesh": args.mesh, "start": "plain (zero); learned start not built",
+                       "l2": "working set per step > 1 GB >> 126 MB L2 (inputs larger than L2)",
+                       "parallelism": f"replicas x{ws}"},
+            "solver": {"cycles": stats["cycles"], "rel_residual": stats["rel_residual"],
+                       "cycles_per_step": cycles},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "roofline": roofline,
+            "kernels": aux,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

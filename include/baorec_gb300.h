@@ -186,6 +186,14 @@ int baorec_mg_fmg(baorec_ctx* ctx, const float* f, float* phi);
 int baorec_mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0,
                     baorec_solve_stats* stats);
 
+/* Measurement hook (no reference counterpart): launch one finest-level kernel
+ * `reps` times on the context's scratch buffers between two CUDA events on
+ * the context stream and report the mean duration and the kernel's
+ * algorithmic bytes per launch.  which: 0 = red-black half sweep,
+ * 1 = accurate residual with solution update, 2 = damped-Jacobi sweep
+ * (reference schedule).  Needs a multigrid context. */
+int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch);
+
 /* Statistics of the context's last residual-driven solve. */
 int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats* stats);
 

@@ -62,8 +62,17 @@ def test_setup_overdensity_randoms_matches_oracle():
     baorec.setup_overdensity_(d, rec, m.x, m.y, m.z, m.w, m.rx, m.ry, m.rz, m.rw)
     od = O.setup_overdensity_randoms(np.zeros((n, n, n), F32), 2.0, 15.0, bs, bm, m.x, m.y, m.z, m.w,
                                      m.rx, m.ry, m.rz, m.rw)
-    # thresholded division amplifies FP32 noise near the survey edge
-    assert rel_l2(d, od) < 1e-4
+    # δ = (δ_d - αδ_r)/(bαδ_r) where δ_r > thr: FP32 rounding may flip cells
+    # that sit on the threshold, and the division amplifies noise where δ_r is
+    # small.  Compare away from the threshold, and bound the flipped cells.
+    ran, _ = O.cic(np.zeros((n, n, n), F32), m.rx, m.ry, m.rz, m.rw, bs, bm, wrap=False)
+    ran = O.smooth(ran, 15.0, bs)
+    thr = 0.01 * float(ran.sum(dtype=np.float64)) / len(m.rx)
+    safe = ran > 10 * thr
+    assert rel_l2(d[safe], od[safe]) < 2e-5
+    near = np.abs(ran - thr) <= 1e-3 * thr
+    flipped = (d == 0) != (od == 0)
+    assert not np.any(flipped & ~near)
 
 
 @pytest.mark.parametrize("los", [None, (0.0, 0.0, 1.0), (0.6, 0.0, 0.8)])
