@@ -11,6 +11,7 @@ from . import _build
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_NOT_CONVERGED, ERR_OOB, ERR_STATE, ERR_NOMEM = 1, 2, 3, 4, 5, 6, 7
+ERR_TOO_LARGE = 8
 HOST, ASYNC, WRITEBACK = 0x1, 0x2, 0x4
 ITERATIVE, MULTIGRID = 0, 1
 LOS_LOCAL, LOS_GLOBAL = 0, 1
@@ -69,6 +70,7 @@ _SIGS = {
     "baorec_kernel_launches": (I64, [P]),
     "baorec_result_ptr": (P, [P]),
     "baorec_setup_box": (C.c_int, [P, P, P, P, I64, C.c_float, U32, F3, F3]),
+    "baorec_setup_box_noalloc": (C.c_int, [P, P, P, I64, C.c_float, P, F3, F3]),
     "baorec_cic": (C.c_int, [P, P, P, P, P, P, I64, C.c_int, U32]),
     "baorec_tsc": (C.c_int, [P, P, P, P, P, P, I64, C.c_int, U32]),
     "baorec_cell_bins": (C.c_int, [P, P, P, P, I64, C.c_int, U32, P, P]),

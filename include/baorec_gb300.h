@@ -39,7 +39,8 @@ typedef enum {
   BAOREC_ERR_NOT_CONVERGED = 4, /* residual-driven solve hit its cycle cap */
   BAOREC_ERR_OOB = 5,           /* particle outside the mesh (reference: BoundsError) */
   BAOREC_ERR_STATE = 6,         /* call order error, e.g. no result yet */
-  BAOREC_ERR_NOMEM = 7          /* device allocation failed */
+  BAOREC_ERR_NOMEM = 7,         /* device allocation failed */
+  BAOREC_ERR_TOO_LARGE = 8      /* input exceeds the fixed scratch of a no-allocation entry point */
 } baorec_status;
 
 /* flags */
@@ -122,6 +123,23 @@ float* baorec_result_ptr(baorec_ctx* ctx);
 int baorec_setup_box(baorec_ctx* ctx, const float* x, const float* y, const float* z,
                      int64_t n, float pad, uint32_t flags,
                      float box_size_out[3], float box_min_out[3]);
+
+/* Bounding box without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot let the
+ * library call cudaMalloc: hosts whose pool allocator (CUDA.jl, PyTorch)
+ * already owns the device memory budget, and latency-sensitive pipelines that
+ * cannot afford the device-wide synchronisation of cudaMalloc / cudaFree.
+ * It computes what baorec_setup_box computes, needs no context, and keeps its
+ * partial results in a fixed 24.6 KB device array that every GPU loading the
+ * library holds until exit.  x, y, z are device arrays of n particles; at most
+ * 16,777,216 particles per call (larger n returns BAOREC_ERR_TOO_LARGE, n < 1
+ * BAOREC_ERR_ARG).  The outputs are host arrays.  Work runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and the call waits for it.
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU race. */
+int baorec_setup_box_noalloc(const float* x, const float* y, const float* z, int64_t n, float pad,
+                             void* stream, float box_size_out[3], float box_min_out[3]);
 
 /* cic! (src/mas.jl:1-52 CPU, :53-107 GPU): add the CIC weights of n particles
  * to `mesh` (device, not cleared).  wrap != 0 applies the reference's
