@@ -74,16 +74,22 @@ int stage_out_copy(baorec_ctx* ctx, float* user, const float* dev, int64_t n, ui
   return BAOREC_OK;
 }
 
-static int make_plan(baorec_ctx* ctx, cufftHandle* p, cufftType t, int batch, size_t* maxw) {
-  int n[3] = {ctx->n3, ctx->n2, ctx->n1};
+// interleave4: C2R of `batch` spectra into one mesh of 4-float cells
+// (component b of cell i at 4 i + b), the layout of the read-out.
+static int make_plan(baorec_ctx* ctx, cufftHandle* p, cufftType t, int batch, size_t* maxw, bool interleave4 = false) {
   long long dims[3] = {ctx->n3, ctx->n2, ctx->n1};
-  (void)n;
   size_t w = 0;
   CKFFT(cufftCreate(p));
   CKFFT(cufftSetAutoAllocation(*p, 0));
   long long idist = t == CUFFT_R2C ? (long long)ctx->N : (long long)ctx->Nk;
   long long odist = t == CUFFT_R2C ? (long long)ctx->Nk : (long long)ctx->N;
-  CKFFT(cufftMakePlanMany64(*p, 3, dims, nullptr, 1, idist, nullptr, 1, odist, t, batch, &w));
+  if (interleave4) {
+    long long inembed[3] = {ctx->n3, ctx->n2, ctx->n1h};
+    long long onembed[3] = {ctx->n3, ctx->n2, ctx->n1};
+    CKFFT(cufftMakePlanMany64(*p, 3, dims, inembed, 1, (long long)ctx->Nk, onembed, 4, 1, t, batch, &w));
+  } else {
+    CKFFT(cufftMakePlanMany64(*p, 3, dims, nullptr, 1, idist, nullptr, 1, odist, t, batch, &w));
+  }
   CKFFT(cufftSetStream(*p, ctx->stream));
   if (w > *maxw) *maxw = w;
   return BAOREC_OK;
@@ -177,8 +183,8 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
   CKC(cudaMalloc(&ctx->psi, ctx->N * 4 * 6));
   CKC(cudaMalloc(&ctx->ck, ctx->Nk * sizeof(cufftComplex) * 6));
   for (int a = 0; a < 3; ++a) CKC(cudaMalloc(&ctx->xvec[a], (size_t)cfg->n[a] * 4));
-  CKC(cudaMalloc(&ctx->dred, 4096 * sizeof(double)));
-  CKC(cudaMallocHost(&ctx->hred, 4096 * sizeof(double)));
+  CKC(cudaMalloc(&ctx->dred, kRedCapacity * sizeof(double)));
+  CKC(cudaMallocHost(&ctx->hred, kRedCapacity * sizeof(double)));
   CKC(cudaMalloc(&ctx->derr, sizeof(unsigned)));
   CKC(cudaMallocHost(&ctx->herr, sizeof(unsigned)));
   CKC(cudaMemset(ctx->derr, 0, sizeof(unsigned)));
@@ -187,7 +193,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
       (st = make_plan(ctx, &ctx->plan_r2c2, CUFFT_R2C, 2, &maxw)) ||
       (st = make_plan(ctx, &ctx->plan_c2r, CUFFT_C2R, 1, &maxw)) ||
       (st = make_plan(ctx, &ctx->plan_c2r2, CUFFT_C2R, 2, &maxw)) ||
-      (st = make_plan(ctx, &ctx->plan_c2r3, CUFFT_C2R, 3, &maxw)) ||
+      (st = make_plan(ctx, &ctx->plan_c2r3, CUFFT_C2R, 3, &maxw, true)) ||
       (st = make_plan(ctx, &ctx->plan_c2r6, CUFFT_C2R, 6, &maxw)))
     return fail(st);
   CKC(cudaMalloc(&ctx->fft_work, maxw > 0 ? maxw : 256));
@@ -213,6 +219,7 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   cudaFree(ctx->ck);
   for (int a = 0; a < 3; ++a) cudaFree(ctx->xvec[a]);
   cudaFree(ctx->phi_lo);
+  cudaFree(ctx->coarse_M);
   for (int l = 0; l < ctx->nlev; ++l) {
     cudaFree(ctx->lev[l].f);
     for (int a = 0; a < 3; ++a) cudaFree(ctx->lev[l].ax[a]);
@@ -564,9 +571,11 @@ static int ensure_psi(baorec_ctx* ctx) {
 extern "C" int baorec_displacement_meshes(baorec_ctx* ctx, float* px, float* py, float* pz) {
   if (!ctx || !px || !py || !pz) return set_error(ctx, BAOREC_ERR_ARG, "displacement_meshes: missing output");
   CKS(ensure_psi(ctx));
-  CK(cudaMemcpyAsync(px, ctx->psi, ctx->N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(py, ctx->psi + ctx->N, ctx->N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(pz, ctx->psi + 2 * ctx->N, ctx->N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  // the context keeps Ψ interleaved (4 floats per cell); copy out one component per mesh
+  float* out[3] = {px, py, pz};
+  for (int a = 0; a < 3; ++a)
+    CK(cudaMemcpy2DAsync(out[a], sizeof(float), ctx->psi + a, 4 * sizeof(float), sizeof(float), ctx->N,
+                         cudaMemcpyDeviceToDevice, ctx->stream));
   return finish(ctx, 0);
 }
 

@@ -7,11 +7,14 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <vector>
+
 #include "baorec_gb300.h"
 
 namespace baorec {
 
 constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
+constexpr size_t kRedCapacity = 1u << 17;   // FP64 entries of the reduction-partials buffer
 
 // Device-side error word bits (set by kernels, read after a sync).
 enum : unsigned {
@@ -24,7 +27,9 @@ struct Level {                        // one multigrid level
   float* f;                            // right-hand side
   float* v;                            // solution / correction
   float* r;                            // residual / scratch
-  float* ax[3];                        // x_vec axes of this level (device, FP32)
+  float* ax[3];                        // p tables (x_vec / cell) of this level (device, FP32)
+  std::vector<float> ptab[3];          // host copies of the p tables
+  bool needs_clamp = false;            // some cell next to the observer needs a clamped coefficient
 };
 
 struct DevBuf {                       // a growable device buffer
@@ -55,6 +60,8 @@ struct baorec_ctx {
   // multigrid levels (level 0 = finest)
   int nlev = 0;
   baorec::Level lev[16];
+  double* coarse_M = nullptr;          // dense FP64 inverse of level dense_level (or null)
+  int dense_level = -1;                // first level with at most 512 cells
   // reductions
   double* dred = nullptr;              // device FP64 partial sums
   double* hred = nullptr;              // pinned host mirror

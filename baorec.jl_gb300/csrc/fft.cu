@@ -157,11 +157,27 @@ __global__ void grad_kernel(const cufftComplex* __restrict__ src, cufftComplex* 
   }
 }
 
-// FP64 block partial sums of up to two meshes (deterministic two-stage reduction).
+// FP64 block partial sums of up to two meshes (deterministic two-stage
+// reduction).  Each group of 4 consecutive cells is added in FP32 before it
+// joins the FP64 accumulator: FP64 arithmetic is slow on this GPU, and a
+// 4-term FP32 sum carries at most 3 roundings.
 __global__ void sum2_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, size_t N,
                                     double* __restrict__ part) {
   double sa = 0.0, sb = 0.0;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+  // vector path only for 16-byte aligned meshes (sub-meshes of a batch may not be)
+  const bool vec = ((uintptr_t)a % 16 == 0) && (!b || (uintptr_t)b % 16 == 0);
+  const size_t N4 = vec ? N / 4 : 0;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  const float4* b4 = reinterpret_cast<const float4*>(b);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
+    const float4 u = a4[e];
+    sa += (double)((u.x + u.y) + (u.z + u.w));
+    if (b) {
+      const float4 w = b4[e];
+      sb += (double)((w.x + w.y) + (w.z + w.w));
+    }
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
     sa += (double)a[e];
     if (b) sb += (double)b[e];
   }
@@ -181,19 +197,33 @@ __global__ void sum2_partial_kernel(const float* __restrict__ a, const float* __
   }
 }
 
+// Block-cooperative total of the nb two-component FP64 partials; the result
+// is valid in thread 0.  Summation order is fixed, so it is deterministic.
 __device__ __forceinline__ void total2(const double* part, int nb, double& ta, double& tb) {
   ta = 0.0; tb = 0.0;
-  for (int k = 0; k < nb; ++k) { ta += part[2 * k]; tb += part[2 * k + 1]; }
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) { ta += part[2 * k]; tb += part[2 * k + 1]; }
+  for (int o = 16; o > 0; o >>= 1) {
+    ta += __shfl_xor_sync(0xffffffffu, ta, o);
+    tb += __shfl_xor_sync(0xffffffffu, tb, o);
+  }
+  __shared__ double s[2][32];
+  if ((threadIdx.x & 31) == 0) { s[0][threadIdx.x >> 5] = ta; s[1][threadIdx.x >> 5] = tb; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ta = 0.0; tb = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { ta += s[0][k]; tb += s[1][k]; }
+  }
 }
+
+constexpr unsigned kElemBlocks = 8 * kNumSMs;   // grid of the element-wise passes
 
 // setup_overdensity! data only (src/recon.jl:54-55): δ = (δ/mean - 1)/b.
 __global__ void norm_data_kernel(float* __restrict__ d, size_t N, const double* __restrict__ part, int nb,
                                  float bias) {
   __shared__ float mean_s;
-  if (threadIdx.x == 0) {
-    double ta, tb; total2(part, nb, ta, tb);
-    mean_s = (float)(ta / (double)N);
-  }
+  double ta, tb;
+  total2(part, nb, ta, tb);
+  if (threadIdx.x == 0) mean_s = (float)(ta / (double)N);
   __syncthreads();
   float mean = mean_s;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
@@ -205,8 +235,9 @@ __global__ void norm_randoms_kernel(float* __restrict__ d, const float* __restri
                                     const double* __restrict__ part, int nb, float bias, float ran_min,
                                     float nrand) {
   __shared__ float al_s, thr_s;
+  double ta, tb;
+  total2(part, nb, ta, tb);
   if (threadIdx.x == 0) {
-    double ta, tb; total2(part, nb, ta, tb);
     al_s = (float)(ta / tb);
     thr_s = __fdiv_rn(__fmul_rn(ran_min, (float)tb), nrand);
   }
@@ -237,7 +268,13 @@ int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
 
 __global__ void sumsq_partial_kernel(const float* __restrict__ a, size_t N, double* __restrict__ part) {
   double s = 0.0;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+  const size_t N4 = ((uintptr_t)a % 16 == 0) ? N / 4 : 0;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
+    const float4 u = a4[e];
+    s += (double)((u.x * u.x + u.y * u.y) + (u.z * u.z + u.w * u.w));
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
     s += (double)a[e] * (double)a[e];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   __shared__ double sh[32];
@@ -289,8 +326,7 @@ int smooth_pair(baorec_ctx* ctx, float* a, float* b) {
 int normalize_data(baorec_ctx* ctx, float* delta) {
   sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, nullptr, ctx->N, ctx->dred);
   CKLAUNCH();
-  norm_data_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(delta, ctx->N, ctx->dred, kRedBlocks,
-                                                                   ctx->cfg.bias);
+  norm_data_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(delta, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias);
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -298,7 +334,7 @@ int normalize_data(baorec_ctx* ctx, float* delta) {
 int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr) {
   sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, ran, ctx->N, ctx->dred);
   CKLAUNCH();
-  norm_randoms_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(
+  norm_randoms_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(
       delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr);
   CKLAUNCH();
   return BAOREC_OK;

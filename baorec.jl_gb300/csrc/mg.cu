@@ -25,95 +25,13 @@
 #include <math.h>
 #include <vector>
 
-#include "common.cuh"
+#include "mg_common.cuh"
 
 namespace baorec {
 namespace {
 
-constexpr float kClamp = 0.5f;       // κ for the V-cycle operators
-constexpr int kCoarseSweeps = 200;   // FP64 red-black sweeps on the coarsest level
+constexpr int kCoarseSweeps = 200;   // FP64 red-black sweeps on the coarsest level (fallback)
 constexpr int kCoarseMaxCells = 2048;
-
-struct LG {                           // level geometry passed to kernels
-  int n[3];
-  float cell2[3], icell2[3];
-  const float* P[3];                  // p_a tables (local) — n[a] entries each
-  float pg[3];                        // los / cell (global)
-  float beta;
-  int local;
-  float clamp;                        // > 0: clamp derivative coefficients
-};
-
-struct Coef {
-  float gpx, gpy, gpz, g, pxy, pxz, pyz, dx, dy, dz;
-};
-
-__device__ __forceinline__ Coef coef_at(const LG& G, int i, int j, int k) {
-  float px, py, pz;
-  if (G.local) { px = G.P[0][i]; py = G.P[1][j]; pz = G.P[2][k]; }
-  else { px = G.pg[0]; py = G.pg[1]; pz = G.pg[2]; }
-  Coef c;
-  float px2 = px * px, py2 = py * py, pz2 = pz * pz;
-  c.g = G.beta / (G.cell2[0] * px2 + G.cell2[1] * py2 + G.cell2[2] * pz2);
-  c.gpx = G.icell2[0] + c.g * px2;
-  c.gpy = G.icell2[1] + c.g * py2;
-  c.gpz = G.icell2[2] + c.g * pz2;
-  c.pxy = px * py; c.pxz = px * pz; c.pyz = py * pz;
-  if (G.local) {
-    c.dx = c.g * px; c.dy = c.g * py; c.dz = c.g * pz;
-    if (G.clamp > 0.0f) {
-      c.dx = fminf(fmaxf(c.dx, -G.clamp * c.gpx), G.clamp * c.gpx);
-      c.dy = fminf(fmaxf(c.dy, -G.clamp * c.gpy), G.clamp * c.gpy);
-      c.dz = fminf(fmaxf(c.dz, -G.clamp * c.gpz), G.clamp * c.gpz);
-    }
-  } else {
-    c.dx = c.dy = c.dz = 0.0f;
-  }
-  return c;
-}
-
-struct Nb {                           // the 18 neighbours
-  float xp, xm, yp, ym, zp, zm;
-  float pp0, mm0, mp0, pm0;           // xy plane: (+,+), (−,−), (−,+), (+,−)
-  float p0p, m0m, m0p, p0m;           // xz
-  float _pp, _mm, _mp, _pm;           // yz
-};
-
-__device__ __forceinline__ void cell_ijk(size_t e, const int n[3], int& i, int& j, int& k) {
-  i = (int)(e % (unsigned)n[0]);
-  size_t r = e / (unsigned)n[0];
-  j = (int)(r % (unsigned)n[1]);
-  k = (int)(r / (unsigned)n[1]);
-}
-
-template <typename F>
-__device__ __forceinline__ Nb gather(F get, const int n[3], int i, int j, int k) {
-  int ip = i + 1 == n[0] ? 0 : i + 1, im = i == 0 ? n[0] - 1 : i - 1;
-  int jp = j + 1 == n[1] ? 0 : j + 1, jm = j == 0 ? n[1] - 1 : j - 1;
-  int kp = k + 1 == n[2] ? 0 : k + 1, km = k == 0 ? n[2] - 1 : k - 1;
-  Nb b;
-  b.xp = get(ip, j, k); b.xm = get(im, j, k);
-  b.yp = get(i, jp, k); b.ym = get(i, jm, k);
-  b.zp = get(i, j, kp); b.zm = get(i, j, km);
-  b.pp0 = get(ip, jp, k); b.mm0 = get(im, jm, k); b.mp0 = get(im, jp, k); b.pm0 = get(ip, jm, k);
-  b.p0p = get(ip, j, kp); b.m0m = get(im, j, km); b.m0p = get(im, j, kp); b.p0m = get(ip, j, km);
-  b._pp = get(i, jp, kp); b._mm = get(i, jm, km); b._mp = get(i, jm, kp); b._pm = get(i, jp, km);
-  return b;
-}
-
-// The bracket of src/multigrid.jl:64-79 (neighbour part), reference order.
-__device__ __forceinline__ float offdiag(const Coef& c, const Nb& b, int local) {
-  float s = c.gpx * (b.xp + b.xm) + c.gpy * (b.yp + b.ym) + c.gpz * (b.zp + b.zm) +
-            c.g / 2.0f * (c.pxy * (b.pp0 + b.mm0 - b.mp0 - b.pm0) + c.pxz * (b.p0p + b.m0m - b.m0p - b.p0m) +
-                          c.pyz * (b._pp + b._mm - b._mp - b._pm));
-  if (local) s += c.dx * (b.xp - b.xm) + c.dy * (b.yp - b.ym) + c.dz * (b.zp - b.zm);
-  return s;
-}
-
-__device__ __forceinline__ size_t at(const int n[3], int i, int j, int k) {
-  return (size_t)i + (size_t)n[0] * ((size_t)j + (size_t)n[1] * (size_t)k);
-}
-
 // ---- reference-schedule kernels -------------------------------------------
 
 // One damped-Jacobi sweep (src/multigrid.jl:137-191, 207): out = (1-ω)v + ω jac.
@@ -206,22 +124,6 @@ __global__ void rb_half_kernel(const float* __restrict__ in, float* __restrict__
     out[e] = (rhs[e] - shift + offdiag(c, b, G.local)) / (2.0f * (c.gpx + c.gpy + c.gpz));
   }
 }
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
-  s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// v' = (hi + lo) + e as a renormalised double-float pair.
-__device__ __forceinline__ void df_add(float hi, float lo, float e, float& ohi, float& olo) {
-  float s, err;
-  two_sum(hi, e, s, err);
-  float t = __fadd_rn(lo, err);
-  ohi = __fadd_rn(s, t);
-  olo = __fsub_rn(t, __fsub_rn(ohi, s));
-}
-
 // Accurate residual with the exact (unclamped) operator, fused with the
 // solution update v' = v + e:  r = (f - α) + [neighbour bracket in differences
 // D = v_nb - v_0].  Writes hi', lo', r and FP64 block partials (Σr, Σr²).
@@ -345,6 +247,20 @@ __global__ void coarse_solve_kernel(const float* __restrict__ rhs, float* __rest
   for (int e = threadIdx.x; e < N; e += blockDim.x) v[e] = (float)(sv[e] - vm);
 }
 
+// Coarsest level: v = M rhs with M the top-left block of the inverse of the
+// bordered matrix [[A, 1], [1ᵀ, 0]] (FP64, precomputed on the host), i.e. the
+// mean-free solution of A v + λ1 = rhs.  M 1 = 0, so a constant shift of the
+// right-hand side does not change v.
+__global__ void coarse_dense_kernel(const double* __restrict__ M, const float* __restrict__ rhs, float* __restrict__ v,
+                                    int N) {
+  for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < N; i += blockDim.x * gridDim.x) {
+    double s = 0.0;
+    const double* row = M + (size_t)i * N;
+    for (int j = 0; j < N; ++j) s += row[j] * (double)rhs[j];
+    v[i] = (float)s;
+  }
+}
+
 LG level_geom(const baorec_ctx* ctx, int l, float clamp) {
   const baorec::Level& L = ctx->lev[l];
   LG G;
@@ -380,8 +296,12 @@ unsigned blocks_for(size_t N) {
 }
 
 constexpr int kResBlocks = 2 * kNumSMs;
+constexpr size_t kMaxPartials = kRedCapacity / 2;   // blocks whose (Σr, Σr²) fit the partials buffer
+constexpr int kDenseMaxCells = 512;                  // coarsest levels up to 8^3 use the dense inverse
 
 }  // namespace
+
+int coarse_setup(baorec_ctx* ctx);
 
 // Allocate the level hierarchy and the per-level p tables (x_vec / cell of
 // src/utils.jl:21-25 with that level's cell size, rounded to FP32).
@@ -420,8 +340,131 @@ int mg_update_tables(baorec_ctx* ctx) {
         t[i] = xv / cell;
       }
       CK(cudaMemcpy(L.ax[a], t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+      L.ptab[a] = t;
+    }
+    // Does any cell of this level need its first-derivative coefficient
+    // clamped (|g p_a| > κ gp_a)?  |g p_a| <= β / (c² |p|) and κ gp_a >= κ / c²,
+    // so only cells with |p| < β/κ can: search the cells near the observer.
+    L.needs_clamp = false;
+    if (ctx->cfg.los_mode == BAOREC_LOS_LOCAL) {
+      const float lim = ctx->cfg.beta / kClamp + 1.0f;
+      std::vector<int> near[3];
+      for (int a = 0; a < 3; ++a)
+        for (int i = 0; i < L.n[a]; ++i)
+          if (fabsf(L.ptab[a][i]) < lim) near[a].push_back(i);
+      float c2[3], ic2[3];
+      for (int a = 0; a < 3; ++a) {
+        float cell = ctx->cfg.box_size[a] / (float)L.n[a];
+        c2[a] = cell * cell;
+        ic2[a] = 1.0f / c2[a];
+      }
+      for (int i : near[0])
+        for (int j : near[1])
+          for (int k : near[2]) {
+            const float p[3] = {L.ptab[0][i], L.ptab[1][j], L.ptab[2][k]};
+            const float g = ctx->cfg.beta / (c2[0] * p[0] * p[0] + c2[1] * p[1] * p[1] + c2[2] * p[2] * p[2]);
+            for (int a = 0; a < 3; ++a)
+              if (fabsf(g * p[a]) > kClamp * (ic2[a] + g * p[a] * p[a])) L.needs_clamp = true;
+          }
     }
   }
+  return coarse_setup(ctx);
+}
+
+// Dense FP64 inverse for the coarsest level (the "FP64 coarsest solve"): the
+// matrix of the V-cycle operator (clamped first-derivative coefficients, as
+// the smoother uses), bordered by a row and a column of ones so that the
+// singular periodic system becomes A v + λ1 = rhs with Σv = 0; inverted by
+// Gauss-Jordan elimination with partial pivoting.  Geometry only: recomputed
+// when the box changes.
+int coarse_setup(baorec_ctx* ctx) {
+  if (ctx->coarse_M) { cudaFree(ctx->coarse_M); ctx->coarse_M = nullptr; }
+  // the first level small enough for the dense inverse ends the residual-driven V-cycles
+  ctx->dense_level = -1;
+  for (int l = 0; l < ctx->nlev; ++l)
+    if (ctx->lev[l].N <= (size_t)kDenseMaxCells) { ctx->dense_level = l; break; }
+  if (ctx->dense_level < 0) return BAOREC_OK;
+  const baorec::Level& C = ctx->lev[ctx->dense_level];
+  const int N = (int)C.N;
+  const int n0 = C.n[0], n1 = C.n[1], n2 = C.n[2];
+  const bool local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL;
+  float cell[3], cell2[3], icell2[3], pg[3];
+  std::vector<float> P[3];
+  for (int a = 0; a < 3; ++a) {
+    cell[a] = ctx->cfg.box_size[a] / (float)C.n[a];
+    cell2[a] = cell[a] * cell[a];
+    icell2[a] = 1.0f / cell2[a];
+    pg[a] = ctx->cfg.los[a] / cell[a];
+    P[a].resize(C.n[a]);
+    for (int i = 0; i < C.n[a]; ++i) {
+      float xv = (float)((double)ctx->cfg.box_min[a] + ((double)i + 0.5) * (double)cell[a]);
+      P[a][i] = xv / cell[a];
+    }
+  }
+  const int B = N + 1;
+  std::vector<double> A((size_t)B * B, 0.0), Inv((size_t)B * B, 0.0);
+  auto id = [&](int i, int j, int k) {
+    i = (i + n0) % n0; j = (j + n1) % n1; k = (k + n2) % n2;
+    return i + n0 * (j + n1 * k);
+  };
+  for (int k = 0; k < n2; ++k)
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n0; ++i) {
+        const int r = id(i, j, k);
+        const float px = local ? P[0][i] : pg[0], py = local ? P[1][j] : pg[1], pz = local ? P[2][k] : pg[2];
+        const float g = ctx->cfg.beta / (cell2[0] * px * px + cell2[1] * py * py + cell2[2] * pz * pz);
+        const float gp[3] = {icell2[0] + g * px * px, icell2[1] + g * py * py, icell2[2] + g * pz * pz};
+        float d[3] = {0.0f, 0.0f, 0.0f};
+        if (local) {
+          const float p[3] = {px, py, pz};
+          for (int a = 0; a < 3; ++a) d[a] = fminf(fmaxf(g * p[a], -kClamp * gp[a]), kClamp * gp[a]);
+        }
+        double* row = &A[(size_t)r * B];
+        row[r] += 2.0 * ((double)gp[0] + gp[1] + gp[2]);
+        row[id(i + 1, j, k)] -= (double)gp[0] + d[0];
+        row[id(i - 1, j, k)] -= (double)gp[0] - d[0];
+        row[id(i, j + 1, k)] -= (double)gp[1] + d[1];
+        row[id(i, j - 1, k)] -= (double)gp[1] - d[1];
+        row[id(i, j, k + 1)] -= (double)gp[2] + d[2];
+        row[id(i, j, k - 1)] -= (double)gp[2] - d[2];
+        const double hxy = 0.5 * g * px * py, hxz = 0.5 * g * px * pz, hyz = 0.5 * g * py * pz;
+        row[id(i + 1, j + 1, k)] -= hxy; row[id(i - 1, j - 1, k)] -= hxy;
+        row[id(i - 1, j + 1, k)] += hxy; row[id(i + 1, j - 1, k)] += hxy;
+        row[id(i + 1, j, k + 1)] -= hxz; row[id(i - 1, j, k - 1)] -= hxz;
+        row[id(i - 1, j, k + 1)] += hxz; row[id(i + 1, j, k - 1)] += hxz;
+        row[id(i, j + 1, k + 1)] -= hyz; row[id(i, j - 1, k - 1)] -= hyz;
+        row[id(i, j - 1, k + 1)] += hyz; row[id(i, j + 1, k - 1)] += hyz;
+        row[N] = 1.0;
+        A[(size_t)N * B + r] = 1.0;
+      }
+  for (int i = 0; i < B; ++i) Inv[(size_t)i * B + i] = 1.0;
+  for (int c = 0; c < B; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < B; ++r)
+      if (fabs(A[(size_t)r * B + c]) > fabs(A[(size_t)piv * B + c])) piv = r;
+    if (fabs(A[(size_t)piv * B + c]) < 1e-300) return set_error(ctx, BAOREC_ERR_ARG, "coarsest multigrid level is singular");
+    if (piv != c)
+      for (int q = 0; q < B; ++q) {
+        std::swap(A[(size_t)c * B + q], A[(size_t)piv * B + q]);
+        std::swap(Inv[(size_t)c * B + q], Inv[(size_t)piv * B + q]);
+      }
+    const double inv = 1.0 / A[(size_t)c * B + c];
+    for (int q = 0; q < B; ++q) { A[(size_t)c * B + q] *= inv; Inv[(size_t)c * B + q] *= inv; }
+    for (int r = 0; r < B; ++r) {
+      if (r == c) continue;
+      const double fct = A[(size_t)r * B + c];
+      if (fct == 0.0) continue;
+      for (int q = 0; q < B; ++q) {
+        A[(size_t)r * B + q] -= fct * A[(size_t)c * B + q];
+        Inv[(size_t)r * B + q] -= fct * Inv[(size_t)c * B + q];
+      }
+    }
+  }
+  std::vector<double> M((size_t)N * N);
+  for (int r = 0; r < N; ++r)
+    for (int q = 0; q < N; ++q) M[(size_t)r * N + q] = Inv[(size_t)r * B + q];
+  CK(cudaMalloc(&ctx->coarse_M, M.size() * sizeof(double)));
+  CK(cudaMemcpy(ctx->coarse_M, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice));
   return BAOREC_OK;
 }
 
@@ -524,13 +567,61 @@ int mg_fmg(baorec_ctx* ctx, const float* f, float* phi) {
 // ---- convergent solve -------------------------------------------------------
 
 // One correction V-cycle on level lvl: lev[lvl].v ← V(rhs), rhs = lev[lvl].f - shift.
+// `nsweeps` red-black sweeps on level lvl; the result ends in L.v.
+static int smooth_rb(baorec_ctx* ctx, int lvl, const LG& G, float shift, int nsweeps) {
+  baorec::Level& L = ctx->lev[lvl];
+  const size_t N = L.N;
+  float* a = L.v;
+  float* b = L.r + N;   // ping-pong partner
+  for (int s = 0; s < nsweeps; ++s) {
+    if (tile_ok(L.n)) {
+      CK(launch_rb_sweep(ctx->stream, a, b, L.f, G, shift, L.needs_clamp));
+      ctx->launches++;
+      float* q = a; a = b; b = q;
+    } else {
+      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, b, L.f, G, N, 0, shift);
+      CKLAUNCH();
+      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(b, a, L.f, G, N, 1, shift);
+      CKLAUNCH();
+    }
+  }
+  if (a != L.v) CK(cudaMemcpyAsync(L.v, a, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  return BAOREC_OK;
+}
+
 static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
   baorec::Level& L = ctx->lev[lvl];
   LG G = level_geom(ctx, lvl, kClamp);
   const size_t N = L.N;
   float* v = L.v;
   float* t = L.r + N;   // ping-pong partner
-  if (lvl + 1 == ctx->nlev) {
+  // small levels down to the dense one: one cooperative kernel
+  if (ctx->coarse_M && L.N <= (size_t)kTailMaxCells && ctx->dense_level - lvl + 1 <= kTailMaxLevels) {
+    TailArgs A;
+    A.nl = ctx->dense_level - lvl + 1;
+    A.nu1 = ctx->cfg.nu1;
+    A.nu2 = ctx->cfg.nu2;
+    A.shift0 = shift;
+    A.M = ctx->coarse_M;
+    for (int q = 0; q < A.nl; ++q) {
+      baorec::Level& T = ctx->lev[lvl + q];
+      A.L[q].f = T.f;
+      A.L[q].v = T.v;
+      A.L[q].r = T.r;
+      A.L[q].t = T.r + T.N;
+      A.L[q].G = level_geom(ctx, lvl + q, kClamp);
+      A.L[q].N = (int)T.N;
+    }
+    CK(launch_coarse_tail(ctx->stream, A));
+    ctx->launches++;
+    return BAOREC_OK;
+  }
+  if (lvl == ctx->dense_level || lvl + 1 == ctx->nlev) {
+    if (ctx->coarse_M && lvl == ctx->dense_level) {
+      coarse_dense_kernel<<<(unsigned)((N + 255) / 256), 256, 0, ctx->stream>>>(ctx->coarse_M, L.f, v, (int)N);
+      CKLAUNCH();
+      return BAOREC_OK;
+    }
     if (N <= (size_t)kCoarseMaxCells) {
       // the shift only moves the mean, which the coarse solve removes
       coarse_solve_kernel<<<1, 256, 2 * N * sizeof(double), ctx->stream>>>(L.f, v, G, kCoarseSweeps);
@@ -547,25 +638,19 @@ static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
     return BAOREC_OK;
   }
   CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
-  for (int s = 0; s < ctx->cfg.nu1; ++s) {
-    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
-    CKLAUNCH();
-    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
+  CKS(smooth_rb(ctx, lvl, G, shift, ctx->cfg.nu1));
+  baorec::Level& C = ctx->lev[lvl + 1];
+  if (tile_ok(L.n)) {
+    CK(launch_resid(ctx->stream, v, L.f, L.r, G, shift, L.needs_clamp));
+    ctx->launches++;
+  } else {
+    residual_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, L.f, L.r, G, N, shift);
     CKLAUNCH();
   }
-  baorec::Level& C = ctx->lev[lvl + 1];
-  residual_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, L.f, L.r, G, N, shift);
-  CKLAUNCH();
   CKS(mg_reduce(ctx, C.f, L.r, L.n));
   CKS(vcycle_rb(ctx, lvl + 1, 0.0f));
   CKS(mg_prolong(ctx, v, C.v, L.n, 1));
-  for (int s = 0; s < ctx->cfg.nu2; ++s) {
-    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
-    CKLAUNCH();
-    rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
-    CKLAUNCH();
-  }
-  return BAOREC_OK;
+  return smooth_rb(ctx, lvl, G, shift, ctx->cfg.nu2);
 }
 
 int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st) {
@@ -589,14 +674,22 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   int cycles = 0;
   double rho = 0.0, rho0 = 0.0;
   int status = BAOREC_ERR_NOT_CONVERGED;
+  const bool tile0 = tile_ok(L0.n) && (size_t)tile_blocks(L0.n) <= kMaxPartials;
+  int nparts = kResBlocks;
   for (int it = 0;; ++it) {
-    resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
-                                                          G, N, (float)alpha, ctx->dred);
-    CKLAUNCH();
-    CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kResBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (tile0) {
+      CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
+                          ctx->dred, &nparts));
+      ctx->launches++;
+    } else {
+      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
+                                                            G, N, (float)alpha, ctx->dred);
+      CKLAUNCH();
+    }
+    CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     double s1 = 0.0, s2 = 0.0;
-    for (int q = 0; q < kResBlocks; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
+    for (int q = 0; q < nparts; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
     double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;
     rho = fn2 > 0.0 ? sqrt(s2 / fn2) : 0.0;
     if (it == 0) rho0 = rho;
@@ -641,12 +734,17 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
+  int np = 0;
   auto launch = [&]() {
-    if (which == 0)
+    if (which == 0 && tile_ok(L.n))
+      launch_rb_sweep(ctx->stream, L.v, t, L.f, Gc, 0.0f, L.needs_clamp);
+    else if (which == 0)
       rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, t, L.f, Gc, N, 0, 0.0f);
+    else if (which == 1 && tile_ok(L.n))
+      launch_resid_acc(ctx->stream, L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, 0.0f, ctx->dred, &np);
     else if (which == 1)
-      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, ctx->phi_lo2, L.r, L.f, ctx->phi_hi2, t,
-                                                            L.r, G, N, 0.0f, ctx->dred);
+      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, N,
+                                                            0.0f, ctx->dred);
     else
       jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
   };
@@ -663,8 +761,9 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *avg_ms = ms / reps;
-  // algorithmic bytes: a full smoothing sweep reads v and f and writes v (12 B/cell),
-  // half of it per colour; the accurate residual reads hi, lo, e, f and writes hi, lo, r
-  *bytes = which == 0 ? 6.0 * N : which == 1 ? 28.0 * N : 12.0 * N;
+  // algorithmic bytes: a full smoothing sweep reads v and f and writes v (12 B/cell;
+  // the one-cell kernel does one colour, half of that); the accurate residual
+  // reads hi, lo, e, f and writes hi, lo, r (28 B/cell)
+  *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : which == 1 ? 28.0 * N : 12.0 * N;
   return BAOREC_OK;
 }

@@ -73,9 +73,25 @@ __global__ void readout_kernel(const float* __restrict__ psi, size_t N, const fl
                          xl + n0 * yh + n01 * zh, xh + n0 * yl + n01 * zl, xh + n0 * yl + n01 * zh,
                          xh + n0 * yh + n01 * zl, xh + n0 * yh + n01 * zh};
     if (mode == 2) { o0[q] = tri(psi, o, dx, dy, dz, ux, uy, uz); continue; }
+    // Ψ is interleaved (x, y, z, pad) per cell: one 16-byte load per corner
+    const float4* p4 = reinterpret_cast<const float4*>(psi);
+    const float4 c0 = __ldg(p4 + o[0]), c1 = __ldg(p4 + o[1]), c2 = __ldg(p4 + o[2]), c3 = __ldg(p4 + o[3]);
+    const float4 c4 = __ldg(p4 + o[4]), c5 = __ldg(p4 + o[5]), c6 = __ldg(p4 + o[6]), c7 = __ldg(p4 + o[7]);
     float s[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) s[a] = tri(psi + a * N, o, dx, dy, dz, ux, uy, uz);
+    for (int a = 0; a < 3; ++a) {
+      auto C = [&](const float4& v) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); };
+      float t = __fmul_rn(__fmul_rn(__fmul_rn(C(c0), dx), dy), dz);
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c1), dx), dy), uz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c2), dx), uy), dz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c3), dx), uy), uz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c4), ux), dy), dz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c5), ux), dy), uz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c6), ux), uy), dz));
+      t = __fadd_rn(t, __fmul_rn(__fmul_rn(__fmul_rn(C(c7), ux), uy), uz));
+      s[a] = t;
+    }
+    (void)N;
     if (field != 0) {
       float l0, l1, l2;
       if (G.local) {
