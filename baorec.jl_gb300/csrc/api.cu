@@ -100,6 +100,8 @@ static int validate(baorec_ctx* ctx, const baorec_config* c) {
     if (c->n[a] < 2 || c->n[a] > 4096) return set_error(ctx, BAOREC_ERR_ARG, "mesh size n[%d]=%d out of range", a, c->n[a]);
   }
   if (c->n[0] % 2) return set_error(ctx, BAOREC_ERR_ARG, "n[0] must be even (real-to-complex layout)");
+  if ((double)c->n[0] * c->n[1] * c->n[2] >= 2147483648.0)
+    return set_error(ctx, BAOREC_ERR_ARG, "mesh of %d x %d x %d cells exceeds 2^31 cells", c->n[0], c->n[1], c->n[2]);
   for (int a = 0; a < 3; ++a)
     if (!(c->box_size[a] > 0.0f)) return set_error(ctx, BAOREC_ERR_ARG, "box_size[%d] must be positive", a);
   if (!(c->bias != 0.0f)) return set_error(ctx, BAOREC_ERR_ARG, "bias must be non-zero");
@@ -180,7 +182,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
   CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CKC(cudaMalloc(&ctx->mesh3, ctx->N * 4 * 3));
   ctx->result = ctx->mesh3;
-  CKC(cudaMalloc(&ctx->psi, ctx->N * 4 * 6));
+  CKC(cudaMalloc(&ctx->psi, ctx->N * 4 * 7));   // 6 iterative parts, or interleaved Ψ (4N) + its planes (3N)
   CKC(cudaMalloc(&ctx->ck, ctx->Nk * sizeof(cufftComplex) * 6));
   for (int a = 0; a < 3; ++a) CKC(cudaMalloc(&ctx->xvec[a], (size_t)cfg->n[a] * 4));
   CKC(cudaMalloc(&ctx->dred, kRedCapacity * sizeof(double)));
@@ -193,7 +195,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
       (st = make_plan(ctx, &ctx->plan_r2c2, CUFFT_R2C, 2, &maxw)) ||
       (st = make_plan(ctx, &ctx->plan_c2r, CUFFT_C2R, 1, &maxw)) ||
       (st = make_plan(ctx, &ctx->plan_c2r2, CUFFT_C2R, 2, &maxw)) ||
-      (st = make_plan(ctx, &ctx->plan_c2r3, CUFFT_C2R, 3, &maxw, true)) ||
+      (st = make_plan(ctx, &ctx->plan_c2r3, CUFFT_C2R, 3, &maxw)) ||
       (st = make_plan(ctx, &ctx->plan_c2r6, CUFFT_C2R, 6, &maxw)))
     return fail(st);
   CKC(cudaMalloc(&ctx->fft_work, maxw > 0 ? maxw : 256));

@@ -372,14 +372,25 @@ int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter) {
   return BAOREC_OK;
 }
 
-int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3) {
+// (x, y, z) planes -> one mesh of 4-float cells (x, y, z, 0), the read-out layout.
+__global__ void interleave3_kernel(const float* __restrict__ p, float4* __restrict__ out, size_t N) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    out[e] = make_float4(p[e], p[e + N], p[e + 2 * N], 0.0f);
+}
+
+// Ψ (iterative: i k δ_k / k²; multigrid: i k φ_k) as an interleaved mesh at
+// psi4[0, 4N); psi4[4N, 7N) holds the three planes on the way.
+int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
   KGeom g = kgeom_of(ctx);
   // cuFFT's R2C reads but does not modify its input
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
   grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g,
                                                                ctx->cfg.method == BAOREC_ITERATIVE ? 1 : 0);
   CKLAUNCH();
-  CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, psi3));
+  float* planes = psi4 + 4 * ctx->N;
+  CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, planes));
+  interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
+  CKLAUNCH();
   return BAOREC_OK;
 }
 

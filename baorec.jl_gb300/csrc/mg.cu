@@ -674,7 +674,10 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   int cycles = 0;
   double rho = 0.0, rho0 = 0.0;
   int status = BAOREC_ERR_NOT_CONVERGED;
-  const bool tile0 = tile_ok(L0.n) && (size_t)tile_blocks(L0.n) <= kMaxPartials;
+  // the tile kernel reads the solution pair in 16-byte chunks
+  const bool aligned = (uintptr_t)phi % 16 == 0 && (uintptr_t)ctx->phi_lo % 16 == 0 && (uintptr_t)ctx->phi_hi2 % 16 == 0 &&
+                       (uintptr_t)ctx->phi_lo2 % 16 == 0;
+  const bool tile0 = aligned && tile_ok(L0.n) && (size_t)tile_blocks(L0.n) <= kMaxPartials;
   int nparts = kResBlocks;
   for (int it = 0;; ++it) {
     if (tile0) {

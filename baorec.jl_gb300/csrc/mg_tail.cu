@@ -25,13 +25,40 @@ __device__ __forceinline__ void ijk_of(int e, const int n[3], int& i, int& j, in
 
 __device__ __forceinline__ int id3(const int n[3], int i, int j, int k) { return i + n[0] * (j + n[1] * k); }
 
-// (rhs - shift + neighbours(in)) / diag for cell e of level T.
+// coef_at with fast division (the tail is a preconditioner)
+__device__ __forceinline__ Coef coef_tail(const LG& G, int i, int j, int k) {
+  float px, py, pz;
+  if (G.local) { px = G.P[0][i]; py = G.P[1][j]; pz = G.P[2][k]; }
+  else { px = G.pg[0]; py = G.pg[1]; pz = G.pg[2]; }
+  Coef c;
+  const float px2 = px * px, py2 = py * py, pz2 = pz * pz;
+  c.g = __fdividef(G.beta, G.cell2[0] * px2 + G.cell2[1] * py2 + G.cell2[2] * pz2);
+  c.gpx = G.icell2[0] + c.g * px2;
+  c.gpy = G.icell2[1] + c.g * py2;
+  c.gpz = G.icell2[2] + c.g * pz2;
+  c.pxy = px * py; c.pxz = px * pz; c.pyz = py * pz;
+  if (G.local) {
+    c.dx = fminf(fmaxf(c.g * px, -G.clamp * c.gpx), G.clamp * c.gpx);
+    c.dy = fminf(fmaxf(c.g * py, -G.clamp * c.gpy), G.clamp * c.gpy);
+    c.dz = fminf(fmaxf(c.g * pz, -G.clamp * c.gpz), G.clamp * c.gpz);
+  } else {
+    c.dx = c.dy = c.dz = 0.0f;
+  }
+  return c;
+}
+
+// (rhs - shift + neighbours(in)) / diag for cell e of level T; in == nullptr
+// means a zero field (the first half sweep after zeroing the correction).
 __device__ __forceinline__ float gs_cell(const TailLevel& T, const float* __restrict__ in, int e, float shift) {
   int i, j, k;
   ijk_of(e, T.G.n, i, j, k);
-  const Coef c = coef_at(T.G, i, j, k);
-  const Nb b = gather([&](int a, int bb, int cc) { return in[id3(T.G.n, a, bb, cc)]; }, T.G.n, i, j, k);
-  return (T.f[e] - shift + offdiag(c, b, T.G.local)) / (2.0f * (c.gpx + c.gpy + c.gpz));
+  const Coef c = coef_tail(T.G, i, j, k);
+  float o = 0.0f;
+  if (in) {
+    const Nb b = gather([&](int a, int bb, int cc) { return in[id3(T.G.n, a, bb, cc)]; }, T.G.n, i, j, k);
+    o = offdiag(c, b, T.G.local);
+  }
+  return __fdividef(T.f[e] - shift + o, 2.0f * (c.gpx + c.gpy + c.gpz));
 }
 
 __global__ void coarse_tail_kernel(TailArgs A) {
@@ -43,7 +70,7 @@ __global__ void coarse_tail_kernel(TailArgs A) {
     for (int e = tid; e < T.N; e += nth) {
       int i, j, k;
       ijk_of(e, T.G.n, i, j, k);
-      out[e] = (((i + j + k) & 1) == colour) ? gs_cell(T, in, e, shift) : in[e];
+      out[e] = (((i + j + k) & 1) == colour) ? gs_cell(T, in, e, shift) : (in ? in[e] : 0.0f);
     }
     grid.sync();
   };
@@ -51,11 +78,14 @@ __global__ void coarse_tail_kernel(TailArgs A) {
   for (int l = 0; l < last; ++l) {
     const TailLevel& T = A.L[l];
     const float shift = l == 0 ? A.shift0 : 0.0f;
-    for (int e = tid; e < T.N; e += nth) T.v[e] = 0.0f;
-    grid.sync();
+    // the correction starts at zero: the first half sweep reads no field
     for (int s = 0; s < A.nu1; ++s) {
-      half_sweep(T, T.v, T.t, 0, shift);
+      half_sweep(T, s == 0 ? nullptr : T.v, T.t, 0, shift);
       half_sweep(T, T.t, T.v, 1, shift);
+    }
+    if (A.nu1 == 0) {
+      for (int e = tid; e < T.N; e += nth) T.v[e] = 0.0f;
+      grid.sync();
     }
     // residual r = rhs - shift - A v
     for (int e = tid; e < T.N; e += nth) {

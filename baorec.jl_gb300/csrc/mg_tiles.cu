@@ -1,12 +1,15 @@
 // Shared-memory tile kernels of the residual-driven multigrid solver.
 //
-// A block owns a TX x TY x TZ tile of a periodic level mesh.  It stages the
-// tile plus a halo (2 cells for the red-black sweep, 1 for residuals) in
-// shared memory with row-coalesced loads, computes from shared memory and
-// writes the tile.  Every launch is specialised on the line-of-sight mode
-// (local: per-cell coefficients from p tables; global: uniform coefficients)
-// and on whether the level has cells next to the observer whose
-// first-derivative coefficients need clamping.
+// A block owns a 32 x TY x TZ tile of a periodic level mesh.  It stages the
+// tile plus a halo (y/z: 2 cells for the red-black sweep, 1 for residuals;
+// x: 4 cells, so that every window row is ten aligned 16-byte chunks) in
+// shared memory.  Each chunk is either wholly inside the mesh or wholly
+// wrapped, and the wrapped offsets of the window rows are tabulated once per
+// block, so a chunk costs a handful of instructions.  Right-hand sides have
+// no reuse and are read straight from global memory.  Every launch is
+// specialised on the line-of-sight mode (local: per-cell coefficients from p
+// tables; global: uniform coefficients) and on whether the level has cells
+// next to the observer whose first-derivative coefficients need clamping.
 #include <mutex>
 
 #include "mg_common.cuh"
@@ -14,36 +17,51 @@
 namespace baorec {
 namespace {
 
-constexpr int TX = 32, NT = 512;   // tile width and threads per block (tile height/depth: template)
-constexpr int NWARP = NT / 32;
+constexpr int TX = 32, XH = 4, WX = TX + 2 * XH;   // tile width, x-halo, window pitch
+constexpr int NT = 512, NWARP = NT / 32;           // threads per block
+constexpr int CH = WX / 4;                         // 16-byte chunks per window row
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Periodic window [x0-H, x0+TX+H) x [y0-H, ..) x [z0-H, ..) of g into s (pitch TX+2H).
-template <int H, int TY, int TZ>
-__device__ __forceinline__ void load_window(float* __restrict__ s, const float* __restrict__ g, int x0, int y0, int z0,
-                                            const int n[3]) {
-  constexpr int SX = TX + 2 * H, SY = TY + 2 * H, SZ = TZ + 2 * H;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gxa = wrapi(x0 - H + lane, n[0]);
-  const bool has_b = lane < SX - 32;
-  const int gxb = has_b ? wrapi(x0 - H + 32 + lane, n[0]) : 0;
-  const size_t plane = (size_t)n[0] * n[1];
-  for (int row = warp; row < SY * SZ; row += NWARP) {
-    const int ly = row % SY, lz = row / SY;
-    const float* gr = g + (size_t)n[0] * wrapi(y0 - H + ly, n[1]) + plane * wrapi(z0 - H + lz, n[2]);
-    float* sr = s + row * SX;
-    sr[lane] = __ldg(gr + gxa);
-    if (has_b) sr[32 + lane] = __ldg(gr + gxb);
+// Row offsets (ix = 0 of the row) of the periodic window rows
+// y in [y0-HY, y0+TY+HY), z in [z0-HY, z0+TZ+HY).
+template <int HY, int TY, int TZ>
+__device__ __forceinline__ void row_table(int* __restrict__ ro, int y0, int z0, const int n[3]) {
+  constexpr int SY = TY + 2 * HY, SZ = TZ + 2 * HY;
+  for (int r = threadIdx.x; r < SY * SZ; r += NT) {
+    const int ly = r % SY, lz = r / SY;
+    ro[r] = n[0] * (wrapi(y0 - HY + ly, n[1]) + n[1] * wrapi(z0 - HY + lz, n[2]));
   }
 }
 
-template <int H, int TY, int TZ>
+// Window chunks: s[row][4c .. 4c+3] = g[row offset + wrap(x0 - XH + 4c) ..].
+template <int HY, int TY, int TZ>
+__device__ __forceinline__ void load_rows(float* __restrict__ s, const int* __restrict__ ro, const float* __restrict__ g,
+                                          int x0, int n0) {
+  constexpr int ROWS = (TY + 2 * HY) * (TZ + 2 * HY);
+  constexpr int K = (ROWS * CH + NT - 1) / NT;   // chunks per thread, all in flight together
+  float4* s4 = reinterpret_cast<float4*>(s);
+  float4 v[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = threadIdx.x + k * NT;
+    if (t < ROWS * CH) {
+      const int row = t / CH, c = t - CH * row;
+      v[k] = __ldg(reinterpret_cast<const float4*>(g + ro[row] + wrapi(x0 - XH + 4 * c, n0)));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = threadIdx.x + k * NT;
+    if (t < ROWS * CH) s4[t] = v[k];
+  }
+}
+
+template <int HY, int TY, int TZ>
 __device__ __forceinline__ void load_ptab(float* __restrict__ sp, const LG& G, int x0, int y0, int z0) {
-  constexpr int SX = TX + 2 * H;
-  for (int q = threadIdx.x; q < TX + 2 * H; q += NT) sp[q] = G.P[0][wrapi(x0 - H + q, G.n[0])];
-  for (int q = threadIdx.x; q < TY + 2 * H; q += NT) sp[SX + q] = G.P[1][wrapi(y0 - H + q, G.n[1])];
-  for (int q = threadIdx.x; q < TZ + 2 * H; q += NT) sp[2 * SX + q] = G.P[2][wrapi(z0 - H + q, G.n[2])];
+  for (int q = threadIdx.x; q < WX; q += NT) sp[q] = G.P[0][wrapi(x0 - XH + q, G.n[0])];
+  for (int q = threadIdx.x; q < TY + 2 * HY; q += NT) sp[WX + q] = G.P[1][wrapi(y0 - HY + q, G.n[1])];
+  for (int q = threadIdx.x; q < TZ + 2 * HY; q += NT) sp[2 * WX + q] = G.P[2][wrapi(z0 - HY + q, G.n[2])];
 }
 
 // Operator coefficients of one cell (approximate division: smoother and
@@ -78,8 +96,9 @@ __device__ __forceinline__ Cf coef_fast(float px, float py, float pz, const LG& 
 }
 
 // Neighbour sum (the bracket of the operator) at shared index q.
-template <bool LOCAL, int SX, int SXY>
+template <bool LOCAL, int SXY>
 __device__ __forceinline__ float nbr(const float* __restrict__ s, int q, const Cf& c) {
+  constexpr int SX = WX;
   const float xp = s[q + 1], xm = s[q - 1], yp = s[q + SX], ym = s[q - SX], zp = s[q + SXY], zm = s[q - SXY];
   float o = c.gpx * (xp + xm) + c.gpy * (yp + ym) + c.gpz * (zp + zm) +
             c.hxy * ((s[q + 1 + SX] + s[q - 1 - SX]) - (s[q - 1 + SX] + s[q + 1 - SX])) +
@@ -92,26 +111,26 @@ __device__ __forceinline__ float nbr(const float* __restrict__ s, int q, const C
 // One red-black Gauss-Seidel sweep, both colours in one pass, out of place.
 // Red cells of the tile and of a one-cell ring around it are updated from the
 // old window; then the black cells of the tile from the red-updated window.
+// Window frame: x = x0 - 4 + lx, y = y0 - 2 + ly, z = z0 - 2 + lz; all three
+// origins are even, so window parity is mesh parity.
 template <bool LOCAL, bool CLAMP, int TY, int TZ>
-__global__ void __launch_bounds__(NT) rb_sweep_kernel(const float* __restrict__ vin, float* __restrict__ vout,
-                                                      const float* __restrict__ rhs, LG G, float shift) {
-  constexpr int SX = TX + 4, SY = TY + 4, SZ = TZ + 4, SXY = SX * SY;
-  constexpr int FX = TX + 2, FY = TY + 2, FXY = FX * FY;
-  extern __shared__ float smem[];
-  float* sv = smem;                         // SX*SY*SZ
-  float* sf = sv + SX * SY * SZ;            // FX*FY*(TZ+2)
-  float* sp = sf + FX * FY * (TZ + 2);      // 3*SX
+__global__ void __launch_bounds__(NT, 2) rb_sweep_kernel(const float* __restrict__ vin, float* __restrict__ vout,
+                                                         const float* __restrict__ rhs, LG G, float shift) {
+  constexpr int SY = TY + 4, SZ = TZ + 4, SXY = WX * SY;
+  extern __shared__ __align__(16) float smem[];
+  float* sv = smem;                              // WX*SY*SZ
+  int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);   // SY*SZ
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);    // 3*WX
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  load_window<2, TY, TZ>(sv, vin, x0, y0, z0, G.n);
-  load_window<1, TY, TZ>(sf, rhs, x0, y0, z0, G.n);
+  row_table<2, TY, TZ>(ro, y0, z0, G.n);
   if (LOCAL) load_ptab<2, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
+  load_rows<2, TY, TZ>(sv, ro, vin, x0, G.n[0]);
   Cf cu;
   if (!LOCAL) cu = coef_fast<false, false>(G.pg[0], G.pg[1], G.pg[2], G);
   __syncthreads();
-  // red: 1 <= l < S-1, (lx+ly+lz) even (the tile origin and halo are even, so
-  // window parity is mesh parity)
-  constexpr int RPR = (SX - 2) / 2, RROWY = SY - 2, NRED = RPR * RROWY * (SZ - 2);
-  constexpr int KR = (NRED + NT - 1) / NT;
+  // red: rows ly, lz in [1, S-1); cells lx in [3, 37) with even lx+ly+lz (17 per row)
+  constexpr int RPR = 17, RROWY = SY - 2, NRED = RPR * RROWY * (SZ - 2), KR = (NRED + NT - 1) / NT;
   float nv[KR];
   int qr[KR];
 #pragma unroll
@@ -119,14 +138,14 @@ __global__ void __launch_bounds__(NT) rb_sweep_kernel(const float* __restrict__ 
     const int c = threadIdx.x + k * NT;
     qr[k] = -1;
     if (c < NRED) {
-      const int t = c % RPR, row = c / RPR;
+      const int row = c / RPR, t = c - RPR * row;
       const int ly = 1 + row % RROWY, lz = 1 + row / RROWY;
-      const int lx = 1 + ((ly + lz + 1) & 1) + 2 * t;
-      const int q = lx + SX * ly + SXY * lz;
+      const int lx = 3 + ((ly + lz + 1) & 1) + 2 * t;
+      const int q = lx + WX * ly + SXY * lz;
       qr[k] = q;
-      const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[SX + ly], sp[2 * SX + lz], G) : cu;
-      const float f = sf[(lx - 1) + FX * (ly - 1) + FXY * (lz - 1)] - shift;
-      nv[k] = __fdividef(f + nbr<LOCAL, SX, SXY>(sv, q, cf), cf.diag);
+      const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
+      const float f = __ldg(rhs + ro[ly + SY * lz] + wrapi(x0 - XH + lx, G.n[0])) - shift;
+      nv[k] = __fdividef(f + nbr<LOCAL, SXY>(sv, q, cf), cf.diag);
     }
   }
   __syncthreads();
@@ -134,32 +153,31 @@ __global__ void __launch_bounds__(NT) rb_sweep_kernel(const float* __restrict__ 
   for (int k = 0; k < KR; ++k)
     if (qr[k] >= 0) sv[qr[k]] = nv[k];
   __syncthreads();
-  // black: tile cells (2 <= l < S-2) with odd (lx+ly+lz)
-  constexpr int BPR = TX / 2, NBLK = BPR * TY * TZ, KB = NBLK / NT;
+  // black: tile rows ly, lz in [2, S-2); cells lx in [4, 36) with odd lx+ly+lz (16 per row)
+  constexpr int NBLK = 16 * TY * TZ, KB = NBLK / NT;
   static_assert(NBLK % NT == 0, "black cells must divide evenly");
   float nb[KB];
   int qb[KB];
 #pragma unroll
   for (int k = 0; k < KB; ++k) {
     const int c = threadIdx.x + k * NT;
-    const int t = c % BPR, row = c / BPR;
+    const int row = c >> 4, t = c & 15;
     const int ly = 2 + row % TY, lz = 2 + row / TY;
-    const int lx = 2 + ((ly + lz + 1) & 1) + 2 * t;
-    const int q = lx + SX * ly + SXY * lz;
+    const int lx = 4 + ((ly + lz + 1) & 1) + 2 * t;
+    const int q = lx + WX * ly + SXY * lz;
     qb[k] = q;
-    const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[SX + ly], sp[2 * SX + lz], G) : cu;
-    const float f = sf[(lx - 1) + FX * (ly - 1) + FXY * (lz - 1)] - shift;
-    nb[k] = __fdividef(f + nbr<LOCAL, SX, SXY>(sv, q, cf), cf.diag);
+    const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
+    const float f = __ldg(rhs + ro[ly + SY * lz] + x0 - XH + lx) - shift;
+    nb[k] = __fdividef(f + nbr<LOCAL, SXY>(sv, q, cf), cf.diag);
   }
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < KB; ++k) sv[qb[k]] = nb[k];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t plane = (size_t)G.n[0] * G.n[1];
   for (int row = warp; row < TY * TZ; row += NWARP) {
-    const int ly = row % TY, lz = row / TY;
-    vout[(size_t)(x0 + lane) + (size_t)G.n[0] * (y0 + ly) + plane * (z0 + lz)] = sv[2 + lane + SX * (ly + 2) + SXY * (lz + 2)];
+    const int ly = 2 + row % TY, lz = 2 + row / TY;
+    vout[ro[ly + SY * lz] + x0 + lane] = sv[XH + lane + WX * ly + SXY * lz];
   }
 }
 
@@ -167,29 +185,31 @@ __global__ void __launch_bounds__(NT) rb_sweep_kernel(const float* __restrict__ 
 template <bool LOCAL, bool CLAMP, int TY, int TZ>
 __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
                                                    float* __restrict__ r, LG G, float shift) {
-  constexpr int SX = TX + 2, SY = TY + 2, SZ = TZ + 2, SXY = SX * SY;
-  extern __shared__ float smem[];
+  constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY;
+  extern __shared__ __align__(16) float smem[];
   float* sv = smem;
-  float* sp = sv + SX * SY * SZ;
+  int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  load_window<1, TY, TZ>(sv, e, x0, y0, z0, G.n);
+  row_table<1, TY, TZ>(ro, y0, z0, G.n);
   if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
+  load_rows<1, TY, TZ>(sv, ro, e, x0, G.n[0]);
   Cf cu;
   if (!LOCAL) cu = coef_fast<false, false>(G.pg[0], G.pg[1], G.pg[2], G);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t plane = (size_t)G.n[0] * G.n[1];
   for (int row = warp; row < TY * TZ; row += NWARP) {
-    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = 1 + lane;
-    const int q = lx + SX * ly + SXY * lz;
-    const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[SX + ly], sp[2 * SX + lz], G) : cu;
-    const size_t o = (size_t)(x0 + lane) + (size_t)G.n[0] * (y0 + ly - 1) + plane * (z0 + lz - 1);
-    r[o] = (rhs[o] - shift) - (cf.diag * sv[q] - nbr<LOCAL, SX, SXY>(sv, q, cf));
+    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
+    const int q = lx + WX * ly + SXY * lz;
+    const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
+    const int o = ro[ly + SY * lz] + x0 + lane;
+    r[o] = (__ldg(rhs + o) - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
   }
 }
 
-// Accurate residual with solution update: the window of (hi, lo) + e is
-// turned into the updated double-float pair as it is loaded; then
+// Accurate residual with solution update: each window chunk of (hi, lo) + e
+// becomes the updated double-float pair as it is loaded; then
 // r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
 // operator, whose coefficients are evaluated with IEEE round-to-nearest
 // operations in the reference's order.  Per-block (Σr, Σr²) to part.
@@ -199,41 +219,57 @@ __global__ void __launch_bounds__(NT) resid_acc_kernel(const float* __restrict__
                                                        float* __restrict__ ohi, float* __restrict__ olo,
                                                        float* __restrict__ r, LG G, float alpha,
                                                        double* __restrict__ part) {
-  constexpr int SX = TX + 2, SY = TY + 2, SZ = TZ + 2, SXY = SX * SY, SN = SX * SY * SZ;
-  extern __shared__ float smem[];
+  constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY, SN = WX * SY * SZ;
+  extern __shared__ __align__(16) float smem[];
   float* sh = smem;
   float* sl = sh + SN;
-  float* sp = sl + SN;
+  int* ro = reinterpret_cast<int*>(sl + SN);
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  row_table<1, TY, TZ>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
   {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gxa = wrapi(x0 - 1 + lane, G.n[0]);
-    const bool has_b = lane < SX - 32;
-    const int gxb = has_b ? wrapi(x0 - 1 + 32 + lane, G.n[0]) : 0;
-    const size_t plane = (size_t)G.n[0] * G.n[1];
-    for (int row = warp; row < SY * SZ; row += NWARP) {
-      const int ly = row % SY, lz = row / SY;
-      const size_t base = (size_t)G.n[0] * wrapi(y0 - 1 + ly, G.n[1]) + plane * wrapi(z0 - 1 + lz, G.n[2]);
+    float4* sh4 = reinterpret_cast<float4*>(sh);
+    float4* sl4 = reinterpret_cast<float4*>(sl);
+    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = 4;   // B chunks of each array in flight
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        if (half && !has_b) break;
-        const size_t gidx = base + (half ? gxb : gxa);
-        float h = __ldg(hi + gidx), l = __ldg(lo + gidx);
-        if (ec) df_add(h, l, __ldg(ec + gidx), h, l);
-        sh[row * SX + half * 32 + lane] = h;
-        sl[row * SX + half * 32 + lane] = l;
+    for (int k0 = 0; k0 < K; k0 += B) {
+      float4 h[B], l[B], e[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = threadIdx.x + (k0 + b) * NT;
+        if (k0 + b < K && t < TOT) {
+          const int row = t / CH, c = t - CH * row;
+          const int o = ro[row] + wrapi(x0 - XH + 4 * c, G.n[0]);
+          h[b] = __ldg(reinterpret_cast<const float4*>(hi + o));
+          l[b] = __ldg(reinterpret_cast<const float4*>(lo + o));
+          if (ec) e[b] = __ldg(reinterpret_cast<const float4*>(ec + o));
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = threadIdx.x + (k0 + b) * NT;
+        if (k0 + b < K && t < TOT) {
+          if (ec) {
+            df_add(h[b].x, l[b].x, e[b].x, h[b].x, l[b].x);
+            df_add(h[b].y, l[b].y, e[b].y, h[b].y, l[b].y);
+            df_add(h[b].z, l[b].z, e[b].z, h[b].z, l[b].z);
+            df_add(h[b].w, l[b].w, e[b].w, h[b].w, l[b].w);
+          }
+          sh4[t] = h[b];
+          sl4[t] = l[b];
+        }
       }
     }
   }
-  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
   __syncthreads();
   float s1 = 0.0f, s2 = 0.0f;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t plane = (size_t)G.n[0] * G.n[1];
   for (int row = warp; row < TY * TZ; row += NWARP) {
-    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = 1 + lane;
-    const int q = lx + SX * ly + SXY * lz;
-    const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[SX + ly] : G.pg[1], pz = LOCAL ? sp[2 * SX + lz] : G.pg[2];
+    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
+    const int q = lx + WX * ly + SXY * lz;
+    const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1], pz = LOCAL ? sp[2 * WX + lz] : G.pg[2];
     const float px2 = __fmul_rn(px, px), py2 = __fmul_rn(py, py), pz2 = __fmul_rn(pz, pz);
     const float den = __fadd_rn(__fadd_rn(__fmul_rn(G.cell2[0], px2), __fmul_rn(G.cell2[1], py2)),
                                 __fmul_rn(G.cell2[2], pz2));
@@ -243,6 +279,7 @@ __global__ void __launch_bounds__(NT) resid_acc_kernel(const float* __restrict__
     const float gpz = __fadd_rn(G.icell2[2], __fmul_rn(g, pz2));
     const float h0 = sh[q], l0 = sl[q];
     auto D = [&](int u) { return __fadd_rn(__fsub_rn(sh[u], h0), __fsub_rn(sl[u], l0)); };
+    constexpr int SX = WX;
     const float dxp = D(q + 1), dxm = D(q - 1), dyp = D(q + SX), dym = D(q - SX), dzp = D(q + SXY), dzm = D(q - SXY);
     float br = gpx * (dxp + dxm) + gpy * (dyp + dym) + gpz * (dzp + dzm) +
                g / 2.0f *
@@ -250,12 +287,12 @@ __global__ void __launch_bounds__(NT) resid_acc_kernel(const float* __restrict__
                     __fmul_rn(px, pz) * ((D(q + 1 + SXY) + D(q - 1 - SXY)) - (D(q - 1 + SXY) + D(q + 1 - SXY))) +
                     __fmul_rn(py, pz) * ((D(q + SX + SXY) + D(q - SX - SXY)) - (D(q - SX + SXY) + D(q + SX - SXY))));
     if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
-    const size_t o = (size_t)(x0 + lane) + (size_t)G.n[0] * (y0 + ly - 1) + plane * (z0 + lz - 1);
-    const float rv = (f[o] - alpha) + br;
+    const int o = ro[ly + SY * lz] + x0 + lane;
+    const float rv = (__ldg(f + o) - alpha) + br;
     ohi[o] = h0;
     olo[o] = l0;
     r[o] = rv;
-    s1 += rv;          // FP32 over this thread's 16 cells; FP64 across warps and blocks
+    s1 += rv;          // FP32 over this thread's cells; FP64 across warps and blocks
     s2 += rv * rv;
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -274,18 +311,305 @@ __global__ void __launch_bounds__(NT) resid_acc_kernel(const float* __restrict__
   }
 }
 
-template <int TY, int TZ>
-constexpr size_t sweep_smem() {
-  return sizeof(float) * ((TX + 4) * (TY + 4) * (TZ + 4) + (TX + 2) * (TY + 2) * (TZ + 2) + 3 * (TX + 4));
+// ---- packed FP32x2 arithmetic: two cells per instruction ---------------------
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 P2(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
 }
-template <int TY, int TZ>
-constexpr size_t resid_smem() { return sizeof(float) * ((TX + 2) * (TY + 2) * (TZ + 2) + 3 * (TX + 2)); }
-template <int TY, int TZ>
-constexpr size_t acc_smem() { return sizeof(float) * (2 * (TX + 2) * (TY + 2) * (TZ + 2) + 3 * (TX + 2)); }
+__device__ __forceinline__ void U2(f2 r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ f2 B2(float a) { return P2(a, a); }
+#define BAOREC_F2OP(name, op)                                                 \
+  __device__ __forceinline__ f2 name(f2 a, f2 b) {                            \
+    f2 d;                                                                     \
+    asm(op ".rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));               \
+    return d;                                                                 \
+  }
+BAOREC_F2OP(add2, "add")
+BAOREC_F2OP(sub2, "sub")
+BAOREC_F2OP(mul2, "mul")
+#undef BAOREC_F2OP
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 rcp2(f2 a) {
+  float x, y;
+  U2(a, x, y);
+  return P2(__frcp_rn(x), __frcp_rn(y));
+}
 
-// Tile height/depth for a level: 16 x 16 when that still gives >= 2 blocks per SM, else 8 x 8.
+// Gauss-Seidel values of two cells (shared indices qa, qb) that share p_y:
+// (rhs + neighbours) / diagonal, clamped operator, fast reciprocals.
+template <bool LOCAL, bool CLAMP, int SXY>
+__device__ __forceinline__ f2 gs_two(const float* __restrict__ s, int qa, int qb, f2 fr, f2 Px, float py, f2 Pz,
+                                     const Cf& cu, const LG& G) {
+  constexpr int SX = WX;
+  auto L2 = [&](int off) { return P2(s[qa + off], s[qb + off]); };
+  const f2 xp = L2(1), xm = L2(-1), yp = L2(SX), ym = L2(-SX), zp = L2(SXY), zm = L2(-SXY);
+  const f2 Sx = add2(xp, xm), Sy = add2(yp, ym), Sz = add2(zp, zm);
+  const f2 Xxy = sub2(add2(L2(1 + SX), L2(-1 - SX)), add2(L2(-1 + SX), L2(1 - SX)));
+  const f2 Xxz = sub2(add2(L2(1 + SXY), L2(-1 - SXY)), add2(L2(-1 + SXY), L2(1 - SXY)));
+  const f2 Xyz = sub2(add2(L2(SX + SXY), L2(-SX - SXY)), add2(L2(-SX + SXY), L2(SX - SXY)));
+  f2 gpx, gpy, gpz, hxy, hxz, hyz;
+  if (LOCAL) {
+    const f2 px2 = mul2(Px, Px), pz2 = mul2(Pz, Pz);
+    const float py2 = py * py;
+    const f2 den = fma2(B2(G.cell2[0]), px2, fma2(B2(G.cell2[2]), pz2, B2(G.cell2[1] * py2)));
+    const f2 g = mul2(B2(G.beta), rcp2(den));
+    gpx = fma2(g, px2, B2(G.icell2[0]));
+    gpy = fma2(g, B2(py2), B2(G.icell2[1]));
+    gpz = fma2(g, pz2, B2(G.icell2[2]));
+    f2 dx = mul2(g, Px), dy = mul2(g, B2(py)), dz = mul2(g, Pz);
+    const f2 hPz = mul2(B2(0.5f), Pz);
+    hxy = mul2(dx, B2(0.5f * py));
+    hxz = mul2(dx, hPz);
+    hyz = mul2(dy, hPz);
+    if (CLAMP) {
+      float a[3], b[3], la[3], lb[3];
+      U2(dx, a[0], b[0]); U2(dy, a[1], b[1]); U2(dz, a[2], b[2]);
+      U2(gpx, la[0], lb[0]); U2(gpy, la[1], lb[1]); U2(gpz, la[2], lb[2]);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        a[q] = fminf(fmaxf(a[q], -kClamp * la[q]), kClamp * la[q]);
+        b[q] = fminf(fmaxf(b[q], -kClamp * lb[q]), kClamp * lb[q]);
+      }
+      dx = P2(a[0], b[0]); dy = P2(a[1], b[1]); dz = P2(a[2], b[2]);
+    }
+    f2 o = mul2(gpx, Sx);
+    o = fma2(gpy, Sy, o);
+    o = fma2(gpz, Sz, o);
+    o = fma2(hxy, Xxy, o);
+    o = fma2(hxz, Xxz, o);
+    o = fma2(hyz, Xyz, o);
+    o = fma2(dx, sub2(xp, xm), o);
+    o = fma2(dy, sub2(yp, ym), o);
+    o = fma2(dz, sub2(zp, zm), o);
+    return mul2(add2(fr, o), mul2(B2(0.5f), rcp2(add2(add2(gpx, gpy), gpz))));
+  }
+  f2 o = mul2(B2(cu.gpx), Sx);
+  o = fma2(B2(cu.gpy), Sy, o);
+  o = fma2(B2(cu.gpz), Sz, o);
+  o = fma2(B2(cu.hxy), Xxy, o);
+  o = fma2(B2(cu.hxz), Xxz, o);
+  o = fma2(B2(cu.hyz), Xyz, o);
+  return mul2(add2(fr, o), B2(1.0f / cu.diag));
+}
+
+// The same sweep as rb_sweep_kernel with fixed cell positions per thread and
+// two cells per evaluation.  Red (ring rows ly, lz in [1, S-1), 17 cells per
+// row): thread -> (row slot, cell t) once; rows of plane lz pair with plane
+// lz + H (H = TZ/2 + 1 is odd, so the pair's parities differ and so do their
+// x positions).  Black (tile rows, 16 cells per row): planes lz and lz + TZ/2
+// pair (same parity, same x position).
+template <bool LOCAL, bool CLAMP, int TY, int TZ>
+__global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restrict__ vin, float* __restrict__ vout,
+                                                          const float* __restrict__ rhs, LG G, float shift) {
+  constexpr int SY = TY + 4, SZ = TZ + 4, SXY = WX * SY;
+  extern __shared__ __align__(16) float smem[];
+  float* sv = smem;
+  int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  row_table<2, TY, TZ>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<2, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
+  load_rows<2, TY, TZ>(sv, ro, vin, x0, G.n[0]);
+  Cf cu;
+  if (!LOCAL) cu = coef_fast<false, false>(G.pg[0], G.pg[1], G.pg[2], G);
+  __syncthreads();
+  const f2 sh2 = B2(shift);
+  // ---- red
+  constexpr int RPR = 17, RSL = NT / RPR, RY = SY - 2, HP = TZ / 2 + 1, PR = RY * HP;
+  constexpr int KR = (PR + RSL - 1) / RSL;
+  static_assert(HP % 2 == 1, "red pairs need planes of opposite parity");
+  const unsigned slot = threadIdx.x / RPR, t = threadIdx.x - RPR * slot;
+  const int lxo = 3 + 2 * (int)t, lxe = lxo + 1;   // odd and even x positions of this thread's cells
+  const float pxe = LOCAL ? sp[lxe] : 0.0f, pxo = LOCAL ? sp[lxo] : 0.0f;
+  const int gxe = wrapi(x0 - XH + lxe, G.n[0]), gxo = wrapi(x0 - XH + lxo, G.n[0]);
+  f2 nv[KR];
+  int qa[KR], qb[KR];
+#pragma unroll
+  for (int k = 0; k < KR; ++k) {
+    const unsigned pr = slot + RSL * k;
+    qa[k] = -1;
+    if (slot < RSL && pr < PR) {
+      const int ly = 1 + pr % RY, lza = 1 + pr / RY, lzb = lza + HP;
+      const bool ea = ((ly + lza) & 1) == 0;   // red: lx+ly+lz even, so cell a sits at an even lx
+      const int lxa = ea ? lxe : lxo, lxb = ea ? lxo : lxe;
+      qa[k] = lxa + WX * ly + SXY * lza;
+      qb[k] = lxb + WX * ly + SXY * lzb;
+      const f2 Px = P2(ea ? pxe : pxo, ea ? pxo : pxe);
+      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : 0;
+      const float py = LOCAL ? sp[WX + ly] : 0.0f;
+      const f2 fr = sub2(P2(__ldg(rhs + ro[ly + SY * lza] + (ea ? gxe : gxo)),
+                            __ldg(rhs + ro[ly + SY * lzb] + (ea ? gxo : gxe))), sh2);
+      nv[k] = gs_two<LOCAL, CLAMP, SXY>(sv, qa[k], qb[k], fr, Px, py, Pz, cu, G);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < KR; ++k)
+    if (qa[k] >= 0) {
+      float a, b;
+      U2(nv[k], a, b);
+      sv[qa[k]] = a;
+      sv[qb[k]] = b;
+    }
+  __syncthreads();
+  // ---- black
+  constexpr int BSL = NT / 16, HB = TZ / 2, PB = TY * HB, KB = (PB + BSL - 1) / BSL;
+  const unsigned bslot = threadIdx.x >> 4, tb = threadIdx.x & 15;
+  f2 nb[KB];
+  int qc[KB];
+#pragma unroll
+  for (int k = 0; k < KB; ++k) {
+    const unsigned pr = bslot + BSL * k;
+    qc[k] = -1;
+    if (pr < PB) {
+      const int ly = 2 + pr % TY, lza = 2 + pr / TY, lzb = lza + HB;
+      const int lx = 4 + ((ly + lza + 1) & 1) + 2 * (int)tb;
+      qc[k] = lx + WX * ly + SXY * lza;
+      const float px = LOCAL ? sp[lx] : 0.0f, py = LOCAL ? sp[WX + ly] : 0.0f;
+      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : 0;
+      const int gx = x0 - XH + lx;
+      const f2 fr = sub2(P2(__ldg(rhs + ro[ly + SY * lza] + gx), __ldg(rhs + ro[ly + SY * lzb] + gx)), sh2);
+      nb[k] = gs_two<LOCAL, CLAMP, SXY>(sv, qc[k], qc[k] + HB * SXY, fr, B2(px), py, Pz, cu, G);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < KB; ++k)
+    if (qc[k] >= 0) {
+      float a, b;
+      U2(nb[k], a, b);
+      sv[qc[k]] = a;
+      sv[qc[k] + HB * SXY] = b;
+    }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int row = warp; row < TY * TZ; row += NWARP) {
+    const int ly = 2 + row % TY, lz = 2 + row / TY;
+    vout[ro[ly + SY * lz] + x0 + lane] = sv[XH + lane + WX * ly + SXY * lz];
+  }
+}
+
+// The accurate residual of resid_acc_kernel with the double-float window held
+// as interleaved (hi, lo) pairs: one 8-byte shared load per neighbour and one
+// packed subtraction give both parts of a difference.
+template <bool LOCAL, int TY, int TZ>
+__global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
+                                                        const float* __restrict__ ec, const float* __restrict__ f,
+                                                        float* __restrict__ ohi, float* __restrict__ olo,
+                                                        float* __restrict__ r, LG G, float alpha,
+                                                        double* __restrict__ part) {
+  constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY, SN = WX * SY * SZ;
+  extern __shared__ __align__(16) float smem[];
+  f2* sw = reinterpret_cast<f2*>(smem);                      // SN (hi, lo) pairs
+  int* ro = reinterpret_cast<int*>(smem + 2 * SN);
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  row_table<1, TY, TZ>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
+  {
+    float4* sw4 = reinterpret_cast<float4*>(smem);
+    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = 4;
+#pragma unroll
+    for (int k0 = 0; k0 < K; k0 += B) {
+      float4 h[B], l[B], e[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = threadIdx.x + (k0 + b) * NT;
+        if (k0 + b < K && t < TOT) {
+          const int row = t / CH, c = t - CH * row;
+          const int o = ro[row] + wrapi(x0 - XH + 4 * c, G.n[0]);
+          h[b] = __ldg(reinterpret_cast<const float4*>(hi + o));
+          l[b] = __ldg(reinterpret_cast<const float4*>(lo + o));
+          if (ec) e[b] = __ldg(reinterpret_cast<const float4*>(ec + o));
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = threadIdx.x + (k0 + b) * NT;
+        if (k0 + b < K && t < TOT) {
+          if (ec) {
+            df_add(h[b].x, l[b].x, e[b].x, h[b].x, l[b].x);
+            df_add(h[b].y, l[b].y, e[b].y, h[b].y, l[b].y);
+            df_add(h[b].z, l[b].z, e[b].z, h[b].z, l[b].z);
+            df_add(h[b].w, l[b].w, e[b].w, h[b].w, l[b].w);
+          }
+          sw4[2 * t] = make_float4(h[b].x, l[b].x, h[b].y, l[b].y);
+          sw4[2 * t + 1] = make_float4(h[b].z, l[b].z, h[b].w, l[b].w);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  float s1 = 0.0f, s2 = 0.0f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int SX = WX;
+  for (int row = warp; row < TY * TZ; row += NWARP) {
+    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
+    const int q = lx + SX * ly + SXY * lz;
+    const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1], pz = LOCAL ? sp[2 * WX + lz] : G.pg[2];
+    const float px2 = __fmul_rn(px, px), py2 = __fmul_rn(py, py), pz2 = __fmul_rn(pz, pz);
+    const float den = __fadd_rn(__fadd_rn(__fmul_rn(G.cell2[0], px2), __fmul_rn(G.cell2[1], py2)),
+                                __fmul_rn(G.cell2[2], pz2));
+    const float g = __fdiv_rn(G.beta, den);
+    const float gpx = __fadd_rn(G.icell2[0], __fmul_rn(g, px2));
+    const float gpy = __fadd_rn(G.icell2[1], __fmul_rn(g, py2));
+    const float gpz = __fadd_rn(G.icell2[2], __fmul_rn(g, pz2));
+    const f2 c0 = sw[q];
+    auto D = [&](int u) {
+      float a, b;
+      U2(sub2(sw[u], c0), a, b);   // (h_u - h_0, l_u - l_0), each rounded once
+      return __fadd_rn(a, b);
+    };
+    const float dxp = D(q + 1), dxm = D(q - 1), dyp = D(q + SX), dym = D(q - SX), dzp = D(q + SXY), dzm = D(q - SXY);
+    float br = gpx * (dxp + dxm) + gpy * (dyp + dym) + gpz * (dzp + dzm) +
+               g / 2.0f *
+                   (__fmul_rn(px, py) * ((D(q + 1 + SX) + D(q - 1 - SX)) - (D(q - 1 + SX) + D(q + 1 - SX))) +
+                    __fmul_rn(px, pz) * ((D(q + 1 + SXY) + D(q - 1 - SXY)) - (D(q - 1 + SXY) + D(q + 1 - SXY))) +
+                    __fmul_rn(py, pz) * ((D(q + SX + SXY) + D(q - SX - SXY)) - (D(q - SX + SXY) + D(q + SX - SXY))));
+    if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
+    const int o = ro[ly + SY * lz] + x0 + lane;
+    const float rv = (__ldg(f + o) - alpha) + br;
+    float h0, l0;
+    U2(c0, h0, l0);
+    ohi[o] = h0;
+    olo[o] = l0;
+    r[o] = rv;
+    s1 += rv;
+    s2 += rv * rv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double red[2][NWARP];
+  if (lane == 0) { red[0][warp] = s1; red[1][warp] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < NWARP; ++k) { a += red[0][k]; b += red[1][k]; }
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    part[2 * bid] = a;
+    part[2 * bid + 1] = b;
+  }
+}
+
+template <int HY, int TY, int TZ>
+constexpr size_t win_bytes(int arrays) {
+  return sizeof(float) * (size_t)arrays * WX * (TY + 2 * HY) * (TZ + 2 * HY) +
+         sizeof(int) * (TY + 2 * HY) * (TZ + 2 * HY) + sizeof(float) * 3 * WX;
+}
+
+// Tile height/depth for a level: 16 x 16 when that still gives every SM a block, else 8 x 8.
 bool big_tiles(const int n[3]) {
-  return n[1] % 16 == 0 && n[2] % 16 == 0 && (n[0] / TX) * (n[1] / 16) * (n[2] / 16) >= 2 * kNumSMs;
+  return n[1] % 16 == 0 && n[2] % 16 == 0 && (n[0] / TX) * (n[1] / 16) * (n[2] / 16) >= kNumSMs;
 }
 
 template <int TY, int TZ>
@@ -309,29 +633,32 @@ cudaError_t allow_smem(K kernel, size_t bytes) {
 
 template <bool LOCAL, bool CLAMP, int TY, int TZ>
 cudaError_t sweep_t(cudaStream_t s, const float* vin, float* vout, const float* rhs, const LG& G, float shift) {
-  auto k = rb_sweep_kernel<LOCAL, CLAMP, TY, TZ>;
-  cudaError_t e = allow_smem(k, sweep_smem<TY, TZ>());
+  auto k = rb_sweep2_kernel<LOCAL, CLAMP, TY, TZ>;
+  constexpr size_t b = win_bytes<2, TY, TZ>(1);
+  cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, sweep_smem<TY, TZ>(), s>>>(vin, vout, rhs, G, shift);
+  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(vin, vout, rhs, G, shift);
   return cudaGetLastError();
 }
 
 template <bool LOCAL, bool CLAMP, int TY, int TZ>
 cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float shift) {
   auto k = resid_kernel<LOCAL, CLAMP, TY, TZ>;
-  cudaError_t e = allow_smem(k, resid_smem<TY, TZ>());
+  constexpr size_t b = win_bytes<1, TY, TZ>(1);
+  cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, resid_smem<TY, TZ>(), s>>>(ec, rhs, r, G, shift);
+  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(ec, rhs, r, G, shift);
   return cudaGetLastError();
 }
 
 template <bool LOCAL, int TY, int TZ>
 cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f, float* ohi,
                   float* olo, float* r, const LG& G, float alpha, double* part) {
-  auto k = resid_acc_kernel<LOCAL, TY, TZ>;
-  cudaError_t e = allow_smem(k, acc_smem<TY, TZ>());
+  auto k = resid_acc2_kernel<LOCAL, TY, TZ>;
+  constexpr size_t b = win_bytes<1, TY, TZ>(2);
+  cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, acc_smem<TY, TZ>(), s>>>(hi, lo, ec, f, ohi, olo, r, G, alpha, part);
+  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(hi, lo, ec, f, ohi, olo, r, G, alpha, part);
   return cudaGetLastError();
 }
 
