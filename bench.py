@@ -251,18 +251,19 @@ def run_gb300(args):
     value = ws * 1000.0 / ms
     stats = ctx.solve_stats()
 
-    # roofline of the dominant kernel (finest-level red-black half sweep), measured live
+    # roofline of the dominant kernel (finest-level red-black sweep), measured live
     peak, peak_src = measured_peak()
     avg = C.c_float()
     nbytes = C.c_double()
     ctx.call("baorec_profile_kernel", 0, 50, C.byref(avg), C.byref(nbytes))
     achieved = nbytes.value / (avg.value * 1e-3) / 1e9
-    roofline = {"kernel": "rb_half_kernel (finest level, 256^3)", "bound": "hbm", "achieved": achieved,
+    roofline = {"kernel": "rb_sweep2_kernel (full red-black sweep, finest level %s)" % "x".join(map(str, n)), "bound": "hbm", "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                "traffic": traffic_per_launch("rb_half_kernel", int(np.prod(n))),
+                "traffic": traffic_per_launch("rb_sweep2_kernel", int(np.prod(n))),
                 "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
     ctx.call("baorec_profile_kernel", 1, 20, C.byref(avg), C.byref(nbytes))
-    aux = {"resid_acc_kernel": {"ms": avg.value, "GB/s": nbytes.value / (avg.value * 1e-3) / 1e9}}
+    aux = {"resid_acc2_kernel": {"ms": avg.value, "GB/s": nbytes.value / (avg.value * 1e-3) / 1e9,
+                                 "traffic": traffic_per_launch("resid_acc2_kernel", int(np.prod(n)))}}
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
