@@ -17,6 +17,7 @@ ITERATIVE, MULTIGRID = 0, 1
 LOS_LOCAL, LOS_GLOBAL = 0, 1
 MAS_CIC, MAS_TSC = 0, 1
 MG_REFERENCE, MG_CONVERGENT = 0, 1
+START_ZERO, START_SPECTRAL, START_LEARNED = 0, 1, 2
 FIELD = {"disp": 0, "rsd": 1, "sum": 2}
 
 
@@ -44,13 +45,16 @@ class Config(C.Structure):
         ("jacobi_damping_factor", C.c_float), ("jacobi_niterations", C.c_int32),
         ("vcycle_niterations", C.c_int32), ("ran_min", C.c_float), ("mas", C.c_int32),
         ("mg_mode", C.c_int32), ("nu1", C.c_int32), ("nu2", C.c_int32), ("rtol", C.c_float),
-        ("max_cycles", C.c_int32),
+        ("max_cycles", C.c_int32), ("mg_start", C.c_int32), ("start_rate", C.c_float),
     ]
 
 
 class SolveStats(C.Structure):
-    _fields_ = [("cycles", C.c_int32), ("rel_residual", C.c_double), ("alpha", C.c_double),
+    _fields_ = [("cycles", C.c_int32), ("spectral_steps", C.c_int32), ("rel_residual", C.c_double), ("alpha", C.c_double),
                 ("rel_residual_initial", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 P = C.c_void_p
@@ -192,8 +196,7 @@ class Context:
     def solve_stats(self) -> dict:
         st = SolveStats()
         self.call("baorec_last_solve_stats", C.byref(st))
-        return {"cycles": st.cycles, "rel_residual": st.rel_residual, "alpha": st.alpha,
-                "rel_residual_initial": st.rel_residual_initial}
+        return st.as_dict()
 
     def set_box(self, box_size, box_min):
         self.call("baorec_set_box", F3(*box_size), F3(*box_min))

@@ -62,6 +62,9 @@ class IterativeRecon:
             self.beta = float(F32(F32(self.f) / F32(self.bias)))
 
 
+_STARTS = {"zero": _lib.START_ZERO, "spectral": _lib.START_SPECTRAL, "learned": _lib.START_LEARNED}
+
+
 @dataclass
 class MultigridRecon:
     """``MultigridRecon`` (``src/recon.jl:18-33``) plus the residual-driven
@@ -84,11 +87,15 @@ class MultigridRecon:
     nu2: int = 2
     rtol: float = 1e-6
     max_cycles: int = 50
+    start: str = "zero"                  # convergent mode: "zero" | "spectral" | "learned"
+    start_rate: float = 0.5
     solve_stats: dict = dc_field(default_factory=dict)
 
     def __post_init__(self):
         if self.beta is None:
             self.beta = float(F32(F32(self.f) / F32(self.bias)))
+        if self.start not in _STARTS:
+            raise ValueError(f"start must be one of {sorted(_STARTS)}, got {self.start!r}")
 
 
 # ----------------------------------------------------------------------------
@@ -238,6 +245,8 @@ def _config(recon, shape, ran_min=0.01) -> _lib.Config:
         c.nu1, c.nu2 = int(recon.nu1), int(recon.nu2)
         c.rtol = float(recon.rtol)
         c.max_cycles = int(recon.max_cycles)
+        c.mg_start = _STARTS[recon.start]
+        c.start_rate = float(recon.start_rate)
     else:
         c.n_iter = int(recon.n_iter)
     return c
@@ -637,8 +646,7 @@ def solve_(phi, f, recon, phi0=None):
                 code = ctx.status("baorec_mg_solve", b.ptr, a.ptr, c.ptr, C.byref(st))
         else:
             code = ctx.status("baorec_mg_solve", b.ptr, a.ptr, None, C.byref(st))
-    stats = {"cycles": st.cycles, "rel_residual": st.rel_residual, "alpha": st.alpha,
-             "rel_residual_initial": st.rel_residual_initial, "status": code}
+    stats = dict(st.as_dict(), status=code)
     recon.solve_stats = stats
     if code != _lib.OK:
         _lib.check(ctx.h, code)

@@ -112,6 +112,10 @@ static int validate(baorec_ctx* ctx, const baorec_config* c) {
   if (c->mas != BAOREC_MAS_CIC && c->mas != BAOREC_MAS_TSC) return set_error(ctx, BAOREC_ERR_ARG, "unknown mas %d", c->mas);
   if (c->n_iter < 0 || c->jacobi_niterations < 0 || c->vcycle_niterations < 0 || c->nu1 < 0 || c->nu2 < 0)
     return set_error(ctx, BAOREC_ERR_ARG, "negative iteration count");
+  if (c->mg_start < BAOREC_START_ZERO || c->mg_start > BAOREC_START_LEARNED)
+    return set_error(ctx, BAOREC_ERR_ARG, "unknown mg_start %d", c->mg_start);
+  if (c->mg_start != BAOREC_START_ZERO && !(c->start_rate > 0.0f && c->start_rate <= 1.0f))
+    return set_error(ctx, BAOREC_ERR_ARG, "start_rate %g outside (0, 1]", (double)c->start_rate);
   return BAOREC_OK;
 }
 
@@ -141,9 +145,11 @@ extern "C" void baorec_config_default(baorec_config* c) {
   c->nu2 = 2;
   c->rtol = 1e-6f;
   c->max_cycles = 50;
+  c->mg_start = BAOREC_START_ZERO;
+  c->start_rate = 0.5f;
 }
 
-static_assert(sizeof(baorec_config) == 4 * 29, "baorec_config layout is part of the ABI");
+static_assert(sizeof(baorec_config) == 4 * 31, "baorec_config layout is part of the ABI");
 static_assert(sizeof(baorec_solve_stats) == 32, "baorec_solve_stats layout is part of the ABI");
 
 static thread_local char g_create_msg[512];

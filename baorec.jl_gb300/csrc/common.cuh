@@ -148,6 +148,7 @@ int normalize_data(baorec_ctx* ctx, float* delta);
 int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr);
 int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
+int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
 int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
 int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
 int smooth_pair(baorec_ctx* ctx, float* a, float* b);   // b == a + N uses one batched transform pair

@@ -6,6 +6,9 @@
 // with i < n1/2+1 at i + (n1/2+1)*(j + n2*k); the halved axis is x as in
 // rfftfreq(dims[1]) (src/utils.jl:6).  The 1/N of the inverse transform is
 // folded into the k-space multiply that precedes every C2R.
+#include <algorithm>
+#include <cmath>
+
 #include "common.cuh"
 
 namespace baorec {
@@ -391,6 +394,92 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
   CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, planes));
   interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
   CKLAUNCH();
+  return BAOREC_OK;
+}
+
+// ---- FFT preconditioner of the multigrid operator ------------------------
+//
+// With one line of sight l for the whole mesh the 19-point operator of the
+// multigrid (src/multigrid.jl:14-135, first-derivative terms dropped) is a
+// convolution, diagonal in Fourier space.  Per axis a with cell c_a and grid
+// angle θ_a = 2π m_a / n_a:
+//   A(k) = Σ_a (1 + β l_a²)/c_a² · 4 sin²(θ_a/2)
+//        + Σ_{a<b} 2 β l_a l_b / (c_a c_b) · sin θ_a sin θ_b,
+// positive except at k = 0.  For a fixed line of sight this is the exact
+// inverse; for a radial one, l is the direction of the box centre (or the
+// isotropic average l_a l_b -> δ_ab/3 when the observer sits inside the box).
+namespace {
+
+struct SGeom {
+  int n1, n2, n3, n1h;
+  float diag[3];   // (1 + β l_a²) / c_a², times 4
+  float cross[3];  // 2 β l_a l_b / (c_a c_b) for ab = xy, xz, yz
+  float invN;
+};
+
+SGeom sgeom_of(const baorec_ctx* c) {
+  SGeom g;
+  g.n1 = c->n1; g.n2 = c->n2; g.n3 = c->n3; g.n1h = c->n1h;
+  const int n[3] = {c->n1, c->n2, c->n3};
+  double cell[3], l[3] = {0.0, 0.0, 0.0};
+  double Lmax = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    cell[a] = (double)(c->cfg.box_size[a] / (float)n[a]);
+    Lmax = std::max(Lmax, (double)c->cfg.box_size[a]);
+  }
+  const double beta = c->cfg.beta;
+  bool iso = false;
+  if (c->cfg.los_mode == BAOREC_LOS_GLOBAL) {
+    for (int a = 0; a < 3; ++a) l[a] = c->cfg.los[a];
+  } else {
+    for (int a = 0; a < 3; ++a) l[a] = (double)c->cfg.box_min[a] + 0.5 * (double)c->cfg.box_size[a];
+  }
+  double nl = sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
+  if (c->cfg.los_mode == BAOREC_LOS_LOCAL && nl < 0.25 * Lmax) iso = true;
+  if (!(nl > 0.0)) iso = true;
+  for (int a = 0; a < 3; ++a) l[a] = iso ? 0.0 : l[a] / nl;
+  for (int a = 0; a < 3; ++a) {
+    const double lp = iso ? 1.0 / 3.0 : l[a] * l[a];
+    g.diag[a] = (float)(4.0 * (1.0 + beta * lp) / (cell[a] * cell[a]));
+  }
+  g.cross[0] = (float)(2.0 * beta * l[0] * l[1] / (cell[0] * cell[1]));
+  g.cross[1] = (float)(2.0 * beta * l[0] * l[2] / (cell[0] * cell[2]));
+  g.cross[2] = (float)(2.0 * beta * l[1] * l[2] / (cell[1] * cell[2]));
+  g.invN = (float)(1.0 / (double)c->N);
+  return g;
+}
+
+__global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, size_t nk, SGeom g) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nk; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.n1h);
+    const size_t q = e / g.n1h;
+    const int j = (int)(q % g.n2), k = (int)(q / g.n2);
+    const int mj = j < (g.n2 + 1) / 2 ? j : j - g.n2;
+    const int mk = k < (g.n3 + 1) / 2 ? k : k - g.n3;
+    // sin(θ/2) and sin θ with θ = 2π m / n, through sinpi for exact arguments
+    const float hx = sinpif((float)i / (float)g.n1), hy = sinpif((float)mj / (float)g.n2);
+    const float hz = sinpif((float)mk / (float)g.n3);
+    const float sx = sinpif(2.0f * (float)i / (float)g.n1), sy = sinpif(2.0f * (float)mj / (float)g.n2);
+    const float sz = sinpif(2.0f * (float)mk / (float)g.n3);
+    const float A = g.diag[0] * hx * hx + g.diag[1] * hy * hy + g.diag[2] * hz * hz + g.cross[0] * sx * sy +
+                    g.cross[1] * sx * sz + g.cross[2] * sy * sz;
+    const float s = e == 0 ? 0.0f : g.invN / A;
+    cufftComplex v = a[e];
+    v.x *= s; v.y *= s;
+    a[e] = v;
+  }
+}
+
+}  // namespace
+
+// e = S⁻¹ r (zero mean), S the operator with the box's mean line of sight.
+// r is read only; e may not alias r.
+int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
+  SGeom g = sgeom_of(ctx);
+  CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));
+  spectral_inverse_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, g);
+  CKLAUNCH();
+  CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, e));
   return BAOREC_OK;
 }
 

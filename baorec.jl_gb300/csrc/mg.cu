@@ -679,6 +679,12 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
                        (uintptr_t)ctx->phi_lo2 % 16 == 0;
   const bool tile0 = aligned && tile_ok(L0.n) && (size_t)tile_blocks(L0.n) <= kMaxPartials;
   int nparts = kResBlocks;
+  // spectral corrections (FFT inverse of the operator with the box's mean line
+  // of sight) run first, for as long as each one shrinks the residual by at
+  // least start_rate; V-cycles take over after the first one that does not
+  bool spectral = ctx->cfg.mg_start != BAOREC_START_ZERO;
+  int nspec = 0;
+  double rho_prev = 0.0;
   for (int it = 0;; ++it) {
     if (tile0) {
       CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
@@ -706,15 +712,24 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
     }
     double mean_r = s1 / (double)N;
     alpha += mean_r;
-    // the correction V-cycle solves A e = r - mean(r); r sits in lev[0].f
-    CKS(vcycle_rb(ctx, 0, (float)mean_r));
+    if (spectral && nspec > 0 && !(rho <= (double)ctx->cfg.start_rate * rho_prev)) spectral = false;
+    if (spectral && nspec >= ctx->cfg.max_cycles) spectral = false;
+    rho_prev = rho;
+    // the correction solves A e = r - mean(r); r sits in lev[0].f
+    if (spectral) {
+      CKS(spectral_correction(ctx, L0.f, L0.v));
+      ++nspec;
+    } else {
+      CKS(vcycle_rb(ctx, 0, (float)mean_r));
+      ++cycles;
+    }
     have_e = true;
-    ++cycles;
   }
   if (hiA != phi) CK(cudaMemcpyAsync(phi, hiA, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
   if (loA != ctx->phi_lo) CK(cudaMemcpyAsync(ctx->phi_lo, loA, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
   baorec_solve_stats s;
   s.cycles = cycles;
+  s.spectral_steps = nspec;
   s.rel_residual = rho;
   s.alpha = alpha;
   s.rel_residual_initial = rho0;

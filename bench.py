@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--start", default="spectral", choices=["zero", "spectral", "learned"],
+                    help="initial guess of the timed multigrid solve; a plain (zero) start arm is timed beside it")
     return ap.parse_args()
 
 
@@ -198,9 +200,13 @@ def run_gb300(args):
         dist.init_process_group("nccl")
     m, bs, bm = workload(args, args.seed + rank)
     n = (args.mesh,) * 3
-    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=None,
-                                mg_mode="convergent", rtol=1e-6, nu1=2, nu2=2, max_cycles=50)
-    ctx = baorec.setup_fft_(rec, n)
+    def make(start):
+        rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=None,
+                                    mg_mode="convergent", rtol=1e-6, nu1=2, nu2=2, max_cycles=50, start=start)
+        return baorec.setup_fft_(rec, n)
+
+    ctx = make(args.start)
+    ctx_plain = make("zero") if args.start != "zero" else None
     nd, nr = len(m.x), len(m.rx)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
@@ -212,7 +218,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     SUM, DISP = _lib.FIELD["sum"], _lib.FIELD["disp"]
 
-    def step(flags=0, xs=None, rs=None, od=None, ors=None, ori=None):
+    def step(flags=0, xs=None, rs=None, od=None, ors=None, ori=None, ctx=ctx):
         xs = xs or ptr(X)
         rs = rs or ptr(R)
         st = ctx.status("baorec_reconstructed_potential", *xs, nd, *rs, nr, flags)
@@ -222,34 +228,44 @@ def run_gb300(args):
         ctx.call("baorec_reconstructed_positions", *rs[:3], nr, SUM, *(ors or ptr(out_rs)), flags | _lib.ASYNC)
         ctx.call("baorec_reconstructed_positions", *rs[:3], nr, DISP, *(ori or ptr(out_ri)), flags)
 
-    for _ in range(args.warmup):
-        step()
-    stats = ctx.solve_stats()
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = Clocks(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    l0 = ctx.launches()
-    clocks.start()
-    ev0.record(stream)
-    cycles = []
-    for _ in range(args.steps):
-        step()
-        cycles.append(ctx.solve_stats()["cycles"])
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    launches = ctx.launches() - l0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    def timed(c):
+        """W warm-up steps, then K steps between CUDA events on the context's stream (max over ranks)."""
+        for _ in range(args.warmup):
+            step(ctx=c)
+        stream = torch.cuda.ExternalStream(c.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks = Clocks(local)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = c.launches()
+        clocks.start()
+        ev0.record(stream)
+        hist = []
+        for _ in range(args.steps):
+            step(ctx=c)
+            s = c.solve_stats()
+            hist.append((s["spectral_steps"], s["cycles"]))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        launches = c.launches() - l0
+        ms = ev0.elapsed_time(ev1) / args.steps
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms, hist, clk, launches, c.solve_stats()
+
+    plain = None
+    if ctx_plain is not None:
+        pms, phist, pclk, _, pstats = timed(ctx_plain)
+        plain = {"value": ws * 1000.0 / pms, "ms_per_step": pms, "cycles_per_step": [h[1] for h in phist],
+                 "rel_residual": pstats["rel_residual"], "clocks": pclk}
+    ms, hist, clk, launches, stats = timed(ctx)
+    cycles = [h[1] for h in hist]
     value = ws * 1000.0 / ms
-    stats = ctx.solve_stats()
 
     # roofline of the dominant kernel (finest-level red-black sweep), measured live
     peak, peak_src = measured_peak()
@@ -300,13 +316,15 @@ def run_gb300(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"lightcone plain-start MG reconstruction {args.mesh}^3 to 1e-6, "
+            "config": {"workload": f"lightcone MG reconstruction {args.mesh}^3 to 1e-6 relative residual, "
                                    f"{nd} data + {nr} randoms, CIC, R=15, b=2, f=0.8, local LOS, 2+2 RB sweeps",
-                       "mesh": args.mesh, "start": "plain (zero); learned start not built",
+                       "mesh": args.mesh, "start": args.start,
                        "l2": "working set per step > 1 GB >> 126 MB L2 (inputs larger than L2)",
                        "parallelism": f"replicas x{ws}"},
-            "solver": {"cycles": stats["cycles"], "rel_residual": stats["rel_residual"],
-                       "cycles_per_step": cycles},
+            "solver": {"start": args.start, "cycles": stats["cycles"], "spectral_steps": stats["spectral_steps"],
+                       "rel_residual": stats["rel_residual"], "cycles_per_step": cycles,
+                       "spectral_steps_per_step": [h[0] for h in hist]},
+            "plain": plain,
             "gpu_launches": launches,
             "clocks": clk,
             "roofline": roofline,

@@ -57,6 +57,9 @@ typedef enum {
 #define BAOREC_MAS_TSC    1     /* no reference counterpart */
 #define BAOREC_MG_REFERENCE  0  /* FMG, damped Jacobi, fixed cycles (src/multigrid.jl:722-752) */
 #define BAOREC_MG_CONVERGENT 1  /* residual-driven V-cycles to rtol (no reference counterpart) */
+#define BAOREC_START_ZERO     0 /* convergent mode: V-cycles from a zero potential (plain multigrid) */
+#define BAOREC_START_SPECTRAL 1 /* convergent mode: FFT-preconditioned corrections first (no reference counterpart) */
+#define BAOREC_START_LEARNED  2 /* convergent mode: CNN initial guess, then as SPECTRAL (no reference counterpart) */
 #define BAOREC_FIELD_DISP 0     /* :disp */
 #define BAOREC_FIELD_RSD  1     /* :rsd  */
 #define BAOREC_FIELD_SUM  2     /* :sum  */
@@ -85,11 +88,15 @@ typedef struct {
   int32_t nu1, nu2;          /* convergent mode: pre/post red-black Gauss-Seidel sweeps (2, 2) */
   float rtol;                /* convergent mode: relative residual target (1e-6) */
   int32_t max_cycles;        /* convergent mode: V-cycle cap (50) */
+  int32_t mg_start;          /* convergent mode: BAOREC_START_ZERO (default) | _SPECTRAL | _LEARNED */
+  float start_rate;          /* spectral corrections continue while each shrinks the residual
+                                by at least this factor (0.5); then V-cycles take over */
 } baorec_config;
 
 /* Solver statistics of the last multigrid solve. */
 typedef struct {
   int32_t cycles;            /* V-cycles run */
+  int32_t spectral_steps;    /* FFT-preconditioned corrections run before the V-cycles */
   double rel_residual;       /* |f - a*1 - A phi| / |f - a*1| after the last cycle (FP64) */
   double alpha;              /* constant shift a removed from the right-hand side */
   double rel_residual_initial;

@@ -44,10 +44,11 @@ def test_config_defaults_match_reference(lib):
     assert c.jacobi_niterations == 5 and c.vcycle_niterations == 6
     assert abs(c.ran_min - 0.01) < 1e-9
     assert c.mg_mode == _lib.MG_REFERENCE and c.mas == _lib.MAS_CIC
+    assert c.mg_start == _lib.START_ZERO and abs(c.start_rate - 0.5) < 1e-9
 
 
 def test_struct_layout_matches_header(lib):
     from baorec import _lib
-    # 29 four-byte words; api.cu static_asserts the same size on the C side
-    assert ctypes.sizeof(_lib.Config) == 4 * 29
+    # 31 four-byte words; api.cu static_asserts the same size on the C side
+    assert ctypes.sizeof(_lib.Config) == 4 * 31
     assert ctypes.sizeof(_lib.SolveStats) == 32

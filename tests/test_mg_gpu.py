@@ -94,3 +94,32 @@ def test_convergent_solution_matches_fp64_oracle_gradient():
     go = O.gradient_meshes(v64, bs.astype(np.float64))
     err = max(rel_l2(g[a], go[a]) for a in range(3))
     assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.0, 1.0], [0.6, 0.0, 0.8]])
+def test_spectral_start_reaches_same_solution_with_fewer_cycles(los):
+    """FFT-preconditioned corrections first (mean line of sight), then
+    V-cycles: the same FP64-checked residual, fewer V-cycles than the zero
+    start, the same gradient."""
+    import baorec
+    f, bs, bm = _problem(n=64, seed=7)
+    ff = np.asfortranarray(f)
+    out = {}
+    for start in ("zero", "spectral"):
+        rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40, start=start)
+        phi = baorec.zeros_mesh(f.shape, device=False)
+        st = baorec.solve_(phi, ff, rec)
+        assert st["rel_residual"] <= 1e-6
+        coef = O.coefs_f64(O.stencil_coefficients(f.shape, bs, bm, rec.beta, los, F32))
+        r = (f.astype(np.float64) - st["alpha"]) - O.apply_operator(np.asarray(phi, np.float64), coef, los is None)
+        assert np.linalg.norm(r) / np.linalg.norm(f.astype(np.float64) - st["alpha"]) < 2e-6
+        out[start] = (st, O.gradient_meshes(np.asarray(phi, np.float64), bs.astype(np.float64)))
+    s0, g0 = out["zero"]
+    s1, g1 = out["spectral"]
+    assert s0["spectral_steps"] == 0 and s1["spectral_steps"] >= 1
+    print("zero", s0, "spectral", s1)
+    assert s1["cycles"] < s0["cycles"], (s0, s1)
+    if los is not None:
+        # one line of sight: the FFT inverse is exact, no V-cycle is needed
+        assert s1["cycles"] == 0, s1
+    assert max(rel_l2(g1[a], g0[a]) for a in range(3)) < 2e-5
