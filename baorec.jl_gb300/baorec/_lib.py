@@ -90,6 +90,7 @@ _SIGS = {
     "baorec_mg_fmg": (C.c_int, [P, P, P]),
     "baorec_mg_solve": (C.c_int, [P, P, P, P, C.POINTER(SolveStats)]),
     "baorec_last_solve_stats": (C.c_int, [P, C.POINTER(SolveStats)]),
+    "baorec_solve_history": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int]),
     "baorec_profile_kernel": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_reconstructed_overdensity": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
     "baorec_reconstructed_potential": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
@@ -197,6 +198,17 @@ class Context:
         st = SolveStats()
         self.call("baorec_last_solve_stats", C.byref(st))
         return st.as_dict()
+
+    def solve_history(self) -> list:
+        """[(relative residual, correction that followed)] of the last solve:
+        0 = V-cycle, m > 0 = m FFT corrections, -1 = none."""
+        n = self.lib.baorec_solve_history(self.h, None, None, 0)
+        if n < 0:
+            raise BaorecError(-n, "solve_history")
+        rho = (C.c_double * max(n, 1))()
+        kind = (C.c_int32 * max(n, 1))()
+        self.lib.baorec_solve_history(self.h, rho, kind, n)
+        return [(rho[i], kind[i]) for i in range(n)]
 
     def set_box(self, box_size, box_min):
         self.call("baorec_set_box", F3(*box_size), F3(*box_min))

@@ -474,6 +474,16 @@ extern "C" int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats
   return BAOREC_OK;
 }
 
+extern "C" int baorec_solve_history(const baorec_ctx* ctx, double* rho, int32_t* kind, int cap) {
+  if (!ctx || cap < 0 || (cap > 0 && (!rho || !kind))) return -BAOREC_ERR_ARG;
+  const int n = (int)ctx->hist_rho.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    rho[i] = ctx->hist_rho[i];
+    kind[i] = ctx->hist_kind[i];
+  }
+  return n;
+}
+
 // reconstructed_overdensity! (src/recon.jl:93-132) into ctx->result.
 static int recon_iterative(baorec_ctx* ctx, const Staged& s, int64_t n, int64_t nr, uint32_t flags) {
   float* A = ctx->mesh3;          // δ_r = result

@@ -72,6 +72,8 @@ struct baorec_ctx {
   // statistics
   int64_t launches = 0;
   baorec_solve_stats last_stats;
+  std::vector<double> hist_rho;        // per outer step of the last solve
+  std::vector<int32_t> hist_kind;
   char msg[512];
 };
 

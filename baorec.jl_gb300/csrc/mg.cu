@@ -23,6 +23,9 @@
 //    coefficients are clamped to |g p_a| <= κ gp_a (only cells next to the
 //    observer change), an FP64 shared-memory solve on the coarsest level.
 #include <math.h>
+
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "mg_common.cuh"
@@ -49,14 +52,33 @@ __global__ void jacobi_kernel(const float* __restrict__ v, const float* __restri
 
 // r = f - A v (src/multigrid.jl:328-376, 393).
 __global__ void residual_kernel(const float* __restrict__ v, const float* __restrict__ f, float* __restrict__ r,
-                                LG G, size_t N, float shift) {
+                                LG G, size_t N, float shift, float* __restrict__ acc = nullptr) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
     int i, j, k; cell_ijk(e, G.n, i, j, k);
     Coef c = coef_at(G, i, j, k);
     Nb b = gather([&](int a, int bb, int cc) { return v[at(G.n, a, bb, cc)]; }, G.n, i, j, k);
     float av = 2.0f * (c.gpx + c.gpy + c.gpz) * v[e] - offdiag(c, b, G.local);
     r[e] = (f[e] - shift) - av;
+    if (acc) acc[e] += v[e];
   }
+}
+
+// r = f - A v over differences v_nb - v_0 (accurate for smooth v); acc += v
+__global__ void residual_diff_kernel(const float* __restrict__ v, const float* __restrict__ f, float* __restrict__ r,
+                                     LG G, size_t N, float* __restrict__ acc) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k; cell_ijk(e, G.n, i, j, k);
+    Coef c = coef_at(G, i, j, k);
+    const float v0 = v[e];
+    Nb b = gather([&](int a, int bb, int cc) { return v[at(G.n, a, bb, cc)] - v0; }, G.n, i, j, k);
+    r[e] = f[e] + offdiag(c, b, G.local);
+    if (acc) acc[e] += v0;
+  }
+}
+
+__global__ void add_kernel(float* __restrict__ a, const float* __restrict__ b, size_t N) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    a[e] += b[e];
 }
 
 // Full-weighting restriction (src/multigrid.jl:586-640): coarse c centred on fine 2c+1.
@@ -298,6 +320,9 @@ unsigned blocks_for(size_t N) {
 constexpr int kResBlocks = 2 * kNumSMs;
 constexpr size_t kMaxPartials = kRedCapacity / 2;   // blocks whose (Σr, Σr²) fit the partials buffer
 constexpr int kDenseMaxCells = 512;                  // coarsest levels up to 8^3 use the dense inverse
+constexpr int kSpectralInnerMax = 6;                 // FFT corrections per accurate residual, at most
+constexpr int kSpectralFirst = 2;                    // FFT corrections in the first outer step
+constexpr double kSpectralRateFloor = 0.1;           // planning never assumes a faster contraction
 
 }  // namespace
 
@@ -682,9 +707,11 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   // spectral corrections (FFT inverse of the operator with the box's mean line
   // of sight) run first, for as long as each one shrinks the residual by at
   // least start_rate; V-cycles take over after the first one that does not
+  ctx->hist_rho.clear();
+  ctx->hist_kind.clear();
   bool spectral = ctx->cfg.mg_start != BAOREC_START_ZERO;
-  int nspec = 0;
-  double rho_prev = 0.0;
+  int nspec = 0, m_last = 0;
+  double rho_prev = 0.0, rate = 0.0;
   for (int it = 0;; ++it) {
     if (tile0) {
       CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
@@ -702,6 +729,8 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
     double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;
     rho = fn2 > 0.0 ? sqrt(s2 / fn2) : 0.0;
     if (it == 0) rho0 = rho;
+    ctx->hist_rho.push_back(rho);
+    ctx->hist_kind.push_back(-1);
     { float* t = hiA; hiA = hiB; hiB = t; t = loA; loA = loB; loB = t; }
     if (!(rho == rho)) { status = set_error(ctx, BAOREC_ERR_NOT_CONVERGED, "multigrid solve produced NaN"); break; }
     if (rho <= (double)ctx->cfg.rtol) { status = BAOREC_OK; break; }
@@ -712,16 +741,55 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
     }
     double mean_r = s1 / (double)N;
     alpha += mean_r;
-    if (spectral && nspec > 0 && !(rho <= (double)ctx->cfg.start_rate * rho_prev)) spectral = false;
+    if (spectral && m_last > 0) {
+      // observed contraction per FFT correction of the last outer step
+      rate = rho_prev > 0.0 ? pow(rho / rho_prev, 1.0 / m_last) : 0.0;
+      if (!(rate <= (double)ctx->cfg.start_rate)) spectral = false;
+    }
     if (spectral && nspec >= ctx->cfg.max_cycles) spectral = false;
     rho_prev = rho;
     // the correction solves A e = r - mean(r); r sits in lev[0].f
     if (spectral) {
-      CKS(spectral_correction(ctx, L0.f, L0.v));
-      ++nspec;
+      // m FFT corrections against an FP32 running residual, no host round trip:
+      //   d_0 = S⁻¹ r_0;  r_q = r_{q-1} - A d_{q-1};  d_q = S⁻¹ r_q;  e = Σ d_q
+      // with m from the observed rate, enough to reach rtol if it holds
+      // The first outer step is held to kSpectralFirst corrections: its shift
+      // α = mean(f) is not yet the consistent one, and the corrections cannot
+      // go below that inconsistency.
+      int m = kSpectralFirst;
+      if (m_last > 0) {
+        const double r = std::min(std::max(rate, kSpectralRateFloor), 0.9);
+        const double want = log((double)ctx->cfg.rtol / rho) / log(r);
+        m = (int)std::min<double>(kSpectralInnerMax, std::max(1.0, ceil(want)));
+      }
+      float* rin = L0.f;
+      float* rout = L0.r + N;
+      float* d = L0.r;
+      CKS(spectral_correction(ctx, rin, L0.v));
+      for (int q = 1; q < m; ++q) {
+        const float* dprev = q == 1 ? L0.v : d;
+        float* acc = q == 1 ? nullptr : L0.v;
+        if (tile0) {
+          CK(launch_resid_diff(ctx->stream, dprev, rin, rout, G, acc));
+          ctx->launches++;
+        } else {
+          residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(dprev, rin, rout, G, N, acc);
+          CKLAUNCH();
+        }
+        std::swap(rin, rout);
+        CKS(spectral_correction(ctx, rin, d));
+      }
+      if (m > 1) {
+        add_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L0.v, d, N);
+        CKLAUNCH();
+      }
+      nspec += m;
+      m_last = m;
+      ctx->hist_kind.back() = m;
     } else {
       CKS(vcycle_rb(ctx, 0, (float)mean_r));
       ++cycles;
+      ctx->hist_kind.back() = 0;
     }
     have_e = true;
   }

@@ -113,7 +113,12 @@ bool tile_ok(const int n[3]);
 cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const float* rhs, const LG& G, float shift,
                             bool clamp);
 // r = rhs - shift - Ã e (clamped operator).
-cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float shift, bool clamp);
+// r = rhs - A e in difference form (exact operator, no clamp), accurate for
+// smooth e; with acc != nullptr also acc += e
+cudaError_t launch_resid_diff(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float* acc);
+// r = rhs - shift - A e; with acc != nullptr also acc += e
+cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float shift, bool clamp,
+                         float* acc = nullptr);
 // Accurate residual with solution update; writes (Σr, Σr²) per block to part, returns the block count.
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* e, const float* f,
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts);

@@ -11,6 +11,8 @@
 // tables; global: uniform coefficients) and on whether the level has cells
 // next to the observer whose first-derivative coefficients need clamping.
 #include <mutex>
+#include <set>
+#include <utility>
 
 #include "mg_common.cuh"
 
@@ -108,6 +110,24 @@ __device__ __forceinline__ float nbr(const float* __restrict__ s, int q, const C
   return o;
 }
 
+// The same bracket over differences D = s_nb - s_q.  The operator's row sums
+// vanish, so A s = -bracket(D); for smooth s the differences are exact to a
+// rounding of their own size, where diag*s_q - bracket(s) cancels to a
+// rounding of s_q's size (relative error growing like 1/(k h)^2).
+template <bool LOCAL, int SXY>
+__device__ __forceinline__ float nbr_diff(const float* __restrict__ s, int q, const Cf& c) {
+  constexpr int SX = WX;
+  const float s0 = s[q];
+  auto D = [&](int o) { return s[q + o] - s0; };
+  const float xp = s[q + 1], xm = s[q - 1], yp = s[q + SX], ym = s[q - SX], zp = s[q + SXY], zm = s[q - SXY];
+  float o = c.gpx * ((xp - s0) + (xm - s0)) + c.gpy * ((yp - s0) + (ym - s0)) + c.gpz * ((zp - s0) + (zm - s0)) +
+            c.hxy * ((D(1 + SX) + D(-1 - SX)) - (D(-1 + SX) + D(1 - SX))) +
+            c.hxz * ((D(1 + SXY) + D(-1 - SXY)) - (D(-1 + SXY) + D(1 - SXY))) +
+            c.hyz * ((D(SX + SXY) + D(-SX - SXY)) - (D(-SX + SXY) + D(SX - SXY)));
+  if (LOCAL) o += c.dx * (xp - xm) + c.dy * (yp - ym) + c.dz * (zp - zm);
+  return o;
+}
+
 // One red-black Gauss-Seidel sweep, both colours in one pass, out of place.
 // Red cells of the tile and of a one-cell ring around it are updated from the
 // old window; then the black cells of the tile from the red-updated window.
@@ -182,9 +202,10 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep_kernel(const float* __restrict
 }
 
 // r = rhs - shift - Ã e (correction equation, clamped operator).
-template <bool LOCAL, bool CLAMP, int TY, int TZ>
+template <bool LOCAL, bool CLAMP, int TY, int TZ, bool DIFF = false>
 __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
-                                                   float* __restrict__ r, LG G, float shift) {
+                                                   float* __restrict__ r, LG G, float shift,
+                                                   float* __restrict__ acc) {
   constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY;
   extern __shared__ __align__(16) float smem[];
   float* sv = smem;
@@ -204,7 +225,11 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
     const int q = lx + WX * ly + SXY * lz;
     const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
     const int o = ro[ly + SY * lz] + x0 + lane;
-    r[o] = (__ldg(rhs + o) - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
+    if (DIFF)
+      r[o] = (__ldg(rhs + o) - shift) + nbr_diff<LOCAL, SXY>(sv, q, cf);
+    else
+      r[o] = (__ldg(rhs + o) - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
+    if (acc) acc[o] += sv[q];   // optional: accumulate the operand into a running sum
   }
 }
 
@@ -615,19 +640,21 @@ bool big_tiles(const int n[3]) {
 template <int TY, int TZ>
 dim3 grid_of(const int n[3]) { return dim3(n[0] / TX, n[1] / TY, n[2] / TZ); }
 
-// Opt each kernel into its dynamic shared memory once per device.
+// Opt each kernel into its dynamic shared memory once per device.  Kernels
+// of the same signature share a function-pointer type, so the cache is keyed
+// by the kernel's address as well as the device.
 template <typename K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
   static std::mutex mu;
-  static bool done[64] = {};
+  static std::set<std::pair<const void*, int>> done;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  const std::pair<const void*, int> key((const void*)kernel, dev);
   std::lock_guard<std::mutex> lock(mu);
-  if (done[dev]) return cudaSuccess;
+  if (done.count(key)) return cudaSuccess;
   e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) done[dev] = true;
+  if (e == cudaSuccess) done.insert(key);
   return e;
 }
 
@@ -641,13 +668,14 @@ cudaError_t sweep_t(cudaStream_t s, const float* vin, float* vout, const float* 
   return cudaGetLastError();
 }
 
-template <bool LOCAL, bool CLAMP, int TY, int TZ>
-cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float shift) {
-  auto k = resid_kernel<LOCAL, CLAMP, TY, TZ>;
+template <bool LOCAL, bool CLAMP, int TY, int TZ, bool DIFF = false>
+cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float shift,
+                    float* acc) {
+  auto k = resid_kernel<LOCAL, CLAMP, TY, TZ, DIFF>;
   constexpr size_t b = win_bytes<1, TY, TZ>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(ec, rhs, r, G, shift);
+  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(ec, rhs, r, G, shift, acc);
   return cudaGetLastError();
 }
 
@@ -681,13 +709,25 @@ cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const
 }
 
 cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float shift,
-                         bool clamp) {
+                         bool clamp, float* acc) {
   const bool big = big_tiles(G.n);
   if (!G.local)
-    return big ? resid_t<false, false, 16, 16>(s, ec, rhs, r, G, shift) : resid_t<false, false, 8, 8>(s, ec, rhs, r, G, shift);
+    return big ? resid_t<false, false, 16, 16>(s, ec, rhs, r, G, shift, acc)
+               : resid_t<false, false, 8, 8>(s, ec, rhs, r, G, shift, acc);
   if (clamp)
-    return big ? resid_t<true, true, 16, 16>(s, ec, rhs, r, G, shift) : resid_t<true, true, 8, 8>(s, ec, rhs, r, G, shift);
-  return big ? resid_t<true, false, 16, 16>(s, ec, rhs, r, G, shift) : resid_t<true, false, 8, 8>(s, ec, rhs, r, G, shift);
+    return big ? resid_t<true, true, 16, 16>(s, ec, rhs, r, G, shift, acc)
+               : resid_t<true, true, 8, 8>(s, ec, rhs, r, G, shift, acc);
+  return big ? resid_t<true, false, 16, 16>(s, ec, rhs, r, G, shift, acc)
+             : resid_t<true, false, 8, 8>(s, ec, rhs, r, G, shift, acc);
+}
+
+cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+  const bool big = big_tiles(G.n);
+  if (!G.local)
+    return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
+               : resid_t<false, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);
+  return big ? resid_t<true, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
+             : resid_t<true, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);
 }
 
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f,

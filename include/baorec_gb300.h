@@ -221,6 +221,11 @@ int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, d
 
 /* Statistics of the context's last residual-driven solve. */
 int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats* stats);
+/* Convergence history of the last residual-driven solve: for each outer step
+ * the relative residual before it (rho[i]) and the correction that followed
+ * (kind[i]: 0 = V-cycle, m > 0 = m FFT corrections, -1 = none, the last
+ * entry).  Copies min(count, cap) entries and returns count (or < 0 on error). */
+int baorec_solve_history(const baorec_ctx* ctx, double* rho, int32_t* kind, int cap);
 
 /* reconstructed_overdensity! (src/recon.jl:93-132): overdensity then n_iter
  * iterations into the context result.  rx.. may be NULL (data only). */
