@@ -49,6 +49,14 @@ class Config(C.Structure):
     ]
 
 
+class GuessTrainConfig(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("seed", C.c_uint32),
+                ("sigma_g", C.c_float), ("pk_slope", C.c_float), ("region_min", C.c_float * 3),
+                ("region_size", C.c_float * 3), ("r_min", C.c_float), ("r_max", C.c_float),
+                ("ra_min", C.c_float), ("ra_max", C.c_float), ("dec_min", C.c_float), ("dec_max", C.c_float),
+                ("rtol", C.c_float)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("cycles", C.c_int32), ("spectral_steps", C.c_int32), ("rel_residual", C.c_double), ("alpha", C.c_double),
                 ("rel_residual_initial", C.c_double)]
@@ -98,6 +106,14 @@ _SIGS = {
     "baorec_get_result": (C.c_int, [P, P, U32]),
     "baorec_set_result": (C.c_int, [P, P, U32]),
     "baorec_displacement_meshes": (C.c_int, [P, P, P, P]),
+    "baorec_guess_num_params": (I64, []),
+    "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
+    "baorec_guess_set_params": (C.c_int, [P, P, I64]),
+    "baorec_guess_get_params": (C.c_int, [P, P, I64]),
+    "baorec_guess_eval": (C.c_int, [P, P, P, P, P, C.POINTER(C.c_double)]),
+    "baorec_guess_apply": (C.c_int, [P, P, P]),
+    "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
+    "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),
     "baorec_read_cic": (C.c_int, [P, P, P, P, P, I64, P, U32]),
     "baorec_read_shifts": (C.c_int, [P, P, P, P, I64, C.c_int, P, P, P, U32]),
     "baorec_reconstructed_positions": (C.c_int, [P, P, P, P, I64, C.c_int, P, P, P, U32]),

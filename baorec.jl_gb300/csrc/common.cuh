@@ -37,6 +37,8 @@ struct DevBuf {                       // a growable device buffer
   size_t bytes = 0;
 };
 
+struct GuessNet;                      // learned initial guess (guess_net.cu)
+
 }  // namespace baorec
 
 struct baorec_ctx {
@@ -62,6 +64,8 @@ struct baorec_ctx {
   baorec::Level lev[16];
   double* coarse_M = nullptr;          // dense FP64 inverse of level dense_level (or null)
   int dense_level = -1;                // first level with at most 512 cells
+  bool coarse_dirty = true;            // coarse_M / dense_level need rebuilding
+  baorec::GuessNet* net = nullptr;     // learned initial guess (weights, workspace)
   // reductions
   double* dred = nullptr;              // device FP64 partial sums
   double* hred = nullptr;              // pinned host mirror
@@ -151,6 +155,13 @@ int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t n
 int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
+// Unit line of sight the FFT preconditioner uses (false: isotropic, l = 0).
+bool mean_los(const baorec_ctx* c, double l[3]);
+// r = f - A v with the finest level's exact operator (difference form, FP32).
+int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r);
+// learned initial guess (guess_net.cu)
+int guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
+void guess_free(baorec_ctx* ctx);
 int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
 int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
 int smooth_pair(baorec_ctx* ctx, float* a, float* b);   // b == a + N uses one batched transform pair

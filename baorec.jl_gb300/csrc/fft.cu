@@ -408,6 +408,18 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
 // positive except at k = 0.  For a fixed line of sight this is the exact
 // inverse; for a radial one, l is the direction of the box centre (or the
 // isotropic average l_a l_b -> δ_ab/3 when the observer sits inside the box).
+bool mean_los(const baorec_ctx* c, double l[3]) {
+  double Lmax = 0.0;
+  for (int a = 0; a < 3; ++a) Lmax = std::max(Lmax, (double)c->cfg.box_size[a]);
+  for (int a = 0; a < 3; ++a)
+    l[a] = c->cfg.los_mode == BAOREC_LOS_GLOBAL ? (double)c->cfg.los[a]
+                                                : (double)c->cfg.box_min[a] + 0.5 * (double)c->cfg.box_size[a];
+  const double nl = sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
+  const bool iso = !(nl > 0.0) || (c->cfg.los_mode == BAOREC_LOS_LOCAL && nl < 0.25 * Lmax);
+  for (int a = 0; a < 3; ++a) l[a] = iso ? 0.0 : l[a] / nl;
+  return !iso;
+}
+
 namespace {
 
 struct SGeom {
@@ -421,23 +433,10 @@ SGeom sgeom_of(const baorec_ctx* c) {
   SGeom g;
   g.n1 = c->n1; g.n2 = c->n2; g.n3 = c->n3; g.n1h = c->n1h;
   const int n[3] = {c->n1, c->n2, c->n3};
-  double cell[3], l[3] = {0.0, 0.0, 0.0};
-  double Lmax = 0.0;
-  for (int a = 0; a < 3; ++a) {
-    cell[a] = (double)(c->cfg.box_size[a] / (float)n[a]);
-    Lmax = std::max(Lmax, (double)c->cfg.box_size[a]);
-  }
+  double cell[3], l[3];
+  for (int a = 0; a < 3; ++a) cell[a] = (double)(c->cfg.box_size[a] / (float)n[a]);
   const double beta = c->cfg.beta;
-  bool iso = false;
-  if (c->cfg.los_mode == BAOREC_LOS_GLOBAL) {
-    for (int a = 0; a < 3; ++a) l[a] = c->cfg.los[a];
-  } else {
-    for (int a = 0; a < 3; ++a) l[a] = (double)c->cfg.box_min[a] + 0.5 * (double)c->cfg.box_size[a];
-  }
-  double nl = sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
-  if (c->cfg.los_mode == BAOREC_LOS_LOCAL && nl < 0.25 * Lmax) iso = true;
-  if (!(nl > 0.0)) iso = true;
-  for (int a = 0; a < 3; ++a) l[a] = iso ? 0.0 : l[a] / nl;
+  const bool iso = !mean_los(c, l);
   for (int a = 0; a < 3; ++a) {
     const double lp = iso ? 1.0 / 3.0 : l[a] * l[a];
     g.diag[a] = (float)(4.0 * (1.0 + beta * lp) / (cell[a] * cell[a]));

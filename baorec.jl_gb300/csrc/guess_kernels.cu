@@ -1,0 +1,315 @@
+// Tensor-core implicit-GEMM kernels of the learned initial guess: the gather
+// convolution (forward and backward-data) and its weight gradient.  BF16
+// operands, FP32 accumulation, warp-level mma.sync (m16n8k16; m16n8k8 for
+// the 8-channel input layer).
+#include <cuda_runtime.h>
+
+#include "guess.cuh"
+
+namespace baorec {
+namespace guess {
+namespace {
+
+constexpr int kWarps = 8;   // warps per block
+constexpr int kMT = 2;      // 16-voxel M tiles per warp in the forward kernel
+constexpr int kG = 4;       // weight-gradient tiles held per warp at a time
+
+__device__ __forceinline__ void mma16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                      uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void mma8(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t b0) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(b0));
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ size_t vox(int n, int x, int y, int z) { return ((size_t)z * n + y) * n + x; }
+
+// Source voxel of output voxel (x, y, z) through tap t; false when it falls
+// in the zero padding.  For UP the tap is the output's parity (checked by the
+// caller) and (x, y, z) are the coarse coordinates.
+template <int KIND>
+__device__ __forceinline__ bool src_of(int t, int x, int y, int z, int n_in, int& xs, int& ys, int& zs) {
+  if (KIND == C3) {
+    xs = x + t % 3 - 1; ys = y + (t / 3) % 3 - 1; zs = z + t / 9 - 1;
+  } else if (KIND == DN) {
+    xs = 2 * x + (t & 1); ys = 2 * y + ((t >> 1) & 1); zs = 2 * z + (t >> 2);
+  } else {
+    xs = x; ys = y; zs = z;
+  }
+  return xs >= 0 && xs < n_in && ys >= 0 && ys < n_in && zs >= 0 && zs < n_in;
+}
+
+// One warp = one task: kMT*16 consecutive x of one output row (for UP: of
+// one coarse row and one output parity), all output channels.
+template <int KIND, int CIN, int COUT>
+__global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
+  constexpr int NB = COUT / 8;
+  constexpr bool K8 = CIN == 8;
+  constexpr int KS = K8 ? 1 : CIN / 16;
+  constexpr int T = KIND == C3 ? 27 : 8;
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  const int nx = KIND == UP ? a.n_in : a.n_out;   // grid the tasks walk
+  const int chunks = (nx + 16 * kMT - 1) / (16 * kMT);
+  const long long task = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const long long ntask = (long long)chunks * nx * nx * (KIND == UP ? 8 : 1);
+  if (task >= ntask) return;
+  const int cx = (int)(task % chunks);
+  long long r = task / chunks;
+  const int y = (int)(r % nx);
+  r /= nx;
+  const int z = (int)(r % nx);
+  const int par = KIND == UP ? (int)(r / nx) : 0;
+  const int x0 = cx * 16 * kMT;
+
+  float acc[kMT][NB][4];
+#pragma unroll
+  for (int m = 0; m < kMT; ++m)
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[m][b][e] = 0.0f;
+
+  for (int t = 0; t < T; ++t) {
+    if (KIND == UP && t != par) continue;
+    const uint32_t* rows[kMT][2];
+#pragma unroll
+    for (int m = 0; m < kMT; ++m)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int x = x0 + 16 * m + g + 8 * h;
+        int xs, ys, zs;
+        const bool ok = x < nx && src_of<KIND>(t, x, y, z, a.n_in, xs, ys, zs);
+        rows[m][h] = ok ? reinterpret_cast<const uint32_t*>(a.in + vox(a.n_in, xs, ys, zs) * a.in_cs) : nullptr;
+      }
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+      uint2 b[NB];
+#pragma unroll
+      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)(t * KS + ks) * NB + nb) * 32 + lane);
+#pragma unroll
+      for (int m = 0; m < kMT; ++m) {
+        const uint32_t* p0 = rows[m][0];
+        const uint32_t* p1 = rows[m][1];
+        const int o = 8 * ks;   // 16 channels = 8 words per K step
+        const uint32_t a0 = p0 ? __ldg(p0 + o + q) : 0u;
+        const uint32_t a1 = p1 ? __ldg(p1 + o + q) : 0u;
+        if (K8) {
+#pragma unroll
+          for (int nb = 0; nb < NB; ++nb) mma8(acc[m][nb], a0, a1, b[nb].x);
+        } else {
+          const uint32_t a2 = p0 ? __ldg(p0 + o + 4 + q) : 0u;
+          const uint32_t a3 = p1 ? __ldg(p1 + o + 4 + q) : 0u;
+#pragma unroll
+          for (int nb = 0; nb < NB; ++nb) mma16(acc[m][nb], a0, a1, a2, a3, b[nb].x, b[nb].y);
+        }
+      }
+    }
+  }
+  // epilogue: bias, addend, ReLU, BF16 store (two channels per thread and row)
+#pragma unroll
+  for (int m = 0; m < kMT; ++m)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int x = x0 + 16 * m + g + 8 * h;
+      if (x >= nx) continue;
+      size_t vo;
+      if (KIND == UP)
+        vo = vox(a.n_out, 2 * x + (par & 1), 2 * y + ((par >> 1) & 1), 2 * z + (par >> 2));
+      else
+        vo = vox(a.n_out, x, y, z);
+#pragma unroll
+      for (int nb = 0; nb < NB; ++nb) {
+        const int n = 8 * nb + 2 * q;
+        float v0 = acc[m][nb][2 * h], v1 = acc[m][nb][2 * h + 1];
+        if (a.bias) { v0 += __ldg(a.bias + n); v1 += __ldg(a.bias + n + 1); }
+        if (a.add) {
+          const __nv_bfloat162 ad = *reinterpret_cast<const __nv_bfloat162*>(a.add + vo * a.add_cs + n);
+          v0 += __bfloat162float(ad.x);
+          v1 += __bfloat162float(ad.y);
+        }
+        if (a.relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+        *reinterpret_cast<__nv_bfloat162*>(a.out + vo * a.out_cs + n) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+}
+
+// Weight gradient dW[t][ci][co] = Σ_v x[src(v,t)][ci] dy[v][co]: an MMA with
+// M = input channels, N = output channels, K = 16 voxels of one output row.
+// Each block walks a contiguous range of 16-voxel rows; each warp holds kG
+// (tap, ci tile, co block) accumulators at a time and flushes them with FP32
+// atomics at the end.
+template <int KIND, int CIN, int COUT>
+__global__ void __launch_bounds__(kWarps * 32) wgrad_kernel(WgradArgs a, int rows_per_block) {
+  constexpr int NB = COUT / 8;
+  constexpr int CIT = (CIN + 15) / 16;
+  constexpr int T = KIND == C3 ? 27 : 8;
+  constexpr int ITEMS = T * CIT * NB;
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3, warp = threadIdx.x >> 5;
+  const int nx = KIND == UP ? a.n_in : a.n_out;
+  const int chunks = (nx + 15) / 16;
+  const long long nrows = (long long)chunks * nx * nx;
+  const long long r0 = (long long)blockIdx.x * rows_per_block;
+  const long long r1 = r0 + rows_per_block < nrows ? r0 + rows_per_block : nrows;
+  for (int i0 = warp; i0 < ITEMS; i0 += kWarps * kG) {
+    float acc[kG][4];
+#pragma unroll
+    for (int j = 0; j < kG; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[j][e] = 0.0f;
+    for (long long rr = r0; rr < r1; ++rr) {
+      const int cx = (int)(rr % chunks);
+      const long long s = rr / chunks;
+      const int y = (int)(s % nx), z = (int)(s / nx);
+      const int x0 = 16 * cx;
+#pragma unroll
+      for (int j = 0; j < kG; ++j) {
+        const int item = i0 + j * kWarps;
+        if (item >= ITEMS) break;
+        const int t = item / (CIT * NB);
+        const int rem = item - t * CIT * NB;
+        const int cit = rem / NB, nb = rem - cit * NB;
+        const int c0 = 16 * cit, n0 = 8 * nb;
+        // the four K columns of this lane: 2q, 2q+1, 2q+8, 2q+9
+        __nv_bfloat16 xa[4], xb[4], dv[4];
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const int k = 2 * q + (kk & 1) + 8 * (kk >> 1);
+          const int x = x0 + k;
+          xa[kk] = xb[kk] = dv[kk] = __float2bfloat16(0.0f);
+          if (x >= nx) continue;
+          size_t vo;
+          int xs, ys, zs;
+          bool ok;
+          if (KIND == UP) {
+            vo = vox(a.n_out, 2 * x + (t & 1), 2 * y + ((t >> 1) & 1), 2 * z + (t >> 2));
+            ok = true;
+            xs = x; ys = y; zs = z;
+          } else {
+            vo = vox(a.n_out, x, y, z);
+            ok = src_of<KIND>(t, x, y, z, a.n_in, xs, ys, zs);
+          }
+          dv[kk] = a.dy[vo * a.dy_cs + n0 + g];
+          if (ok) {
+            const __nv_bfloat16* xp = a.in + vox(a.n_in, xs, ys, zs) * a.in_cs + c0 + g;
+            xa[kk] = xp[0];
+            if (c0 + g + 8 < CIN) xb[kk] = xp[8];
+          }
+        }
+        mma16(acc[j], pack2(xa[0], xa[1]), pack2(xb[0], xb[1]), pack2(xa[2], xa[3]), pack2(xb[2], xb[3]),
+              pack2(dv[0], dv[1]), pack2(dv[2], dv[3]));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+      const int item = i0 + j * kWarps;
+      if (item >= ITEMS) break;
+      const int t = item / (CIT * NB);
+      const int rem = item - t * CIT * NB;
+      const int cit = rem / NB, nb = rem - cit * NB;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int ci = 16 * cit + g + 8 * h;
+        if (ci >= CIN) continue;
+        const int co = 8 * nb + 2 * q;
+        float* d = a.dw + ((size_t)t * CIN + ci) * COUT + co;
+        atomicAdd(d, acc[j][2 * h]);
+        atomicAdd(d + 1, acc[j][2 * h + 1]);
+      }
+    }
+  }
+}
+
+__global__ void frag_kernel(int kind, int cin, int cout, const float* __restrict__ w, uint2* __restrict__ frag,
+                            int backward) {
+  // the convolution these fragments feed: (kind', cin', cout')
+  const int k2 = backward ? (kind == DN ? UP : kind == UP ? DN : C3) : kind;
+  const int ci2 = backward ? cout : cin, co2 = backward ? cin : cout;
+  const int T = k2 == C3 ? 27 : 8;
+  const int KS = ci2 >= 16 ? ci2 / 16 : 1, NB = co2 / 8;
+  const size_t total = (size_t)T * KS * NB * 32;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int lane = (int)(e % 32);
+    size_t r = e / 32;
+    const int nb = (int)(r % NB);
+    r /= NB;
+    const int ks = (int)(r % KS);
+    const int t = (int)(r / KS);
+    const int g = lane >> 2, q = lane & 3;
+    const int n = 8 * nb + g;
+    auto W = [&](int k) -> __nv_bfloat16 {
+      if (k >= ci2) return __float2bfloat16(0.0f);
+      // forward: W[t][k][n]; backward: W[flip t][n][k] (k: original output channel)
+      float v = backward ? w[((size_t)(kind == C3 ? 26 - t : t) * cin + n) * cout + k]
+                         : w[((size_t)t * cin + k) * cout + n];
+      return __float2bfloat16(v);
+    };
+    const int k0 = 16 * ks;
+    uint2 f;
+    f.x = pack2(W(k0 + 2 * q), W(k0 + 2 * q + 1));
+    f.y = ci2 >= 16 ? pack2(W(k0 + 8 + 2 * q), W(k0 + 9 + 2 * q)) : 0u;
+    frag[e] = f;
+  }
+}
+
+template <int KIND, int CIN, int COUT>
+cudaError_t fwd_t(cudaStream_t s, const ConvArgs& a) {
+  const int nx = KIND == UP ? a.n_in : a.n_out;
+  const long long ntask = (long long)((nx + 16 * kMT - 1) / (16 * kMT)) * nx * nx * (KIND == UP ? 8 : 1);
+  const unsigned blocks = (unsigned)((ntask + kWarps - 1) / kWarps);
+  conv_fwd_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int KIND, int CIN, int COUT>
+cudaError_t wgrad_t(cudaStream_t s, const WgradArgs& a) {
+  const int nx = KIND == UP ? a.n_in : a.n_out;
+  const long long nrows = (long long)((nx + 15) / 16) * nx * nx;
+  const int target = 2 * 152;   // two blocks per SM
+  int per = (int)((nrows + target - 1) / target);
+  if (per < 1) per = 1;
+  const unsigned blocks = (unsigned)((nrows + per - 1) / per);
+  wgrad_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a, per);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+#define BAOREC_GUESS_SHAPES(X)                                                                     \
+  X(C3, 8, 16) X(C3, 16, 16) X(C3, 32, 32) X(C3, 64, 64) X(C3, 64, 32) X(C3, 32, 16) X(C3, 16, 32) \
+  X(C3, 32, 64) X(DN, 16, 32) X(DN, 32, 64) X(UP, 64, 32) X(UP, 32, 16)
+
+cudaError_t conv_forward(cudaStream_t s, int kind, int cin, int cout, const ConvArgs& a) {
+#define X(K, I, O) \
+  if (kind == K && cin == I && cout == O) return fwd_t<K, I, O>(s, a);
+  BAOREC_GUESS_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t conv_wgrad(cudaStream_t s, int kind, int cin, int cout, const WgradArgs& a) {
+#define X(K, I, O) \
+  if (kind == K && cin == I && cout == O) return wgrad_t<K, I, O>(s, a);
+  BAOREC_GUESS_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t weight_frags(cudaStream_t s, int kind, int cin, int cout, const float* w, uint2* frag, bool backward) {
+  frag_kernel<<<64, 256, 0, s>>>(kind, cin, cout, w, frag, backward ? 1 : 0);
+  return cudaGetLastError();
+}
+
+}  // namespace guess
+}  // namespace baorec

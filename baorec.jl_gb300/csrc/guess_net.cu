@@ -1,0 +1,790 @@
+// Learned initial guess for the multigrid solve (no reference counterpart).
+//
+// The network predicts the error of the FFT start: with S the operator for
+// the box's mean line of sight, φ_s = S⁻¹ f, the converged potential is
+// φ ≈ φ_s + s·net(features), s = rms(φ_s).  Features per cell (BF16, 8
+// channels): f c²/s, φ_s/s, (f - A φ_s) c²/s, r̂ - l (3), 0, 0; r̂ is the
+// radial direction of the cell centre, l the mean line of sight.
+//
+// The network is a 3-level U-Net (levels n, n/2, n/4 with 16/32/64 channels,
+// 3x3x3 convolutions, strided 2x2x2 down/up-sampling, skip connections by
+// channel concatenation, ReLU, a 1x1x1 linear head; 431,969 parameters).
+// Training runs on the device: synthetic lognormal fields in the survey
+// window of random sub-boxes, targets from the residual-driven solver, MSE
+// loss, Adam.  Parameters are FP32 masters; the convolutions read BF16
+// copies in tensor-core fragment order.
+#include <math.h>
+
+#include <algorithm>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "common.cuh"
+#include "guess.cuh"
+
+namespace baorec {
+
+using guess::C3;
+using guess::DN;
+using guess::UP;
+typedef __nv_bfloat16 bf16;
+
+namespace {
+
+enum TId { T_X, T_A0, T_CAT0, T_B0, T_C0, T_A1, T_B1, T_CAT1, T_D1, T_E1, T_A2, T_B2, T_C2, T_COUNT };
+struct TensorDef { int level, ch; };
+const TensorDef kTensors[T_COUNT] = {{0, 8},  {0, 16}, {0, 32}, {0, 16}, {0, 16}, {1, 32}, {1, 32},
+                                     {1, 64}, {1, 32}, {1, 32}, {2, 64}, {2, 64}, {2, 64}};
+
+struct LayerDef {
+  int kind, cin, cout;
+  int in_t, in_off, out_t, out_off;
+  bool acc_grad;   // the backward-data output adds to a gradient written earlier
+};
+constexpr int kLayers = 14;
+const LayerDef kNet[kLayers] = {
+    {C3, 8, 16, T_X, 0, T_A0, 0, false},       {C3, 16, 16, T_A0, 0, T_CAT0, 16, false},
+    {DN, 16, 32, T_CAT0, 16, T_A1, 0, true},   {C3, 32, 32, T_A1, 0, T_B1, 0, false},
+    {C3, 32, 32, T_B1, 0, T_CAT1, 32, false},  {DN, 32, 64, T_CAT1, 32, T_A2, 0, true},
+    {C3, 64, 64, T_A2, 0, T_B2, 0, false},     {C3, 64, 64, T_B2, 0, T_C2, 0, false},
+    {UP, 64, 32, T_C2, 0, T_CAT1, 0, false},   {C3, 64, 32, T_CAT1, 0, T_D1, 0, false},
+    {C3, 32, 32, T_D1, 0, T_E1, 0, false},     {UP, 32, 16, T_E1, 0, T_CAT0, 0, false},
+    {C3, 32, 16, T_CAT0, 0, T_B0, 0, false},   {C3, 16, 16, T_B0, 0, T_C0, 0, false}};
+constexpr int kHeadIn = 16;
+constexpr int kFeat = 8;
+
+struct ParamLayout {
+  size_t w[kLayers + 1], b[kLayers + 1], total;
+  ParamLayout() {
+    size_t o = 0;
+    for (int l = 0; l < kLayers; ++l) {
+      w[l] = o;
+      o += (size_t)guess::taps_of(kNet[l].kind) * kNet[l].cin * kNet[l].cout;
+      b[l] = o;
+      o += kNet[l].cout;
+    }
+    w[kLayers] = o;
+    o += kHeadIn;
+    b[kLayers] = o;
+    o += 1;
+    total = o;
+  }
+};
+const ParamLayout kP;
+
+constexpr int kRedBlocksG = 2 * kNumSMs;
+
+// ---- elementwise and reduction kernels ------------------------------------
+
+__device__ __forceinline__ size_t gstride() { return (size_t)gridDim.x * blockDim.x; }
+__device__ __forceinline__ size_t gtid() { return blockIdx.x * (size_t)blockDim.x + threadIdx.x; }
+
+// out[v] = b + Σ_c W[c] x[v][c]
+__global__ void head_fwd_kernel(const bf16* __restrict__ x, const float* __restrict__ w, float* __restrict__ out,
+                                size_t nv) {
+  for (size_t v = gtid(); v < nv; v += gstride()) {
+    const uint4* p = reinterpret_cast<const uint4*>(x + v * kHeadIn);
+    float s = __ldg(w + kHeadIn);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint4 u = __ldg(p + h);
+      const uint32_t wd[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&wd[j]);
+        s += __ldg(w + 8 * h + 2 * j) * __bfloat162float(b2.x) + __ldg(w + 8 * h + 2 * j + 1) * __bfloat162float(b2.y);
+      }
+    }
+    out[v] = s;
+  }
+}
+
+// MSE loss: dout = 2 (out - tgt) / N, per-block FP64 partial of Σ (out - tgt)^2
+__global__ void loss_kernel(const float* __restrict__ out, const float* __restrict__ tgt, float* __restrict__ dout,
+                            size_t nv, double* __restrict__ part) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  const float sc = 2.0f / (float)nv;
+  for (size_t v = gtid(); v < nv; v += gstride()) {
+    const float d = out[v] - tgt[v];
+    dout[v] = sc * d;
+    s += (double)(d * d);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// head backward: dx[v][c] = W[c] dout[v]; dW[c] += Σ_v x[v][c] dout[v]; db += Σ dout
+__global__ void head_bwd_kernel(const bf16* __restrict__ x, const float* __restrict__ w, const float* __restrict__ dout,
+                                bf16* __restrict__ dx, float* __restrict__ dw, size_t nv) {
+  __shared__ float sh[kHeadIn + 1][32];
+  float acc[kHeadIn + 1];
+#pragma unroll
+  for (int c = 0; c <= kHeadIn; ++c) acc[c] = 0.0f;
+  for (size_t v = gtid(); v < nv; v += gstride()) {
+    const float d = dout[v];
+#pragma unroll
+    for (int c = 0; c < kHeadIn; c += 2) {
+      const __nv_bfloat162 xv = *reinterpret_cast<const __nv_bfloat162*>(x + v * kHeadIn + c);
+      acc[c] += __bfloat162float(xv.x) * d;
+      acc[c + 1] += __bfloat162float(xv.y) * d;
+      *reinterpret_cast<__nv_bfloat162*>(dx + v * kHeadIn + c) = __floats2bfloat162_rn(__ldg(w + c) * d, __ldg(w + c + 1) * d);
+    }
+    acc[kHeadIn] += d;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c <= kHeadIn; ++c) {
+    float s = acc[c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[c][warp] = s;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x <= kHeadIn) {
+    float s = 0.0f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[threadIdx.x][k];
+    atomicAdd(dw + threadIdx.x, s);   // dw[0..15] = weights, dw[16] = bias
+  }
+}
+
+// dy[v][c] = 0 where the forward output y[v][c] <= 0 (ReLU), C channels at
+// offset (pointers pre-offset), channel stride cs.
+__global__ void relu_bwd_kernel(bf16* __restrict__ dy, const bf16* __restrict__ y, int cs, int C, size_t nv) {
+  const int cp = C / 2;
+  for (size_t e = gtid(); e < nv * cp; e += gstride()) {
+    const size_t v = e / cp;
+    const int c = 2 * (int)(e - v * cp);
+    __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(dy + v * cs + c);
+    const __nv_bfloat162 yy = *reinterpret_cast<const __nv_bfloat162*>(y + v * cs + c);
+    __nv_bfloat162 dd = *d;
+    if (!(__bfloat162float(yy.x) > 0.0f)) dd.x = __float2bfloat16(0.0f);
+    if (!(__bfloat162float(yy.y) > 0.0f)) dd.y = __float2bfloat16(0.0f);
+    *d = dd;
+  }
+}
+
+// db[c] += Σ_v dy[v][c]
+__global__ void bias_grad_kernel(const bf16* __restrict__ dy, int cs, int C, size_t nv, float* __restrict__ db) {
+  __shared__ float sh[256];
+  // thread -> channel c = tid % C, voxel lane = tid / C (C divides 256)
+  const int c = threadIdx.x % C, lanes = blockDim.x / C, vl = threadIdx.x / C;
+  float s = 0.0f;
+  for (size_t v = blockIdx.x * (size_t)lanes + vl; v < nv; v += (size_t)gridDim.x * lanes)
+    s += __bfloat162float(dy[v * cs + c]);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  if ((int)threadIdx.x < C) {
+    float t = 0.0f;
+    for (int k = 0; k < lanes; ++k) t += sh[threadIdx.x + k * C];
+    atomicAdd(db + threadIdx.x, t);
+  }
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, size_t n, float lr, float gscale, float b1, float b2, float c1,
+                            float c2, float eps) {
+  for (size_t i = gtid(); i < n; i += gstride()) {
+    const float gr = g[i] * gscale;
+    const float mi = b1 * m[i] + (1.0f - b1) * gr;
+    const float vi = b2 * v[i] + (1.0f - b2) * gr * gr;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+struct FeatGeom {
+  int n1, n2;
+  float c2s;      // cell² / s
+  float is;       // 1 / s
+  float l[3];     // mean line of sight (0 when isotropic or global)
+  int local;
+};
+
+// X[v] = (f c²/s, φ_s/s, r_s c²/s, r̂ - l, 0, 0)
+__global__ void features_kernel(const float* __restrict__ f, const float* __restrict__ phs,
+                                const float* __restrict__ rs, const float* __restrict__ ax,
+                                const float* __restrict__ ay, const float* __restrict__ az, FeatGeom G,
+                                bf16* __restrict__ X, size_t nv) {
+  for (size_t v = gtid(); v < nv; v += gstride()) {
+    float d[3] = {0.0f, 0.0f, 0.0f};
+    if (G.local) {
+      const int i = (int)(v % G.n1);
+      const size_t r = v / G.n1;
+      const int j = (int)(r % G.n2), k = (int)(r / G.n2);
+      const float x = ax[i], y = ay[j], z = az[k];
+      const float rn = sqrtf(x * x + y * y + z * z);
+      const float ir = rn > 0.0f ? 1.0f / rn : 0.0f;
+      d[0] = x * ir - G.l[0];
+      d[1] = y * ir - G.l[1];
+      d[2] = z * ir - G.l[2];
+    }
+    __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(X + v * kFeat);
+    o[0] = __floats2bfloat162_rn(f[v] * G.c2s, phs[v] * G.is);
+    o[1] = __floats2bfloat162_rn(rs[v] * G.c2s, d[0]);
+    o[2] = __floats2bfloat162_rn(d[1], d[2]);
+    o[3] = __floats2bfloat162_rn(0.0f, 0.0f);
+  }
+}
+
+__global__ void f32_to_bf16_kernel(const float* __restrict__ a, bf16* __restrict__ b, size_t n) {
+  for (size_t i = gtid(); i < n; i += gstride()) b[i] = __float2bfloat16(a[i]);
+}
+
+// phi0 = φ_s + s out
+__global__ void axpy_kernel(float* __restrict__ y, const float* __restrict__ x, float s, size_t n) {
+  for (size_t i = gtid(); i < n; i += gstride()) y[i] += s * x[i];
+}
+
+// target = ((φ - mean φ) - φ_s) / s
+__global__ void target_kernel(const float* __restrict__ phi, const float* __restrict__ phs, float mean, float is,
+                              float* __restrict__ t, size_t n) {
+  for (size_t i = gtid(); i < n; i += gstride()) t[i] = ((phi[i] - mean) - phs[i]) * is;
+}
+
+// ---- synthetic fields ------------------------------------------------------
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {   // SplitMix64 finaliser
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ float u01(uint64_t h) { return ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f); }
+
+struct NoiseGeom {
+  int n1, n2, n3, n1h;
+  float kf[3];     // 2π / L per axis
+  float slope2;    // P(k) ∝ k^slope: amplitude ∝ k^(slope/2)
+  float R2h;       // R² / 2 (Gaussian smoothing)
+  uint64_t seed;
+};
+
+// Gaussian random modes: (N1 + i N2) k^(slope/2) exp(-R²k²/2), DC = 0.
+__global__ void noise_kernel(cufftComplex* __restrict__ ck, size_t nk, NoiseGeom G) {
+  for (size_t e = gtid(); e < nk; e += gstride()) {
+    const int i = (int)(e % G.n1h);
+    const size_t r = e / G.n1h;
+    const int j = (int)(r % G.n2), k = (int)(r / G.n2);
+    const int mj = j < (G.n2 + 1) / 2 ? j : j - G.n2;
+    const int mk = k < (G.n3 + 1) / 2 ? k : k - G.n3;
+    const float kx = G.kf[0] * i, ky = G.kf[1] * mj, kz = G.kf[2] * mk;
+    const float k2 = kx * kx + ky * ky + kz * kz;
+    cufftComplex c = make_float2(0.0f, 0.0f);
+    if (k2 > 0.0f) {
+      const uint64_t h1 = mix64(G.seed ^ (2 * e)), h2 = mix64(G.seed ^ (2 * e + 1));
+      // Box-Muller
+      const float rad = sqrtf(-2.0f * logf(u01(h1)));
+      float sn, cs;
+      sincospif(2.0f * u01(h2), &sn, &cs);
+      const float amp = powf(k2, 0.5f * G.slope2) * expf(-G.R2h * k2);
+      c = make_float2(amp * rad * cs, amp * rad * sn);
+    }
+    ck[e] = c;
+  }
+}
+
+struct WindowGeom {
+  int n1, n2;
+  float r2min, r2max;
+  float ra0, ra1, dec0, dec1;   // radians
+  float sig_rms;                // σ_G / rms(G)
+  float half_var;               // σ_G² / 2
+  float ib;                     // 1 / bias
+};
+
+// f = W(x) (exp(σ G/rms - σ²/2) - 1) / b with W the survey window at the cell centre
+__global__ void lognormal_window_kernel(const float* __restrict__ G, const float* __restrict__ ax,
+                                        const float* __restrict__ ay, const float* __restrict__ az,
+                                        WindowGeom W, float* __restrict__ f, size_t nv) {
+  for (size_t v = gtid(); v < nv; v += gstride()) {
+    const int i = (int)(v % W.n1);
+    const size_t r = v / W.n1;
+    const int j = (int)(r % W.n2), k = (int)(r / W.n2);
+    const float x = ax[i], y = ay[j], z = az[k];
+    const float r2 = x * x + y * y + z * z;
+    bool in = r2 >= W.r2min && r2 <= W.r2max;
+    if (in) {
+      const float ra = atan2f(y, x);
+      const float dec = asinf(z * rsqrtf(r2));
+      in = ra >= W.ra0 && ra <= W.ra1 && dec >= W.dec0 && dec <= W.dec1;
+    }
+    f[v] = in ? (expf(W.sig_rms * G[v] - W.half_var) - 1.0f) * W.ib : 0.0f;
+  }
+}
+
+unsigned eblocks(size_t n) {
+  size_t b = (n + 255) / 256;
+  return (unsigned)std::min<size_t>(b, 8 * kNumSMs);
+}
+
+}  // namespace
+
+// ---- the network object ----------------------------------------------------
+
+struct GuessNet {
+  int n = 0;
+  bool has_params = false, frags_ok = false, train_ready = false;
+  float* params = nullptr;   // kP.total
+  float* grads = nullptr;
+  float* adam_m = nullptr;
+  float* adam_v = nullptr;
+  int64_t adam_t = 0;
+  uint2* ffrag[kLayers] = {};
+  uint2* bfrag[kLayers] = {};
+  void* frag_mem = nullptr;
+  bf16* act[T_COUNT] = {};
+  bf16* grad[T_COUNT] = {};
+  void* act_mem = nullptr;
+  void* grad_mem = nullptr;
+  float* out = nullptr;      // head output (N)
+  float* dout = nullptr;
+  float* tgt = nullptr;
+  double* part = nullptr;    // loss partials
+  double* hpart = nullptr;   // pinned
+};
+
+namespace {
+
+size_t nvox(const GuessNet* g, int level) {
+  const size_t m = (size_t)(g->n >> level);
+  return m * m * m;
+}
+
+int net_alloc(baorec_ctx* ctx) {
+  if (ctx->net) return BAOREC_OK;
+  if (!(ctx->n1 == ctx->n2 && ctx->n2 == ctx->n3) || ctx->n1 % 4 != 0)
+    return set_error(ctx, BAOREC_ERR_ARG, "learned guess: needs a cubic mesh with n divisible by 4 (got %d x %d x %d)",
+                     ctx->n1, ctx->n2, ctx->n3);
+  GuessNet* g = new (std::nothrow) GuessNet();
+  if (!g) return set_error(ctx, BAOREC_ERR_NOMEM, "learned guess: host allocation");
+  ctx->net = g;
+  g->n = ctx->n1;
+  CK(cudaMalloc(&g->params, kP.total * sizeof(float)));
+  CK(cudaMemsetAsync(g->params, 0, kP.total * sizeof(float), ctx->stream));
+  size_t nf = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    nf += guess::frag_count(L.kind, L.cin, L.cout);
+    const int k2 = L.kind == DN ? UP : L.kind == UP ? DN : C3;
+    nf += guess::frag_count(k2, L.cout, L.cin);
+  }
+  CK(cudaMalloc(&g->frag_mem, nf * sizeof(uint2)));
+  uint2* fp = (uint2*)g->frag_mem;
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    g->ffrag[l] = fp;
+    fp += guess::frag_count(L.kind, L.cin, L.cout);
+    const int k2 = L.kind == DN ? UP : L.kind == UP ? DN : C3;
+    g->bfrag[l] = fp;
+    fp += guess::frag_count(k2, L.cout, L.cin);
+  }
+  size_t na = 0;
+  for (int t = 0; t < T_COUNT; ++t) na += nvox(g, kTensors[t].level) * kTensors[t].ch;
+  CK(cudaMalloc(&g->act_mem, na * sizeof(bf16)));
+  bf16* ap = (bf16*)g->act_mem;
+  for (int t = 0; t < T_COUNT; ++t) {
+    g->act[t] = ap;
+    ap += nvox(g, kTensors[t].level) * kTensors[t].ch;
+  }
+  const size_t N = nvox(g, 0);
+  CK(cudaMalloc(&g->out, N * sizeof(float)));
+  CK(cudaMalloc(&g->part, kRedBlocksG * sizeof(double)));
+  CK(cudaMallocHost(&g->hpart, kRedBlocksG * sizeof(double)));
+  return BAOREC_OK;
+}
+
+int net_train_alloc(baorec_ctx* ctx) {
+  GuessNet* g = ctx->net;
+  if (g->train_ready) return BAOREC_OK;
+  CK(cudaMalloc(&g->grads, kP.total * sizeof(float)));
+  CK(cudaMalloc(&g->adam_m, kP.total * sizeof(float)));
+  CK(cudaMalloc(&g->adam_v, kP.total * sizeof(float)));
+  CK(cudaMemsetAsync(g->adam_m, 0, kP.total * sizeof(float), ctx->stream));
+  CK(cudaMemsetAsync(g->adam_v, 0, kP.total * sizeof(float), ctx->stream));
+  size_t na = 0;
+  for (int t = 0; t < T_COUNT; ++t) na += nvox(g, kTensors[t].level) * kTensors[t].ch;
+  CK(cudaMalloc(&g->grad_mem, na * sizeof(bf16)));
+  bf16* ap = (bf16*)g->grad_mem;
+  for (int t = 0; t < T_COUNT; ++t) {
+    g->grad[t] = ap;
+    ap += nvox(g, kTensors[t].level) * kTensors[t].ch;
+  }
+  const size_t N = nvox(g, 0);
+  CK(cudaMalloc(&g->dout, N * sizeof(float)));
+  CK(cudaMalloc(&g->tgt, N * sizeof(float)));
+  g->adam_t = 0;
+  g->train_ready = true;
+  return BAOREC_OK;
+}
+
+int net_frags(baorec_ctx* ctx) {
+  GuessNet* g = ctx->net;
+  if (g->frags_ok) return BAOREC_OK;
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    CK(guess::weight_frags(ctx->stream, L.kind, L.cin, L.cout, g->params + kP.w[l], g->ffrag[l], false));
+    ctx->launches++;
+    if (l > 0) {
+      CK(guess::weight_frags(ctx->stream, L.kind, L.cin, L.cout, g->params + kP.w[l], g->bfrag[l], true));
+      ctx->launches++;
+    }
+  }
+  g->frags_ok = true;
+  return BAOREC_OK;
+}
+
+// act[T_X] holds the features; the head output goes to g->out.
+int net_forward(baorec_ctx* ctx) {
+  GuessNet* g = ctx->net;
+  CKS(net_frags(ctx));
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    guess::ConvArgs a;
+    a.in = g->act[L.in_t] + L.in_off;
+    a.in_cs = kTensors[L.in_t].ch;
+    a.out = g->act[L.out_t] + L.out_off;
+    a.out_cs = kTensors[L.out_t].ch;
+    a.add = nullptr;
+    a.add_cs = 0;
+    a.w = g->ffrag[l];
+    a.bias = g->params + kP.b[l];
+    a.relu = 1;
+    a.n_in = g->n >> kTensors[L.in_t].level;
+    a.n_out = g->n >> kTensors[L.out_t].level;
+    CK(guess::conv_forward(ctx->stream, L.kind, L.cin, L.cout, a));
+    ctx->launches++;
+  }
+  head_fwd_kernel<<<eblocks(nvox(g, 0)), 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->out,
+                                                                 nvox(g, 0));
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+// loss and dout from g->out and g->tgt; *loss gets the mean squared error
+int net_loss(baorec_ctx* ctx, double* loss) {
+  GuessNet* g = ctx->net;
+  const size_t N = nvox(g, 0);
+  loss_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->out, g->tgt, g->dout, N, g->part);
+  CKLAUNCH();
+  if (loss) {
+    CK(cudaMemcpyAsync(g->hpart, g->part, kRedBlocksG * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double s = 0.0;
+    for (int b = 0; b < kRedBlocksG; ++b) s += g->hpart[b];
+    *loss = s / (double)N;
+  }
+  return BAOREC_OK;
+}
+
+// accumulates parameter gradients into g->grads from g->dout
+int net_backward(baorec_ctx* ctx) {
+  GuessNet* g = ctx->net;
+  const size_t N = nvox(g, 0);
+  head_bwd_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->dout,
+                                                         g->grad[T_C0], g->grads + kP.w[kLayers], N);
+  CKLAUNCH();
+  for (int l = kLayers - 1; l >= 0; --l) {
+    const LayerDef& L = kNet[l];
+    const int ocs = kTensors[L.out_t].ch, ics = kTensors[L.in_t].ch;
+    const size_t nvo = nvox(g, kTensors[L.out_t].level);
+    bf16* dy = g->grad[L.out_t] + L.out_off;
+    relu_bwd_kernel<<<eblocks(nvo * L.cout / 2), 256, 0, ctx->stream>>>(dy, g->act[L.out_t] + L.out_off, ocs, L.cout, nvo);
+    CKLAUNCH();
+    guess::WgradArgs w;
+    w.in = g->act[L.in_t] + L.in_off;
+    w.in_cs = ics;
+    w.dy = dy;
+    w.dy_cs = ocs;
+    w.dw = g->grads + kP.w[l];
+    w.n_in = g->n >> kTensors[L.in_t].level;
+    w.n_out = g->n >> kTensors[L.out_t].level;
+    CK(guess::conv_wgrad(ctx->stream, L.kind, L.cin, L.cout, w));
+    ctx->launches++;
+    bias_grad_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(dy, ocs, L.cout, nvo, g->grads + kP.b[l]);
+    CKLAUNCH();
+    if (l == 0) break;
+    guess::ConvArgs a;
+    a.in = dy;
+    a.in_cs = ocs;
+    a.out = g->grad[L.in_t] + L.in_off;
+    a.out_cs = ics;
+    a.add = L.acc_grad ? a.out : nullptr;
+    a.add_cs = ics;
+    a.w = g->bfrag[l];
+    a.bias = nullptr;
+    a.relu = 0;
+    a.n_in = w.n_out;
+    a.n_out = w.n_in;
+    const int k2 = L.kind == DN ? UP : L.kind == UP ? DN : C3;
+    CK(guess::conv_forward(ctx->stream, k2, L.cout, L.cin, a));
+    ctx->launches++;
+  }
+  return BAOREC_OK;
+}
+
+// Features of the rhs f into act[T_X]; φ_s = S⁻¹ f into phs; returns s = rms(φ_s).
+int net_features(baorec_ctx* ctx, const float* f, float* phs, float* rs, float* s_out) {
+  GuessNet* g = ctx->net;
+  const size_t N = ctx->N;
+  CKS(spectral_correction(ctx, f, phs));
+  CKS(operator_residual(ctx, phs, f, rs));
+  double ss = 0.0;
+  CKS(sumsq_mesh(ctx, phs, N, &ss));
+  const double rms = sqrt(ss / (double)N);
+  const float s = rms > 0.0 ? (float)rms : 1.0f;
+  FeatGeom G;
+  G.n1 = ctx->n1;
+  G.n2 = ctx->n2;
+  const double cell = (double)ctx->cfg.box_size[0] / ctx->n1;
+  G.c2s = (float)(cell * cell / s);
+  G.is = 1.0f / s;
+  double l[3];
+  mean_los(ctx, l);
+  G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
+  for (int a = 0; a < 3; ++a) G.l[a] = (float)l[a];
+  features_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(f, phs, rs, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], G,
+                                                       g->act[T_X], N);
+  CKLAUNCH();
+  *s_out = s;
+  return BAOREC_OK;
+}
+
+int net_adam(baorec_ctx* ctx, float lr, float gscale) {
+  GuessNet* g = ctx->net;
+  g->adam_t++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = (float)(1.0 - pow((double)b1, (double)g->adam_t));
+  const float c2 = (float)(1.0 - pow((double)b2, (double)g->adam_t));
+  adam_kernel<<<eblocks(kP.total), 256, 0, ctx->stream>>>(g->params, g->grads, g->adam_m, g->adam_v, kP.total, lr,
+                                                          gscale, b1, b2, c1, c2, 1e-8f);
+  CKLAUNCH();
+  g->frags_ok = false;
+  return BAOREC_OK;
+}
+
+int need_params(baorec_ctx* ctx) {
+  if (!ctx->net || !ctx->net->has_params)
+    return set_error(ctx, BAOREC_ERR_ARG, "learned guess: no network parameters (init, set or train them first)");
+  return BAOREC_OK;
+}
+
+// One training pair on this context's mesh: a sub-box at a random origin of
+// the region, lognormal field in the survey window as f, the converged φ.
+int make_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, uint64_t index, float* f, float* phi) {
+  std::mt19937_64 rng(((uint64_t)tc->seed << 32) ^ (index * 0x9E3779B97F4A7C15ull));
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  float bmin[3];
+  for (int a = 0; a < 3; ++a) {
+    const double span = std::max(0.0, (double)tc->region_size[a] - (double)ctx->cfg.box_size[a]);
+    bmin[a] = (float)(tc->region_min[a] + span * U(rng));
+  }
+  CKS(baorec_set_box(ctx, ctx->cfg.box_size, bmin));
+  NoiseGeom NG;
+  NG.n1 = ctx->n1; NG.n2 = ctx->n2; NG.n3 = ctx->n3; NG.n1h = ctx->n1h;
+  for (int a = 0; a < 3; ++a) NG.kf[a] = (float)(2.0 * M_PI / ctx->cfg.box_size[a]);
+  NG.slope2 = 0.5f * tc->pk_slope;
+  NG.R2h = 0.5f * ctx->cfg.smoothing_radius * ctx->cfg.smoothing_radius;
+  NG.seed = mix64(((uint64_t)tc->seed << 20) + index);
+  noise_kernel<<<eblocks(ctx->Nk), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, NG);
+  CKLAUNCH();
+  float* G = ctx->psi;   // scratch
+  CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, G));
+  double ss = 0.0;
+  CKS(sumsq_mesh(ctx, G, ctx->N, &ss));
+  const double rms = sqrt(ss / (double)ctx->N);
+  WindowGeom W;
+  W.n1 = ctx->n1; W.n2 = ctx->n2;
+  W.r2min = tc->r_min * tc->r_min;
+  W.r2max = tc->r_max * tc->r_max;
+  const double d2r = M_PI / 180.0;
+  W.ra0 = (float)(tc->ra_min * d2r); W.ra1 = (float)(tc->ra_max * d2r);
+  W.dec0 = (float)(tc->dec_min * d2r); W.dec1 = (float)(tc->dec_max * d2r);
+  W.sig_rms = rms > 0.0 ? (float)(tc->sigma_g / rms) : 0.0f;
+  W.half_var = 0.5f * tc->sigma_g * tc->sigma_g;
+  W.ib = 1.0f / ctx->cfg.bias;
+  lognormal_window_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(G, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], W, f,
+                                                                    ctx->N);
+  CKLAUNCH();
+  const baorec_config saved = ctx->cfg;
+  ctx->cfg.mg_start = BAOREC_START_SPECTRAL;
+  ctx->cfg.rtol = tc->rtol;
+  const int st = mg_solve(ctx, f, phi, nullptr, nullptr);
+  ctx->cfg = saved;
+  if (st != BAOREC_OK) return st;
+  return BAOREC_OK;
+}
+
+}  // namespace
+
+void guess_free(baorec_ctx* ctx) {
+  GuessNet* g = ctx->net;
+  if (!g) return;
+  cudaFree(g->params);
+  cudaFree(g->grads);
+  cudaFree(g->adam_m);
+  cudaFree(g->adam_v);
+  cudaFree(g->frag_mem);
+  cudaFree(g->act_mem);
+  cudaFree(g->grad_mem);
+  cudaFree(g->out);
+  cudaFree(g->dout);
+  cudaFree(g->tgt);
+  cudaFree(g->part);
+  cudaFreeHost(g->hpart);
+  delete g;
+  ctx->net = nullptr;
+}
+
+// φ0 = φ_s + s net(features(f)) into phi0 (device meshes of the context's size)
+int guess_apply(baorec_ctx* ctx, const float* f, float* phi0) {
+  CKS(need_params(ctx));
+  CKS(mg_setup(ctx));
+  float s = 1.0f;
+  CKS(net_features(ctx, f, phi0, ctx->lev[0].r, &s));
+  CKS(net_forward(ctx));
+  axpy_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(phi0, ctx->net->out, s, ctx->N);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+}  // namespace baorec
+
+using namespace baorec;
+
+static_assert(sizeof(baorec_guess_train_config) == 4 * 19, "baorec_guess_train_config layout is part of the ABI");
+
+extern "C" int64_t baorec_guess_num_params(void) { return (int64_t)kP.total; }
+
+extern "C" int baorec_guess_init(baorec_ctx* ctx, uint32_t seed) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  CKS(net_alloc(ctx));
+  std::mt19937_64 rng(seed);
+  std::vector<float> p(kP.total, 0.0f);
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    const int fan_in = guess::taps_of(L.kind) * L.cin;
+    std::normal_distribution<double> nd(0.0, sqrt(2.0 / fan_in));   // He initialisation
+    const size_t nw = (size_t)guess::taps_of(L.kind) * L.cin * L.cout;
+    for (size_t i = 0; i < nw; ++i) p[kP.w[l] + i] = (float)nd(rng);
+  }
+  // a small head: the untrained network starts close to the FFT start
+  std::normal_distribution<double> nh(0.0, 1e-3);
+  for (int c = 0; c < kHeadIn; ++c) p[kP.w[kLayers] + c] = (float)nh(rng);
+  CK(cudaMemcpyAsync(ctx->net->params, p.data(), p.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->net->has_params = true;
+  ctx->net->frags_ok = false;
+  ctx->net->adam_t = 0;
+  if (ctx->net->train_ready) {
+    CK(cudaMemsetAsync(ctx->net->adam_m, 0, kP.total * 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->net->adam_v, 0, kP.total * 4, ctx->stream));
+  }
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int64_t n) {
+  if (!ctx || !params) return BAOREC_ERR_ARG;
+  if (n != (int64_t)kP.total)
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_set_params: %lld values, the network has %zu", (long long)n, kP.total);
+  CKS(net_alloc(ctx));
+  CK(cudaMemcpyAsync(ctx->net->params, params, kP.total * 4, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->net->has_params = true;
+  ctx->net->frags_ok = false;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n) {
+  if (!ctx || !params) return BAOREC_ERR_ARG;
+  CKS(need_params(ctx));
+  if (n != (int64_t)kP.total)
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_get_params: room for %lld values, the network has %zu", (long long)n,
+                     kP.total);
+  CK(cudaMemcpyAsync(params, ctx->net->params, kP.total * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* target, float* out,
+                                 float* grads, double* loss) {
+  if (!ctx || !features || !out) return BAOREC_ERR_ARG;
+  CKS(need_params(ctx));
+  GuessNet* g = ctx->net;
+  const size_t N = ctx->N;
+  f32_to_bf16_kernel<<<eblocks(N * kFeat), 256, 0, ctx->stream>>>(features, g->act[T_X], N * kFeat);
+  CKLAUNCH();
+  CKS(net_forward(ctx));
+  CK(cudaMemcpyAsync(out, g->out, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (target) {
+    CKS(net_train_alloc(ctx));
+    CK(cudaMemcpyAsync(g->tgt, target, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    double l = 0.0;
+    CKS(net_loss(ctx, &l));
+    if (loss) *loss = l;
+    if (grads) {
+      CK(cudaMemsetAsync(g->grads, 0, kP.total * 4, ctx->stream));
+      CKS(net_backward(ctx));
+      CK(cudaMemcpyAsync(grads, g->grads, kP.total * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+  }
+  return finish(ctx, 0);
+}
+
+extern "C" int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0) {
+  if (!ctx || !f || !phi0) return BAOREC_ERR_ARG;
+  CKS(guess_apply(ctx, f, phi0));
+  return finish(ctx, 0);
+}
+
+extern "C" int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index, float* f,
+                                   float* phi) {
+  if (!ctx || !tc || !f || !phi) return BAOREC_ERR_ARG;
+  CKS(mg_setup(ctx));
+  CKS(make_sample(ctx, tc, (uint64_t)index, f, phi));
+  return finish(ctx, 0);
+}
+
+extern "C" int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history) {
+  if (!ctx || !tc || tc->steps < 0 || tc->batch < 1) return set_error(ctx, BAOREC_ERR_ARG, "guess_train: bad config");
+  CKS(need_params(ctx));
+  CKS(net_train_alloc(ctx));
+  CKS(mg_setup(ctx));
+  GuessNet* g = ctx->net;
+  const size_t N = ctx->N;
+  float* f = ctx->mesh3 + N;       // B
+  float* phi = ctx->mesh3;         // A
+  float* phs = ctx->mesh3 + 2 * N; // C
+  const float saved_box[3] = {ctx->cfg.box_min[0], ctx->cfg.box_min[1], ctx->cfg.box_min[2]};
+  uint64_t index = 0;
+  for (int step = 0; step < tc->steps; ++step) {
+    CK(cudaMemsetAsync(g->grads, 0, kP.total * 4, ctx->stream));
+    double lsum = 0.0;
+    for (int b = 0; b < tc->batch; ++b) {
+      CKS(make_sample(ctx, tc, index++, f, phi));
+      float s = 1.0f;
+      CKS(net_features(ctx, f, phs, ctx->lev[0].r, &s));
+      double mphi = 0.0;
+      CKS(sum_mesh(ctx, phi, N, &mphi));
+      target_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(phi, phs, (float)(mphi / (double)N), 1.0f / s, g->tgt, N);
+      CKLAUNCH();
+      CKS(net_forward(ctx));
+      double l = 0.0;
+      CKS(net_loss(ctx, loss_history ? &l : nullptr));
+      lsum += l;
+      CKS(net_backward(ctx));
+    }
+    CKS(net_adam(ctx, tc->lr, 1.0f / (float)tc->batch));
+    if (loss_history) loss_history[step] = (float)(lsum / tc->batch);
+  }
+  CKS(baorec_set_box(ctx, ctx->cfg.box_size, saved_box));
+  ctx->has_result = false;
+  return finish(ctx, 0);
+}

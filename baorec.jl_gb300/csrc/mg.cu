@@ -393,7 +393,11 @@ int mg_update_tables(baorec_ctx* ctx) {
           }
     }
   }
-  return coarse_setup(ctx);
+  // the dense inverse is built when a V-cycle first needs it (a box change
+  // between spectral-only solves costs no host elimination)
+  if (ctx->coarse_M) { cudaFree(ctx->coarse_M); ctx->coarse_M = nullptr; }
+  ctx->coarse_dirty = true;
+  return BAOREC_OK;
 }
 
 // Dense FP64 inverse for the coarsest level (the "FP64 coarsest solve"): the
@@ -403,6 +407,7 @@ int mg_update_tables(baorec_ctx* ctx) {
 // Gauss-Jordan elimination with partial pivoting.  Geometry only: recomputed
 // when the box changes.
 int coarse_setup(baorec_ctx* ctx) {
+  ctx->coarse_dirty = false;
   if (ctx->coarse_M) { cudaFree(ctx->coarse_M); ctx->coarse_M = nullptr; }
   // the first level small enough for the dense inverse ends the residual-driven V-cycles
   ctx->dense_level = -1;
@@ -615,6 +620,7 @@ static int smooth_rb(baorec_ctx* ctx, int lvl, const LG& G, float shift, int nsw
 }
 
 static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
+  if (ctx->coarse_dirty) CKS(coarse_setup(ctx));
   baorec::Level& L = ctx->lev[lvl];
   LG G = level_geom(ctx, lvl, kClamp);
   const size_t N = L.N;
@@ -678,6 +684,21 @@ static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
   return smooth_rb(ctx, lvl, G, shift, ctx->cfg.nu2);
 }
 
+int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r) {
+  CKS(mg_setup(ctx));
+  const baorec::Level& L0 = ctx->lev[0];
+  LG G = level_geom(ctx, 0, 0.0f);
+  const bool aligned = (uintptr_t)v % 16 == 0;
+  if (aligned && tile_ok(L0.n)) {
+    CK(launch_resid_diff(ctx->stream, v, f, r, G, nullptr));
+    ctx->launches++;
+  } else {
+    residual_diff_kernel<<<blocks_for(L0.N), 256, 0, ctx->stream>>>(v, f, r, G, L0.N, nullptr);
+    CKLAUNCH();
+  }
+  return BAOREC_OK;
+}
+
 int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st) {
   CKS(mg_setup(ctx));
   baorec::Level& L0 = ctx->lev[0];
@@ -691,7 +712,8 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   float* loA = ctx->phi_lo;
   float* loB = ctx->phi_lo2;
   if (phi0 && phi0 != phi) CK(cudaMemcpyAsync(hiA, phi0, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-  if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
+  if (!phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED) CKS(guess_apply(ctx, f, hiA));
+  else if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
   CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
   double alpha = sf / (double)N;
   LG G = level_geom(ctx, 0, 0.0f);

@@ -272,6 +272,44 @@ int baorec_reconstructed_positions(baorec_ctx* ctx, const float* x, const float*
                                    const float* z, int64_t n, int field,
                                    float* ox, float* oy, float* oz, uint32_t flags);
 
+/* ---- Learned initial guess (no reference counterpart) ----------------------
+ * A 3-level 3-D U-Net (16/32/64 channels, BF16 weights and activations, FP32
+ * accumulation) predicts the error of the FFT start of the residual-driven
+ * solve; BAOREC_START_LEARNED uses it.  Meshes must be cubic with n % 4 == 0.
+ * Training draws sub-boxes of `region` with this context's box size, fills
+ * each with a lognormal field (Gaussian field with P(k) ∝ k^pk_slope smoothed
+ * with the context's smoothing radius, RMS sigma_g before the transform) in
+ * the survey window (comoving r, RA, Dec in degrees; the observer at the
+ * origin), divides by the bias, and solves it to `rtol` for the target. */
+typedef struct {
+  int32_t steps, batch;      /* Adam steps; fields per step */
+  float lr;                  /* Adam learning rate */
+  uint32_t seed;
+  float sigma_g, pk_slope;
+  float region_min[3], region_size[3];
+  float r_min, r_max, ra_min, ra_max, dec_min, dec_max;
+  float rtol;                /* solver tolerance of the targets */
+} baorec_guess_train_config;
+
+int64_t baorec_guess_num_params(void);
+/* He-initialised weights (the head starts near zero: the guess starts as the FFT start). */
+int baorec_guess_init(baorec_ctx* ctx, uint32_t seed);
+/* FP32 parameters, host arrays of baorec_guess_num_params() values. */
+int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int64_t n);
+int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n);
+/* Network forward on device features (N x 8 FP32, channels fastest) into
+ * out (N, device); with a target (N, device) also the MSE loss and, when
+ * grads (host, num_params) is given, the parameter gradients. */
+int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* target, float* out,
+                      float* grads, double* loss);
+/* phi0 = FFT start + learned correction for the right-hand side f (device meshes). */
+int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
+/* One training pair (device meshes f and its solution phi); moves the box. */
+int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index,
+                        float* f, float* phi);
+/* Train on the device; loss_history (host, steps values) may be NULL. */
+int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history);
+
 #ifdef __cplusplus
 }
 #endif
