@@ -9,6 +9,7 @@ by the CUDA library ``libbaorec_gb300.so`` (C ABI: ``include/baorec_gb300.h``).
 from .recon import *  # noqa: F401,F403
 from .recon import __all__ as _recon_all
 from . import mocks  # noqa: F401
+from . import guess  # noqa: F401
 from ._lib import load as load_library, lib_path  # noqa: F401
 
-__all__ = list(_recon_all) + ["mocks", "load_library", "lib_path"]
+__all__ = list(_recon_all) + ["mocks", "guess", "load_library", "lib_path"]

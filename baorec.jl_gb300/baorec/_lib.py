@@ -54,7 +54,7 @@ class GuessTrainConfig(C.Structure):
                 ("sigma_g", C.c_float), ("pk_slope", C.c_float), ("region_min", C.c_float * 3),
                 ("region_size", C.c_float * 3), ("r_min", C.c_float), ("r_max", C.c_float),
                 ("ra_min", C.c_float), ("ra_max", C.c_float), ("dec_min", C.c_float), ("dec_max", C.c_float),
-                ("rtol", C.c_float)]
+                ("rtol", C.c_float), ("loss", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -99,6 +99,7 @@ _SIGS = {
     "baorec_mg_solve": (C.c_int, [P, P, P, P, C.POINTER(SolveStats)]),
     "baorec_last_solve_stats": (C.c_int, [P, C.POINTER(SolveStats)]),
     "baorec_solve_history": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int]),
+    "baorec_start_residual": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_double)]),
     "baorec_profile_kernel": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_reconstructed_overdensity": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
     "baorec_reconstructed_potential": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
@@ -110,7 +111,7 @@ _SIGS = {
     "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
     "baorec_guess_set_params": (C.c_int, [P, P, I64]),
     "baorec_guess_get_params": (C.c_int, [P, P, I64]),
-    "baorec_guess_eval": (C.c_int, [P, P, P, P, P, C.POINTER(C.c_double)]),
+    "baorec_guess_eval": (C.c_int, [P, P, P, P, P, C.POINTER(C.c_double), C.c_int]),
     "baorec_guess_apply": (C.c_int, [P, P, P]),
     "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
     "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),

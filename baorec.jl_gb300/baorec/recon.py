@@ -89,6 +89,7 @@ class MultigridRecon:
     max_cycles: int = 50
     start: str = "zero"                  # convergent mode: "zero" | "spectral" | "learned"
     start_rate: float = 0.5
+    guess_params: object = None          # learned start: network parameters (baorec.guess)
     solve_stats: dict = dc_field(default_factory=dict)
 
     def __post_init__(self):
@@ -96,6 +97,8 @@ class MultigridRecon:
             self.beta = float(F32(F32(self.f) / F32(self.bias)))
         if self.start not in _STARTS:
             raise ValueError(f"start must be one of {sorted(_STARTS)}, got {self.start!r}")
+        if self.start == "learned" and self.guess_params is None:
+            raise ValueError("start='learned' needs guess_params (see baorec.guess)")
 
 
 # ----------------------------------------------------------------------------
@@ -280,6 +283,9 @@ def _ctx(recon, shape, ran_min=0.01) -> _lib.Context:
             ctx.close()
         ctx = _lib.Context(cfg)
         recon.fft_plan = ctx
+        if getattr(recon, "guess_params", None) is not None:
+            p = np.ascontiguousarray(recon.guess_params, dtype=np.float32)
+            ctx.call("baorec_guess_set_params", p.ctypes.data, p.size)
     elif recon.box_size is not None and recon.box_min is not None:
         bs, bm = ctx.box()
         if list(bs) != [float(F32(v)) for v in recon.box_size] or list(bm) != [float(F32(v)) for v in recon.box_min]:

@@ -475,6 +475,13 @@ extern "C" int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats
   return BAOREC_OK;
 }
 
+extern "C" int baorec_start_residual(baorec_ctx* ctx, const float* f, int start, double* rel_residual) {
+  if (!ctx || !f || !rel_residual || start < BAOREC_START_ZERO || start > BAOREC_START_LEARNED)
+    return set_error(ctx, BAOREC_ERR_ARG, "start_residual: bad arguments");
+  CKS(start_residual(ctx, f, start, rel_residual));
+  return finish(ctx, 0);
+}
+
 extern "C" int baorec_solve_history(const baorec_ctx* ctx, double* rho, int32_t* kind, int cap) {
   if (!ctx || cap < 0 || (cap > 0 && (!rho || !kind))) return -BAOREC_ERR_ARG;
   const int n = (int)ctx->hist_rho.size();

@@ -159,6 +159,7 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
 bool mean_los(const baorec_ctx* c, double l[3]);
 // r = f - A v with the finest level's exact operator (difference form, FP32).
 int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r);
+int start_residual(baorec_ctx* ctx, const float* f, int start, double* rel);
 // learned initial guess (guess_net.cu)
 int guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
 void guess_free(baorec_ctx* ctx);

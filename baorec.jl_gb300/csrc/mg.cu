@@ -699,6 +699,28 @@ int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r)
   return BAOREC_OK;
 }
 
+// Relative residual |r - mean r| / |f - mean f|, r = f - A φ0, of a start φ0
+// for the right-hand side f: zero, the FFT start S⁻¹ f, or the learned one.
+int start_residual(baorec_ctx* ctx, const float* f, int start, double* rel) {
+  CKS(mg_setup(ctx));
+  baorec::Level& L0 = ctx->lev[0];
+  const size_t N = L0.N;
+  float* v = L0.v;
+  float* r = L0.r + N;
+  if (start == BAOREC_START_ZERO) CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
+  else if (start == BAOREC_START_SPECTRAL) CKS(spectral_correction(ctx, f, v));
+  else CKS(guess_apply(ctx, f, v));
+  CKS(operator_residual(ctx, v, f, r));
+  double sf = 0.0, sf2 = 0.0, sr = 0.0, sr2 = 0.0;
+  CKS(sum_mesh(ctx, f, N, &sf));
+  CKS(sumsq_mesh(ctx, f, N, &sf2));
+  CKS(sum_mesh(ctx, r, N, &sr));
+  CKS(sumsq_mesh(ctx, r, N, &sr2));
+  const double den = sf2 - sf * sf / (double)N;
+  *rel = den > 0.0 ? sqrt(std::max(0.0, sr2 - sr * sr / (double)N) / den) : 0.0;
+  return BAOREC_OK;
+}
+
 int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st) {
   CKS(mg_setup(ctx));
   baorec::Level& L0 = ctx->lev[0];

@@ -226,6 +226,9 @@ int baorec_last_solve_stats(const baorec_ctx* ctx, baorec_solve_stats* stats);
  * (kind[i]: 0 = V-cycle, m > 0 = m FFT corrections, -1 = none, the last
  * entry).  Copies min(count, cap) entries and returns count (or < 0 on error). */
 int baorec_solve_history(const baorec_ctx* ctx, double* rho, int32_t* kind, int cap);
+/* Relative residual |r - mean r| / |f - mean f| of the start of kind
+ * BAOREC_START_* (zero, FFT, learned) for the right-hand side f (device mesh). */
+int baorec_start_residual(baorec_ctx* ctx, const float* f, int start, double* rel_residual);
 
 /* reconstructed_overdensity! (src/recon.jl:93-132): overdensity then n_iter
  * iterations into the context result.  rx.. may be NULL (data only). */
@@ -289,6 +292,7 @@ typedef struct {
   float region_min[3], region_size[3];
   float r_min, r_max, ra_min, ra_max, dec_min, dec_max;
   float rtol;                /* solver tolerance of the targets */
+  int32_t loss;              /* 0: MSE of the potential error; 1: MSE of its 7-point Laplacian */
 } baorec_guess_train_config;
 
 int64_t baorec_guess_num_params(void);
@@ -298,10 +302,11 @@ int baorec_guess_init(baorec_ctx* ctx, uint32_t seed);
 int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int64_t n);
 int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n);
 /* Network forward on device features (N x 8 FP32, channels fastest) into
- * out (N, device); with a target (N, device) also the MSE loss and, when
- * grads (host, num_params) is given, the parameter gradients. */
+ * out (N, device); with a target (N, device) also the loss (loss_kind as in
+ * baorec_guess_train_config.loss) and, when grads (host, num_params) is
+ * given, the parameter gradients. */
 int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* target, float* out,
-                      float* grads, double* loss);
+                      float* grads, double* loss, int loss_kind);
 /* phi0 = FFT start + learned correction for the right-hand side f (device meshes). */
 int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
 /* One training pair (device meshes f and its solution phi); moves the box. */

@@ -136,15 +136,26 @@ def forward(params, feats, n, bf16=True):
     return out, act
 
 
-def loss_and_grads(params, feats, target, n, bf16=True):
-    """MSE loss, head output and the flat parameter gradient."""
+def laplacian(a):
+    """7-point Laplacian on the periodic mesh (cell units)."""
+    return sum(np.roll(a, s, axis=ax) for ax in range(3) for s in (1, -1)) - 6.0 * a
+
+
+def loss_and_grads(params, feats, target, n, bf16=True, loss="mse"):
+    """Loss (MSE of the error, or of its Laplacian), head output and the flat
+    parameter gradient."""
     ws, bs = unpack(params, bf16)
     rnd = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
     out, act = forward(params, feats, n, bf16)
     N = out.size
     d = out - target
-    loss = float(np.mean(d * d))
-    dout = 2.0 * d / N
+    if loss == "laplacian":
+        q = laplacian(d)
+        loss = float(np.mean(q * q))
+        dout = 2.0 * laplacian(q) / N
+    else:
+        loss = float(np.mean(d * d))
+        dout = 2.0 * d / N
     lay, total = layout()
     grad = np.zeros(total)
     gr = {k: np.zeros_like(v) for k, v in act.items()}

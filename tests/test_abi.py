@@ -52,4 +52,4 @@ def test_struct_layout_matches_header(lib):
     # 31 four-byte words; api.cu static_asserts the same size on the C side
     assert ctypes.sizeof(_lib.Config) == 4 * 31
     assert ctypes.sizeof(_lib.SolveStats) == 32
-    assert ctypes.sizeof(_lib.GuessTrainConfig) == 4 * 19
+    assert ctypes.sizeof(_lib.GuessTrainConfig) == 4 * 20

@@ -21,14 +21,14 @@ def test_param_count_matches_library(lib):
     assert lib.baorec_guess_num_params() == G.num_params() == 431969
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_backward_matches_finite_differences(seed):
+@pytest.mark.parametrize("seed,loss", [(0, "mse"), (1, "laplacian")])
+def test_backward_matches_finite_differences(seed, loss):
     n = 8
     rng = np.random.default_rng(seed)
     p = G.init_params(seed, head_scale=0.3)
     feats = rng.normal(size=(n, n, n, 8))
     target = rng.normal(size=(n, n, n))
-    loss, _, grad = G.loss_and_grads(p, feats, target, n, bf16=False)
+    _, _, grad = G.loss_and_grads(p, feats, target, n, bf16=False, loss=loss)
     lay, total = G.layout()
     # a few weights and the bias of every layer, and the head
     idx = []
@@ -39,7 +39,7 @@ def test_backward_matches_finite_differences(seed):
         pp, pm = p.copy(), p.copy()
         pp[i] += eps
         pm[i] -= eps
-        lp = G.loss_and_grads(pp, feats, target, n, bf16=False)[0]
-        lm = G.loss_and_grads(pm, feats, target, n, bf16=False)[0]
+        lp = G.loss_and_grads(pp, feats, target, n, bf16=False, loss=loss)[0]
+        lm = G.loss_and_grads(pm, feats, target, n, bf16=False, loss=loss)[0]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - grad[i]) <= 1e-5 * max(1e-3, abs(fd)) + 1e-9, (i, fd, grad[i])
