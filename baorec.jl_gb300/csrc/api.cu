@@ -228,6 +228,7 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   for (int a = 0; a < 3; ++a) cudaFree(ctx->xvec[a]);
   cudaFree(ctx->phi_lo);
   cudaFree(ctx->coarse_M);
+  cudaFree(ctx->stab);
   guess_free(ctx);
   for (int l = 0; l < ctx->nlev; ++l) {
     cudaFree(ctx->lev[l].f);

@@ -56,6 +56,7 @@ struct baorec_ctx {
   bool psi_valid = false;              // psi[0..2] hold the displacement of `result`
   cufftComplex* ck = nullptr;          // complex work: 6 spectra
   float* xvec[3] = {nullptr, nullptr, nullptr};   // x_vec of the mesh (device)
+  float* stab = nullptr;               // per-axis sine tables of the FFT preconditioner (device)
   float* phi_lo = nullptr;             // low part of the double-float solution
   float* phi_lo2 = nullptr;            // ping-pong partners of the solution pair
   float* phi_hi2 = nullptr;

@@ -448,25 +448,53 @@ SGeom sgeom_of(const baorec_ctx* c) {
   return g;
 }
 
-__global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, size_t nk, SGeom g) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nk; e += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e % g.n1h);
-    const size_t q = e / g.n1h;
-    const int j = (int)(q % g.n2), k = (int)(q / g.n2);
-    const int mj = j < (g.n2 + 1) / 2 ? j : j - g.n2;
-    const int mk = k < (g.n3 + 1) / 2 ? k : k - g.n3;
-    // sin(θ/2) and sin θ with θ = 2π m / n, through sinpi for exact arguments
-    const float hx = sinpif((float)i / (float)g.n1), hy = sinpif((float)mj / (float)g.n2);
-    const float hz = sinpif((float)mk / (float)g.n3);
-    const float sx = sinpif(2.0f * (float)i / (float)g.n1), sy = sinpif(2.0f * (float)mj / (float)g.n2);
-    const float sz = sinpif(2.0f * (float)mk / (float)g.n3);
-    const float A = g.diag[0] * hx * hx + g.diag[1] * hy * hy + g.diag[2] * hz * hz + g.cross[0] * sx * sy +
-                    g.cross[1] * sx * sz + g.cross[2] * sy * sz;
-    const float s = e == 0 ? 0.0f : g.invN / A;
-    cufftComplex v = a[e];
-    v.x *= s; v.y *= s;
-    a[e] = v;
+// Per-axis tables sin²(π m/n) and sin(2π m/n) (m the signed frequency):
+// tab = hx2[n1h] | sx[n1h] | hy2[n2] | sy[n2] | hz2[n3] | sz[n3].  Two k-space
+// rows (fixed j, k) per 256-thread block, x along the threads.
+__global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, SGeom g, const float* __restrict__ tab) {
+  const float* hx2 = tab;
+  const float* sx = hx2 + g.n1h;
+  const float* hy2 = sx + g.n1h;
+  const float* sy = hy2 + g.n2;
+  const float* hz2 = sy + g.n2;
+  const float* sz = hz2 + g.n3;
+  const size_t rows = (size_t)g.n2 * g.n3;
+  for (size_t row = 2 * (size_t)blockIdx.x + (threadIdx.x >> 7); row < rows; row += 2 * (size_t)gridDim.x) {
+    const int j = (int)(row % g.n2), k = (int)(row / g.n2);
+    const float syj = __ldg(sy + j), szk = __ldg(sz + k);
+    const float ryz = g.diag[1] * __ldg(hy2 + j) + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk;
+    const float cx = g.cross[0] * syj + g.cross[1] * szk;
+    cufftComplex* ar = a + row * g.n1h;
+    for (int i = threadIdx.x & 127; i < g.n1h; i += 128) {
+      const float A = ryz + g.diag[0] * __ldg(hx2 + i) + cx * __ldg(sx + i);
+      const float s = (row == 0 && i == 0) ? 0.0f : g.invN / A;
+      cufftComplex v = ar[i];
+      v.x *= s; v.y *= s;
+      ar[i] = v;
+    }
   }
+}
+
+int spectral_tables(baorec_ctx* ctx) {
+  if (ctx->stab) return BAOREC_OK;
+  const int n[3] = {ctx->n1, ctx->n2, ctx->n3};
+  const int len[3] = {ctx->n1h, ctx->n2, ctx->n3};
+  std::vector<float> t;
+  for (int a = 0; a < 3; ++a) {
+    std::vector<float> h(len[a]), sn(len[a]);
+    for (int m = 0; m < len[a]; ++m) {
+      const int f = (a == 0 || m < (n[a] + 1) / 2) ? m : m - n[a];
+      const double th = 2.0 * 3.14159265358979323846 * (double)f / (double)n[a];
+      const double hh = sin(0.5 * th);
+      h[m] = (float)(hh * hh);
+      sn[m] = (float)sin(th);
+    }
+    t.insert(t.end(), h.begin(), h.end());
+    t.insert(t.end(), sn.begin(), sn.end());
+  }
+  CK(cudaMalloc(&ctx->stab, t.size() * sizeof(float)));
+  CK(cudaMemcpy(ctx->stab, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return BAOREC_OK;
 }
 
 }  // namespace
@@ -475,8 +503,11 @@ __global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, size_t nk,
 // r is read only; e may not alias r.
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   SGeom g = sgeom_of(ctx);
+  CKS(spectral_tables(ctx));
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));
-  spectral_inverse_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, g);
+  const size_t rows = (size_t)ctx->n2 * ctx->n3;
+  const unsigned blocks = (unsigned)std::min<size_t>((rows + 1) / 2, 16 * kNumSMs);
+  spectral_inverse_kernel<<<blocks, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab);
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, e));
   return BAOREC_OK;

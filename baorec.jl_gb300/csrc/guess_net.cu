@@ -10,8 +10,9 @@
 // 3x3x3 convolutions, strided 2x2x2 down/up-sampling, skip connections by
 // channel concatenation, ReLU, a 1x1x1 linear head; 431,969 parameters).
 // Training runs on the device: synthetic lognormal fields in the survey
-// window of random sub-boxes, targets from the residual-driven solver, MSE
-// loss, Adam.  Parameters are FP32 masters; the convolutions read BF16
+// window of random sub-boxes, targets from the residual-driven solver, the
+// mean squared error of the potential or of its 7-point Laplacian as loss,
+// Adam.  Parameters are FP32 masters; the convolutions read BF16
 // copies in tensor-core fragment order.
 #include <math.h>
 
