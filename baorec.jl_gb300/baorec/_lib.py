@@ -57,6 +57,12 @@ class GuessTrainConfig(C.Structure):
                 ("rtol", C.c_float), ("loss", C.c_int32)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("w", C.c_void_p), ("n", C.c_int64),
+                ("mesh", C.c_int32), ("box_size", C.c_float), ("mas", C.c_int32), ("smoothing_radius", C.c_float),
+                ("field", C.c_int32), ("out_x", C.c_void_p), ("out_y", C.c_void_p), ("out_z", C.c_void_p)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("cycles", C.c_int32), ("spectral_steps", C.c_int32), ("rel_residual", C.c_double), ("alpha", C.c_double),
                 ("rel_residual_initial", C.c_double)]
@@ -107,6 +113,13 @@ _SIGS = {
     "baorec_get_result": (C.c_int, [P, P, U32]),
     "baorec_set_result": (C.c_int, [P, P, U32]),
     "baorec_displacement_meshes": (C.c_int, [P, P, P, P]),
+    "baorec_batch_create": (C.c_int, [C.POINTER(Config), C.POINTER(BatchItem), C.c_int, C.POINTER(P)]),
+    "baorec_batch_launch": (C.c_int, [P]),
+    "baorec_batch_sync": (C.c_int, [P]),
+    "baorec_batch_stream": (P, [P]),
+    "baorec_batch_kernel_launches": (I64, [P]),
+    "baorec_batch_last_error": (C.c_char_p, [P]),
+    "baorec_batch_destroy": (C.c_int, [P]),
     "baorec_guess_num_params": (I64, []),
     "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
     "baorec_guess_set_params": (C.c_int, [P, P, I64]),

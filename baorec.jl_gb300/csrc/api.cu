@@ -344,6 +344,8 @@ struct Staged {
   const float *x, *y, *z, *w, *rx, *ry, *rz, *rw;
 };
 
+static int ensure_psi(baorec_ctx* ctx);
+
 static int stage_catalogs(baorec_ctx* ctx, const float* x, const float* y, const float* z, const float* w, int64_t n,
                           const float* rx, const float* ry, const float* rz, const float* rw, int64_t nr,
                           uint32_t flags, Staged* s) {
@@ -506,6 +508,19 @@ static int recon_iterative(baorec_ctx* ctx, const Staged& s, int64_t n, int64_t 
   ctx->has_result = true;
   ctx->psi_valid = false;
   return BAOREC_OK;
+}
+
+// Device-pointer, host-sync-free forms for graph capture (batch.cu): the
+// data-only iterative reconstruction and the shifted positions.
+int baorec::reconstruct_iterative_device(baorec_ctx* ctx, float* x, float* y, float* z, const float* w, int64_t n) {
+  Staged s = {x, y, z, w, nullptr, nullptr, nullptr, nullptr};
+  return recon_iterative(ctx, s, n, 0, BAOREC_ASYNC);
+}
+
+int baorec::positions_device(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
+                             float* ox, float* oy, float* oz) {
+  CKS(ensure_psi(ctx));
+  return readout(ctx, ctx->psi, x, y, z, n, field, 1, ox, oy, oz);
 }
 
 // reconstructed_potential! (src/recon.jl:184-212) into ctx->result.

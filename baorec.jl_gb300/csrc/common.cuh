@@ -37,7 +37,11 @@ struct DevBuf {                       // a growable device buffer
   size_t bytes = 0;
 };
 
-struct GuessNet;                      // learned initial guess (guess_net.cu)
+struct GuessNet;                      // capture-safe device forms of the iterative reconstruction and the read-out (api.cu)
+int reconstruct_iterative_device(baorec_ctx* ctx, float* x, float* y, float* z, const float* w, int64_t n);
+int positions_device(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
+                     float* ox, float* oy, float* oz);
+// learned initial guess (guess_net.cu)
 
 }  // namespace baorec
 
@@ -161,6 +165,10 @@ bool mean_los(const baorec_ctx* c, double l[3]);
 // r = f - A v with the finest level's exact operator (difference form, FP32).
 int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r);
 int start_residual(baorec_ctx* ctx, const float* f, int start, double* rel);
+// capture-safe device forms of the iterative reconstruction and the read-out (api.cu)
+int reconstruct_iterative_device(baorec_ctx* ctx, float* x, float* y, float* z, const float* w, int64_t n);
+int positions_device(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
+                     float* ox, float* oy, float* oz);
 // learned initial guess (guess_net.cu)
 int guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
 void guess_free(baorec_ctx* ctx);

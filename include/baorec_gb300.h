@@ -315,6 +315,40 @@ int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, in
 /* Train on the device; loss_history (host, steps values) may be NULL. */
 int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history);
 
+/* ---- Batched box reconstructions in one CUDA graph (no reference counterpart) ----
+ * Each item is one periodic-box mock (device arrays; positions in [0, box),
+ * wrapped in place by the paint as cic! with wrap does) reconstructed with
+ * the iterative method of `base` (bias, f, los, n_iter) on its own mesh,
+ * box, mass assignment and smoothing radius; its shifted positions (field
+ * BAOREC_FIELD_*) go to out_x/y/z.  Items sharing (mesh, box_size) share one
+ * context.  baorec_batch_create runs the batch once and captures it as a
+ * graph; baorec_batch_launch replays all of it (asynchronously, on
+ * baorec_batch_stream) and baorec_batch_sync waits and checks for errors.
+ * On failure of create, *out still holds the batch for baorec_batch_last_error
+ * and must be destroyed. */
+typedef struct {
+  float *x, *y, *z;
+  const float* w;
+  int64_t n;
+  int32_t mesh;              /* cubic mesh edge */
+  float box_size;            /* cubic box edge, box_min = 0 */
+  int32_t mas;               /* BAOREC_MAS_CIC | BAOREC_MAS_TSC */
+  float smoothing_radius;
+  int32_t field;             /* BAOREC_FIELD_DISP | _RSD | _SUM */
+  float *out_x, *out_y, *out_z;
+} baorec_batch_item;
+typedef struct baorec_batch baorec_batch;
+
+int baorec_batch_create(const baorec_config* base, const baorec_batch_item* items, int count,
+                        baorec_batch** out);
+int baorec_batch_launch(baorec_batch* b);
+int baorec_batch_sync(baorec_batch* b);
+void* baorec_batch_stream(baorec_batch* b);
+/* Kernels of this library one replay launches (cuFFT's not counted). */
+int64_t baorec_batch_kernel_launches(const baorec_batch* b);
+const char* baorec_batch_last_error(const baorec_batch* b);
+int baorec_batch_destroy(baorec_batch* b);
+
 #ifdef __cplusplus
 }
 #endif
