@@ -114,8 +114,8 @@ _SIGS = {
     "baorec_set_result": (C.c_int, [P, P, U32]),
     "baorec_displacement_meshes": (C.c_int, [P, P, P, P]),
     "baorec_batch_create": (C.c_int, [C.POINTER(Config), C.POINTER(BatchItem), C.c_int, C.POINTER(P)]),
-    "baorec_batch_launch": (C.c_int, [P]),
-    "baorec_batch_sync": (C.c_int, [P]),
+    "baorec_batch_launch": (C.c_int, [P, P]),
+    "baorec_batch_sync": (C.c_int, [P, P]),
     "baorec_batch_stream": (P, [P]),
     "baorec_batch_kernel_launches": (I64, [P]),
     "baorec_batch_last_error": (C.c_char_p, [P]),

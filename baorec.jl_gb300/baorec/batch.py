@@ -55,11 +55,13 @@ class Batch:
         if st != _lib.OK:
             raise _lib.BaorecError(st, self.lib.baorec_batch_last_error(self.h).decode())
 
-    def launch(self):
-        self._check(self.lib.baorec_batch_launch(self.h))
+    def launch(self, stream: int = 0):
+        """Replay the batch on `stream` (a cudaStream_t handle, e.g.
+        torch.cuda.current_stream().cuda_stream; 0 = the batch's own)."""
+        self._check(self.lib.baorec_batch_launch(self.h, stream or None))
 
-    def sync(self):
-        self._check(self.lib.baorec_batch_sync(self.h))
+    def sync(self, stream: int = 0):
+        self._check(self.lib.baorec_batch_sync(self.h, stream or None))
 
     @property
     def stream(self) -> int:

@@ -145,15 +145,15 @@ extern "C" int baorec_batch_create(const baorec_config* base, const baorec_batch
   return BAOREC_OK;
 }
 
-extern "C" int baorec_batch_launch(baorec_batch* b) {
+extern "C" int baorec_batch_launch(baorec_batch* b, void* stream) {
   if (!b || !b->exec) return BAOREC_ERR_ARG;
-  BK(cudaGraphLaunch(b->exec, b->stream));
+  BK(cudaGraphLaunch(b->exec, stream ? (cudaStream_t)stream : b->stream));
   return BAOREC_OK;
 }
 
-extern "C" int baorec_batch_sync(baorec_batch* b) {
+extern "C" int baorec_batch_sync(baorec_batch* b, void* stream) {
   if (!b) return BAOREC_ERR_ARG;
-  BK(cudaStreamSynchronize(b->stream));
+  BK(cudaStreamSynchronize(stream ? (cudaStream_t)stream : b->stream));
   for (auto* ctx : b->groups) {
     int st = baorec::finish(ctx, 0);
     if (st != BAOREC_OK) {

@@ -875,10 +875,14 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else if (which == 1)
       resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, N,
                                                             0.0f, ctx->dred);
+    else if (which == 3 && tile_ok(L.n))
+      launch_resid_diff(ctx->stream, L.v, L.f, t, G, L.r);
+    else if (which == 3)
+      residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, N, L.r);
     else
       jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
   };
-  if (which < 0 || which > 2) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  if (which < 0 || which > 3) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
   launch();   // warm-up
   CK(cudaEventRecord(a, ctx->stream));
   for (int r = 0; r < reps; ++r) launch();
@@ -893,7 +897,8 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   *avg_ms = ms / reps;
   // algorithmic bytes: a full smoothing sweep reads v and f and writes v (12 B/cell;
   // the one-cell kernel does one colour, half of that); the accurate residual
-  // reads hi, lo, e, f and writes hi, lo, r (28 B/cell)
-  *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : which == 1 ? 28.0 * N : 12.0 * N;
+  // reads hi, lo, e, f and writes hi, lo, r (28 B/cell); the FP32 running
+  // residual of the FFT corrections reads d, r, acc and writes r, acc (20 B/cell)
+  *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : which == 1 ? 28.0 * N : which == 3 ? 20.0 * N : 12.0 * N;
   return BAOREC_OK;
 }

@@ -214,9 +214,10 @@ int baorec_mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* ph
 /* Measurement hook (no reference counterpart): launch one finest-level kernel
  * `reps` times on the context's scratch buffers between two CUDA events on
  * the context stream and report the mean duration and the kernel's
- * algorithmic bytes per launch.  which: 0 = red-black half sweep,
+ * algorithmic bytes per launch.  which: 0 = red-black sweep (both colours),
  * 1 = accurate residual with solution update, 2 = damped-Jacobi sweep
- * (reference schedule).  Needs a multigrid context. */
+ * (reference schedule), 3 = FP32 difference-form running residual of the FFT
+ * corrections.  Needs a multigrid context. */
 int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch);
 
 /* Statistics of the context's last residual-driven solve. */
@@ -322,8 +323,9 @@ int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, flo
  * box, mass assignment and smoothing radius; its shifted positions (field
  * BAOREC_FIELD_*) go to out_x/y/z.  Items sharing (mesh, box_size) share one
  * context.  baorec_batch_create runs the batch once and captures it as a
- * graph; baorec_batch_launch replays all of it (asynchronously, on
- * baorec_batch_stream) and baorec_batch_sync waits and checks for errors.
+ * graph; baorec_batch_launch replays all of it asynchronously on `stream`
+ * (cudaStream_t; NULL = the batch's own, baorec_batch_stream) and
+ * baorec_batch_sync waits for that stream and checks for errors.
  * On failure of create, *out still holds the batch for baorec_batch_last_error
  * and must be destroyed. */
 typedef struct {
@@ -341,8 +343,8 @@ typedef struct baorec_batch baorec_batch;
 
 int baorec_batch_create(const baorec_config* base, const baorec_batch_item* items, int count,
                         baorec_batch** out);
-int baorec_batch_launch(baorec_batch* b);
-int baorec_batch_sync(baorec_batch* b);
+int baorec_batch_launch(baorec_batch* b, void* stream);
+int baorec_batch_sync(baorec_batch* b, void* stream);
 void* baorec_batch_stream(baorec_batch* b);
 /* Kernels of this library one replay launches (cuFFT's not counted). */
 int64_t baorec_batch_kernel_launches(const baorec_batch* b);
