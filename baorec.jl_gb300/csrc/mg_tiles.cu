@@ -128,79 +128,6 @@ __device__ __forceinline__ float nbr_diff(const float* __restrict__ s, int q, co
   return o;
 }
 
-// One red-black Gauss-Seidel sweep, both colours in one pass, out of place.
-// Red cells of the tile and of a one-cell ring around it are updated from the
-// old window; then the black cells of the tile from the red-updated window.
-// Window frame: x = x0 - 4 + lx, y = y0 - 2 + ly, z = z0 - 2 + lz; all three
-// origins are even, so window parity is mesh parity.
-template <bool LOCAL, bool CLAMP, int TY, int TZ>
-__global__ void __launch_bounds__(NT, 2) rb_sweep_kernel(const float* __restrict__ vin, float* __restrict__ vout,
-                                                         const float* __restrict__ rhs, LG G, float shift) {
-  constexpr int SY = TY + 4, SZ = TZ + 4, SXY = WX * SY;
-  extern __shared__ __align__(16) float smem[];
-  float* sv = smem;                              // WX*SY*SZ
-  int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);   // SY*SZ
-  float* sp = reinterpret_cast<float*>(ro + SY * SZ);    // 3*WX
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  row_table<2, TY, TZ>(ro, y0, z0, G.n);
-  if (LOCAL) load_ptab<2, TY, TZ>(sp, G, x0, y0, z0);
-  __syncthreads();
-  load_rows<2, TY, TZ>(sv, ro, vin, x0, G.n[0]);
-  Cf cu;
-  if (!LOCAL) cu = coef_fast<false, false>(G.pg[0], G.pg[1], G.pg[2], G);
-  __syncthreads();
-  // red: rows ly, lz in [1, S-1); cells lx in [3, 37) with even lx+ly+lz (17 per row)
-  constexpr int RPR = 17, RROWY = SY - 2, NRED = RPR * RROWY * (SZ - 2), KR = (NRED + NT - 1) / NT;
-  float nv[KR];
-  int qr[KR];
-#pragma unroll
-  for (int k = 0; k < KR; ++k) {
-    const int c = threadIdx.x + k * NT;
-    qr[k] = -1;
-    if (c < NRED) {
-      const int row = c / RPR, t = c - RPR * row;
-      const int ly = 1 + row % RROWY, lz = 1 + row / RROWY;
-      const int lx = 3 + ((ly + lz + 1) & 1) + 2 * t;
-      const int q = lx + WX * ly + SXY * lz;
-      qr[k] = q;
-      const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
-      const float f = __ldg(rhs + ro[ly + SY * lz] + wrapi(x0 - XH + lx, G.n[0])) - shift;
-      nv[k] = __fdividef(f + nbr<LOCAL, SXY>(sv, q, cf), cf.diag);
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < KR; ++k)
-    if (qr[k] >= 0) sv[qr[k]] = nv[k];
-  __syncthreads();
-  // black: tile rows ly, lz in [2, S-2); cells lx in [4, 36) with odd lx+ly+lz (16 per row)
-  constexpr int NBLK = 16 * TY * TZ, KB = NBLK / NT;
-  static_assert(NBLK % NT == 0, "black cells must divide evenly");
-  float nb[KB];
-  int qb[KB];
-#pragma unroll
-  for (int k = 0; k < KB; ++k) {
-    const int c = threadIdx.x + k * NT;
-    const int row = c >> 4, t = c & 15;
-    const int ly = 2 + row % TY, lz = 2 + row / TY;
-    const int lx = 4 + ((ly + lz + 1) & 1) + 2 * t;
-    const int q = lx + WX * ly + SXY * lz;
-    qb[k] = q;
-    const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
-    const float f = __ldg(rhs + ro[ly + SY * lz] + x0 - XH + lx) - shift;
-    nb[k] = __fdividef(f + nbr<LOCAL, SXY>(sv, q, cf), cf.diag);
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < KB; ++k) sv[qb[k]] = nb[k];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int row = warp; row < TY * TZ; row += NWARP) {
-    const int ly = 2 + row % TY, lz = 2 + row / TY;
-    vout[ro[ly + SY * lz] + x0 + lane] = sv[XH + lane + WX * ly + SXY * lz];
-  }
-}
-
 // r = rhs - shift - Ã e (correction equation, clamped operator).
 template <bool LOCAL, bool CLAMP, int TY, int TZ, bool DIFF = false>
 __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
@@ -230,109 +157,6 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
     else
       r[o] = (__ldg(rhs + o) - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
     if (acc) acc[o] += sv[q];   // optional: accumulate the operand into a running sum
-  }
-}
-
-// Accurate residual with solution update: each window chunk of (hi, lo) + e
-// becomes the updated double-float pair as it is loaded; then
-// r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
-// operator, whose coefficients are evaluated with IEEE round-to-nearest
-// operations in the reference's order.  Per-block (Σr, Σr²) to part.
-template <bool LOCAL, int TY, int TZ>
-__global__ void __launch_bounds__(NT) resid_acc_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                       const float* __restrict__ ec, const float* __restrict__ f,
-                                                       float* __restrict__ ohi, float* __restrict__ olo,
-                                                       float* __restrict__ r, LG G, float alpha,
-                                                       double* __restrict__ part) {
-  constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY, SN = WX * SY * SZ;
-  extern __shared__ __align__(16) float smem[];
-  float* sh = smem;
-  float* sl = sh + SN;
-  int* ro = reinterpret_cast<int*>(sl + SN);
-  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  row_table<1, TY, TZ>(ro, y0, z0, G.n);
-  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
-  __syncthreads();
-  {
-    float4* sh4 = reinterpret_cast<float4*>(sh);
-    float4* sl4 = reinterpret_cast<float4*>(sl);
-    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = 4;   // B chunks of each array in flight
-#pragma unroll
-    for (int k0 = 0; k0 < K; k0 += B) {
-      float4 h[B], l[B], e[B];
-#pragma unroll
-      for (int b = 0; b < B; ++b) {
-        const int t = threadIdx.x + (k0 + b) * NT;
-        if (k0 + b < K && t < TOT) {
-          const int row = t / CH, c = t - CH * row;
-          const int o = ro[row] + wrapi(x0 - XH + 4 * c, G.n[0]);
-          h[b] = __ldg(reinterpret_cast<const float4*>(hi + o));
-          l[b] = __ldg(reinterpret_cast<const float4*>(lo + o));
-          if (ec) e[b] = __ldg(reinterpret_cast<const float4*>(ec + o));
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < B; ++b) {
-        const int t = threadIdx.x + (k0 + b) * NT;
-        if (k0 + b < K && t < TOT) {
-          if (ec) {
-            df_add(h[b].x, l[b].x, e[b].x, h[b].x, l[b].x);
-            df_add(h[b].y, l[b].y, e[b].y, h[b].y, l[b].y);
-            df_add(h[b].z, l[b].z, e[b].z, h[b].z, l[b].z);
-            df_add(h[b].w, l[b].w, e[b].w, h[b].w, l[b].w);
-          }
-          sh4[t] = h[b];
-          sl4[t] = l[b];
-        }
-      }
-    }
-  }
-  __syncthreads();
-  float s1 = 0.0f, s2 = 0.0f;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int row = warp; row < TY * TZ; row += NWARP) {
-    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
-    const int q = lx + WX * ly + SXY * lz;
-    const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1], pz = LOCAL ? sp[2 * WX + lz] : G.pg[2];
-    const float px2 = __fmul_rn(px, px), py2 = __fmul_rn(py, py), pz2 = __fmul_rn(pz, pz);
-    const float den = __fadd_rn(__fadd_rn(__fmul_rn(G.cell2[0], px2), __fmul_rn(G.cell2[1], py2)),
-                                __fmul_rn(G.cell2[2], pz2));
-    const float g = __fdiv_rn(G.beta, den);
-    const float gpx = __fadd_rn(G.icell2[0], __fmul_rn(g, px2));
-    const float gpy = __fadd_rn(G.icell2[1], __fmul_rn(g, py2));
-    const float gpz = __fadd_rn(G.icell2[2], __fmul_rn(g, pz2));
-    const float h0 = sh[q], l0 = sl[q];
-    auto D = [&](int u) { return __fadd_rn(__fsub_rn(sh[u], h0), __fsub_rn(sl[u], l0)); };
-    constexpr int SX = WX;
-    const float dxp = D(q + 1), dxm = D(q - 1), dyp = D(q + SX), dym = D(q - SX), dzp = D(q + SXY), dzm = D(q - SXY);
-    float br = gpx * (dxp + dxm) + gpy * (dyp + dym) + gpz * (dzp + dzm) +
-               g / 2.0f *
-                   (__fmul_rn(px, py) * ((D(q + 1 + SX) + D(q - 1 - SX)) - (D(q - 1 + SX) + D(q + 1 - SX))) +
-                    __fmul_rn(px, pz) * ((D(q + 1 + SXY) + D(q - 1 - SXY)) - (D(q - 1 + SXY) + D(q + 1 - SXY))) +
-                    __fmul_rn(py, pz) * ((D(q + SX + SXY) + D(q - SX - SXY)) - (D(q - SX + SXY) + D(q + SX - SXY))));
-    if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
-    const int o = ro[ly + SY * lz] + x0 + lane;
-    const float rv = (__ldg(f + o) - alpha) + br;
-    ohi[o] = h0;
-    olo[o] = l0;
-    r[o] = rv;
-    s1 += rv;          // FP32 over this thread's cells; FP64 across warps and blocks
-    s2 += rv * rv;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-  }
-  __shared__ double red[2][NWARP];
-  if (lane == 0) { red[0][warp] = s1; red[1][warp] = s2; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int k = 0; k < NWARP; ++k) { a += red[0][k]; b += red[1][k]; }
-    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    part[2 * bid] = a;
-    part[2 * bid + 1] = b;
   }
 }
 
@@ -423,8 +247,12 @@ __device__ __forceinline__ f2 gs_two(const float* __restrict__ s, int qa, int qb
   return mul2(add2(fr, o), B2(1.0f / cu.diag));
 }
 
-// The same sweep as rb_sweep_kernel with fixed cell positions per thread and
-// two cells per evaluation.  Red (ring rows ly, lz in [1, S-1), 17 cells per
+// One red-black Gauss-Seidel sweep, both colours in one pass, out of place.
+// Red cells of the tile and of a one-cell ring around it are updated from the
+// old window; then the black cells of the tile from the red-updated window.
+// Window frame: x = x0 - 4 + lx, y = y0 - 2 + ly, z = z0 - 2 + lz; all three
+// origins are even, so window parity is mesh parity.  Cell positions are fixed
+// per thread, two cells per packed evaluation.  Red (ring rows ly, lz in [1, S-1), 17 cells per
 // row): thread -> (row slot, cell t) once; rows of plane lz pair with plane
 // lz + H (H = TZ/2 + 1 is odd, so the pair's parities differ and so do their
 // x positions).  Black (tile rows, 16 cells per row): planes lz and lz + TZ/2
@@ -521,9 +349,13 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
   }
 }
 
-// The accurate residual of resid_acc_kernel with the double-float window held
-// as interleaved (hi, lo) pairs: one 8-byte shared load per neighbour and one
-// packed subtraction give both parts of a difference.
+// Accurate residual with solution update: each window chunk of (hi, lo) + e
+// becomes the updated double-float pair as it is loaded, held as interleaved
+// (hi, lo) pairs (one 8-byte shared load per neighbour and one packed
+// subtraction give both parts of a difference); then
+// r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
+// operator, whose coefficients are evaluated with IEEE round-to-nearest
+// operations in the reference's order.  Per-block (Σr, Σr²) to part.
 template <bool LOCAL, int TY, int TZ>
 __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
                                                         const float* __restrict__ ec, const float* __restrict__ f,
