@@ -12,7 +12,7 @@ from . import _build
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_NOT_CONVERGED, ERR_OOB, ERR_STATE, ERR_NOMEM = 1, 2, 3, 4, 5, 6, 7
 ERR_TOO_LARGE = 8
-HOST, ASYNC, WRITEBACK = 0x1, 0x2, 0x4
+HOST, ASYNC, WRITEBACK, DETERMINISTIC = 0x1, 0x2, 0x4, 0x8
 ITERATIVE, MULTIGRID = 0, 1
 LOS_LOCAL, LOS_GLOBAL = 0, 1
 MAS_CIC, MAS_TSC = 0, 1

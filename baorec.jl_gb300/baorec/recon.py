@@ -56,6 +56,7 @@ class IterativeRecon:
     fft_plan: object = None
     result_cache: object = None
     mas: str = "cic"                     # addition: "cic" | "tsc"
+    deterministic: bool = False          # paint through the tile counting sort (bit-reproducible mesh)
 
     def __post_init__(self):
         if self.beta is None:            # β = typeof(bias)(f / bias)
@@ -82,6 +83,7 @@ class MultigridRecon:
     fft_plan: object = None
     result_cache: object = None
     mas: str = "cic"
+    deterministic: bool = False          # paint through the tile counting sort (bit-reproducible mesh)
     mg_mode: str = "reference"           # "reference" (FMG schedule) | "convergent"
     nu1: int = 2
     nu2: int = 2
@@ -364,10 +366,10 @@ def setup_box(x, y, z, box_pad):
 # mass assignment — src/mas.jl
 # ----------------------------------------------------------------------------
 
-def _paint(name, rho, x, y, z, w, box_size, box_min, wrap):
+def _paint(name, rho, x, y, z, w, box_size, box_min, wrap, deterministic=False):
     ctx = _prim_ctx(rho.shape, box_size, box_min)
     p = _Particles(x, y, z, w)
-    flags = p.flags | (_lib.WRITEBACK if wrap else 0)
+    flags = p.flags | (_lib.WRITEBACK if wrap else 0) | (_lib.DETERMINISTIC if deterministic else 0)
     with _Mesh(rho) as m:
         ctx.call(name, m.ptr, p.ptrs[0], p.ptrs[1], p.ptrs[2], p.ptrs[3], p.n, int(bool(wrap)), flags)
     if wrap:   # the reference writes the wrapped positions back into its inputs
@@ -376,14 +378,14 @@ def _paint(name, rho, x, y, z, w, box_size, box_min, wrap):
     return rho
 
 
-def cic_(rho, x, y, z, w, box_size, box_min, wrap=True):
+def cic_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False):
     """``cic!`` (``src/mas.jl:1-107``): add CIC weights to ``rho``."""
-    return _paint("baorec_cic", rho, x, y, z, w, box_size, box_min, wrap)
+    return _paint("baorec_cic", rho, x, y, z, w, box_size, box_min, wrap, deterministic)
 
 
-def tsc_(rho, x, y, z, w, box_size, box_min, wrap=True):
+def tsc_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False):
     """Triangular-shaped-cloud paint (no reference counterpart)."""
-    return _paint("baorec_tsc", rho, x, y, z, w, box_size, box_min, wrap)
+    return _paint("baorec_tsc", rho, x, y, z, w, box_size, box_min, wrap, deterministic)
 
 
 def cell_bins(x, y, z, box_size, box_min, dims, wrap=True):
@@ -439,7 +441,7 @@ def setup_overdensity_(delta, recon, x, y, z, w, rx=None, ry=None, rz=None, rw=N
     ctx = _ctx(recon, delta.shape, ran_min)
     if rx is None:
         p = _Particles(x, y, z, w)
-        flags = p.flags | (_lib.WRITEBACK if wrap else 0)
+        flags = p.flags | (_lib.WRITEBACK if wrap else 0) | _det(recon)
         with _Mesh(delta) as m:
             ctx.call("baorec_setup_overdensity", m.ptr, *p.ptrs, p.n, int(bool(wrap)), flags)
         if wrap:
@@ -450,7 +452,7 @@ def setup_overdensity_(delta, recon, x, y, z, w, rx=None, ry=None, rz=None, rw=N
         n = _Particles(x).n
         nr = _Particles(rx).n
         with _Mesh(delta) as m:
-            ctx.call("baorec_setup_overdensity_randoms", m.ptr, *p.ptrs[:4], n, *p.ptrs[4:], nr, p.flags)
+            ctx.call("baorec_setup_overdensity_randoms", m.ptr, *p.ptrs[:4], n, *p.ptrs[4:], nr, p.flags | _det(recon))
     return delta
 
 
@@ -460,6 +462,10 @@ def iterate_(delta_r, delta_s, it, recon):
     with _Mesh(delta_r) as a, _Mesh(delta_s, write=False) as b:
         ctx.call("baorec_iterate", a.ptr, b.ptr, int(it))
     return delta_r
+
+
+def _det(recon) -> int:
+    return _lib.DETERMINISTIC if getattr(recon, "deterministic", False) else 0
 
 
 def _catalog_call(name, recon, shape, x, y, z, w, randoms, writeback):
@@ -473,7 +479,7 @@ def _catalog_call(name, recon, shape, x, y, z, w, randoms, writeback):
         n = _Particles(x).n
         nr = _Particles(randoms[0]).n
         rp = p.ptrs[4:]
-    flags = p.flags | (_lib.WRITEBACK if (writeback and randoms is None) else 0)
+    flags = p.flags | (_lib.WRITEBACK if (writeback and randoms is None) else 0) | _det(recon)
     _sync_torch()
     st = ctx.status(name, *p.ptrs[:4], n, *rp, nr, flags)
     if st not in (_lib.OK, _lib.ERR_NOT_CONVERGED):

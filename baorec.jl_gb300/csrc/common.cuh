@@ -71,6 +71,13 @@ struct baorec_ctx {
   int dense_level = -1;                // first level with at most 512 cells
   bool coarse_dirty = true;            // coarse_M / dense_level need rebuilding
   baorec::GuessNet* net = nullptr;     // learned initial guess (weights, workspace)
+  // deterministic paint scratch: tile keys, permutation, tile counts/offsets, fixed-point mesh
+  baorec::DevBuf sort_keys, sort_perm, sort_tiles, fix_mesh;
+  struct Tune {                        // launch shapes (defaults, or chosen by baorec_autotune)
+    int paint_tile = 8;                // tile edge of the deterministic paint
+    int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1
+    bool tuned = false;
+  } tune;
   // reductions
   double* dred = nullptr;              // device FP64 partial sums
   double* hred = nullptr;              // pinned host mirror
@@ -149,6 +156,8 @@ inline Geom geom_of(const baorec_ctx* c) {
 
 // ---- entry points implemented per translation unit ------------------------
 // paint.cu
+int paint_sorted(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w, int64_t n, int wrap,
+                 int mas, uint32_t flags);
 int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w,
           int64_t n, int wrap, int mas, uint32_t flags);
 int minmax3(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,

@@ -458,16 +458,17 @@ __global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, SGeom g, c
   const float* sy = hy2 + g.n2;
   const float* hz2 = sy + g.n2;
   const float* sz = hz2 + g.n3;
-  const size_t rows = (size_t)g.n2 * g.n3;
-  for (size_t row = 2 * (size_t)blockIdx.x + (threadIdx.x >> 7); row < rows; row += 2 * (size_t)gridDim.x) {
-    const int j = (int)(row % g.n2), k = (int)(row / g.n2);
+  // 32-bit row arithmetic (n2 n3 < 2^31); one reciprocal per mode (a preconditioner)
+  const int rows = g.n2 * g.n3;
+  for (int row = 2 * (int)blockIdx.x + (int)(threadIdx.x >> 7); row < rows; row += 2 * (int)gridDim.x) {
+    const int k = row / g.n2, j = row - k * g.n2;
     const float syj = __ldg(sy + j), szk = __ldg(sz + k);
     const float ryz = g.diag[1] * __ldg(hy2 + j) + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk;
     const float cx = g.cross[0] * syj + g.cross[1] * szk;
-    cufftComplex* ar = a + row * g.n1h;
+    cufftComplex* ar = a + (size_t)row * g.n1h;
     for (int i = threadIdx.x & 127; i < g.n1h; i += 128) {
       const float A = ryz + g.diag[0] * __ldg(hx2 + i) + cx * __ldg(sx + i);
-      const float s = (row == 0 && i == 0) ? 0.0f : g.invN / A;
+      const float s = (row == 0 && i == 0) ? 0.0f : g.invN * __frcp_rn(A);
       cufftComplex v = ar[i];
       v.x *= s; v.y *= s;
       ar[i] = v;

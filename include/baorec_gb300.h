@@ -47,6 +47,8 @@ typedef enum {
 #define BAOREC_HOST       0x1u  /* particle pointers are host memory */
 #define BAOREC_ASYNC      0x2u  /* do not wait for the GPU before returning */
 #define BAOREC_WRITEBACK  0x4u  /* paint with wrap writes wrapped positions back (reference mutates its inputs) */
+#define BAOREC_DETERMINISTIC 0x8u /* paint through the tile counting sort with fixed-point sums: the same mesh
+                                     bits on every run (no reference counterpart) */
 
 /* method / option enums */
 #define BAOREC_ITERATIVE  0

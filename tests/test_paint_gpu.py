@@ -120,3 +120,50 @@ def test_tsc_matches_oracle(wrap):
     orho, _ = O.tsc(np.zeros((n, n, n), F32), x, y, z, w, [L] * 3, [0.0] * 3, wrap=wrap)
     np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
     assert abs(float(rho.sum(dtype=np.float64)) - float(w.sum(dtype=np.float64))) < 1e-4 * float(w.sum())
+
+
+@pytest.mark.parametrize("mas,wrap", [("cic", True), ("cic", False), ("tsc", True), ("tsc", False)])
+def test_deterministic_paint_matches_oracle_and_repeats_bit_for_bit(mas, wrap):
+    """The tile counting sort + fixed-point paint: the oracle's mesh within the
+    paint tolerance, the atomic paint's within FP32 rounding, and the same
+    bits on a second run (the atomic paint's sums depend on thread order)."""
+    import baorec
+    n, npart = 32, 60000
+    L = F32(600.0)
+    x, y, z, w = uniform_box(npart, L * F32(0.8), seed=11)
+    x, y, z = [(a + F32(40)).astype(F32) for a in (x, y, z)]
+    w = (w * F32(0.5) + F32(0.75)).astype(F32)
+    bs, bm = [L] * 3, [0.0] * 3
+    paint = baorec.cic_ if mas == "cic" else baorec.tsc_
+    runs = []
+    for _ in range(2):
+        rho = baorec.zeros_mesh((n, n, n), device=False)
+        paint(rho, x.copy(), y.copy(), z.copy(), w, bs, bm, wrap=wrap, deterministic=True)
+        runs.append(np.array(rho))
+    np.testing.assert_array_equal(runs[0].view(np.uint32), runs[1].view(np.uint32))
+    fast = baorec.zeros_mesh((n, n, n), device=False)
+    paint(fast, x.copy(), y.copy(), z.copy(), w, bs, bm, wrap=wrap)
+    np.testing.assert_allclose(runs[0], fast, rtol=1e-5, atol=1e-6 * float(np.abs(fast).max()))
+    ofn = O.cic if mas == "cic" else O.tsc
+    orho, _ = ofn(np.zeros((n, n, n), F32), x.copy(), y.copy(), z.copy(), w, bs, bm, wrap=wrap)
+    np.testing.assert_allclose(runs[0], orho, rtol=MESH_RTOL, atol=1e-5 * float(np.abs(orho).max()))
+
+
+def test_deterministic_paint_wraps_across_the_periodic_edge():
+    """Particles in the last cell of every axis (their upper CIC neighbour and
+    TSC node wrap to cell 0) land where the atomic paint puts them."""
+    import baorec
+    n = 16
+    L = F32(160.0)
+    rng = np.random.default_rng(4)
+    x = (L - rng.random(3000, dtype=np.float32) * F32(10)).astype(F32)
+    y = (L - rng.random(3000, dtype=np.float32) * F32(10)).astype(F32)
+    z = (rng.random(3000, dtype=np.float32) * L).astype(F32)
+    w = np.ones(3000, F32)
+    for paint in (baorec.cic_, baorec.tsc_):
+        a = baorec.zeros_mesh((n, n, n), device=False)
+        b = baorec.zeros_mesh((n, n, n), device=False)
+        paint(a, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=True, deterministic=True)
+        paint(b, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=True)
+        np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-5)
+        assert abs(float(np.sum(a, dtype=np.float64)) - 3000.0) < 1e-2
