@@ -120,6 +120,8 @@ _SIGS = {
     "baorec_batch_kernel_launches": (I64, [P]),
     "baorec_batch_last_error": (C.c_char_p, [P]),
     "baorec_batch_destroy": (C.c_int, [P]),
+    "baorec_autotune": (C.c_int, [P, U32, I32P, I32P]),
+    "baorec_set_tune": (C.c_int, [P, C.c_int32, I32P]),
     "baorec_guess_num_params": (I64, []),
     "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
     "baorec_guess_set_params": (C.c_int, [P, P, I64]),
@@ -228,6 +230,13 @@ class Context:
         st = SolveStats()
         self.call("baorec_last_solve_stats", C.byref(st))
         return st.as_dict()
+
+    def autotune(self, stencil: bool = True, paint: bool = True) -> dict:
+        """Pick launch shapes by timing (baorec_autotune); returns the choices."""
+        pt = C.c_int32()
+        bt = (C.c_int32 * 16)()
+        self.call("baorec_autotune", (1 if stencil else 0) | (2 if paint else 0), C.byref(pt), bt)
+        return {"paint_tile": pt.value, "tile16_per_level": list(bt)}
 
     def solve_history(self) -> list:
         """[(relative residual, correction that followed)] of the last solve:

@@ -297,6 +297,7 @@ LG level_geom(const baorec_ctx* ctx, int l, float clamp) {
   G.beta = ctx->cfg.beta;
   G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
   G.clamp = clamp;
+  G.tile16 = l < 16 ? ctx->tune.big_tiles[l] : -1;
   return G;
 }
 
@@ -684,6 +685,10 @@ static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
   return smooth_rb(ctx, lvl, G, shift, ctx->cfg.nu2);
 }
 
+int level_count(const baorec_ctx* ctx) { return ctx->nlev; }
+
+LG level_geom_public(const baorec_ctx* ctx, int l, float clamp) { return level_geom(ctx, l, clamp); }
+
 int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r) {
   CKS(mg_setup(ctx));
   const baorec::Level& L0 = ctx->lev[0];
@@ -746,7 +751,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   // the tile kernel reads the solution pair in 16-byte chunks
   const bool aligned = (uintptr_t)phi % 16 == 0 && (uintptr_t)ctx->phi_lo % 16 == 0 && (uintptr_t)ctx->phi_hi2 % 16 == 0 &&
                        (uintptr_t)ctx->phi_lo2 % 16 == 0;
-  const bool tile0 = aligned && tile_ok(L0.n) && (size_t)tile_blocks(L0.n) <= kMaxPartials;
+  const bool tile0 = aligned && tile_ok(L0.n) && (size_t)tile_blocks(G) <= kMaxPartials;
   int nparts = kResBlocks;
   // spectral corrections (FFT inverse of the operator with the box's mean line
   // of sight) run first, for as long as each one shrinks the residual by at

@@ -15,6 +15,7 @@ struct LG {                           // level geometry passed to kernels
   float beta;
   int local;
   float clamp;                        // > 0: clamp derivative coefficients
+  int tile16;                         // tile kernels: -1 heuristic, 0 = 32x8x8, 1 = 32x16x16 tiles
 };
 
 struct Coef {
@@ -122,7 +123,7 @@ cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float
 // Accurate residual with solution update; writes (Σr, Σr²) per block to part, returns the block count.
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* e, const float* f,
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts);
-int tile_blocks(const int n[3]);
+int tile_blocks(const LG& G);
 
 // ---- cooperative coarse tail (mg_tail.cu) -----------------------------------
 constexpr int kTailMaxCells = 64 * 64 * 64;   // levels at most this big run in the tail kernel

@@ -464,9 +464,13 @@ constexpr size_t win_bytes(int arrays) {
          sizeof(int) * (TY + 2 * HY) * (TZ + 2 * HY) + sizeof(float) * 3 * WX;
 }
 
-// Tile height/depth for a level: 16 x 16 when that still gives every SM a block, else 8 x 8.
-bool big_tiles(const int n[3]) {
-  return n[1] % 16 == 0 && n[2] % 16 == 0 && (n[0] / TX) * (n[1] / 16) * (n[2] / 16) >= kNumSMs;
+// Tile height/depth for a level: the autotuner's choice when it made one, else
+// 16 x 16 when that still gives every SM a block, else 8 x 8.
+bool big_tiles(const LG& G) {
+  const int* n = G.n;
+  if (n[1] % 16 || n[2] % 16) return false;
+  if (G.tile16 >= 0) return G.tile16 == 1;
+  return (n[0] / TX) * (n[1] / 16) * (n[2] / 16) >= kNumSMs;
 }
 
 template <int TY, int TZ>
@@ -526,13 +530,14 @@ cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float*
 
 bool tile_ok(const int n[3]) { return n[0] % TX == 0 && n[1] % 8 == 0 && n[2] % 8 == 0; }
 
-int tile_blocks(const int n[3]) {
-  return big_tiles(n) ? (n[0] / TX) * (n[1] / 16) * (n[2] / 16) : (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
+int tile_blocks(const LG& G) {
+  const int* n = G.n;
+  return big_tiles(G) ? (n[0] / TX) * (n[1] / 16) * (n[2] / 16) : (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
 }
 
 cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const float* rhs, const LG& G, float shift,
                             bool clamp) {
-  const bool big = big_tiles(G.n);
+  const bool big = big_tiles(G);
   if (!G.local)
     return big ? sweep_t<false, false, 16, 16>(s, vin, vout, rhs, G, shift) : sweep_t<false, false, 8, 8>(s, vin, vout, rhs, G, shift);
   if (clamp)
@@ -542,7 +547,7 @@ cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const
 
 cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float shift,
                          bool clamp, float* acc) {
-  const bool big = big_tiles(G.n);
+  const bool big = big_tiles(G);
   if (!G.local)
     return big ? resid_t<false, false, 16, 16>(s, ec, rhs, r, G, shift, acc)
                : resid_t<false, false, 8, 8>(s, ec, rhs, r, G, shift, acc);
@@ -554,7 +559,7 @@ cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, floa
 }
 
 cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
-  const bool big = big_tiles(G.n);
+  const bool big = big_tiles(G);
   if (!G.local)
     return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
                : resid_t<false, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);
@@ -564,8 +569,8 @@ cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs,
 
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f,
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts) {
-  *nparts = tile_blocks(G.n);
-  const bool big = big_tiles(G.n);
+  *nparts = tile_blocks(G);
+  const bool big = big_tiles(G);
   if (G.local)
     return big ? acc_t<true, 16, 16>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part)
                : acc_t<true, 8, 8>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part);

@@ -1,0 +1,146 @@
+// Autotuner (no reference counterpart): picks launch shapes by timing the
+// candidates on the context's own meshes with CUDA events.
+//   stencil: per multigrid level, 32x8x8 or 32x16x16 tiles for the tile
+//            kernels (sweep; at the finest level also the accurate and the
+//            running residual), where both are valid;
+//   paint:   the tile edge (4, 8 or 16 cells) of the deterministic paint,
+//            on 2^21 uniform particles in the box.
+// Choices live in ctx->tune and apply to every later launch of the context.
+#include <vector>
+
+#include "common.cuh"
+#include "mg_common.cuh"
+
+namespace baorec {
+
+int level_count(const baorec_ctx* ctx);
+LG level_geom_public(const baorec_ctx* ctx, int l, float clamp);
+
+namespace {
+
+__global__ void uniform_particles_kernel(float* __restrict__ p, int64_t n, float3 lo, float3 span, uint32_t seed) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    // 32-bit integer hash per (particle, axis), kept below the box's upper edge
+    float u[3];
+    for (int a = 0; a < 3; ++a) {
+      uint32_t h = (uint32_t)i * 2654435761u ^ (seed + 0x9E3779B9u * (uint32_t)(a + 1));
+      h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
+      u[a] = (float)(h >> 8) * (1.0f / 16777216.0f) * 0.999f;
+    }
+    p[i] = lo.x + span.x * u[0];
+    p[n + i] = lo.y + span.y * u[1];
+    p[2 * n + i] = lo.z + span.z * u[2];
+    p[3 * n + i] = 1.0f;
+  }
+}
+
+template <typename F>
+int time_ms(baorec_ctx* ctx, F launch, int reps, float* ms) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  int st = launch();   // warm-up
+  if (st == BAOREC_OK) {
+    CK(cudaEventRecord(a, ctx->stream));
+    for (int r = 0; r < reps && st == BAOREC_OK; ++r) st = launch();
+    CK(cudaEventRecord(b, ctx->stream));
+    CK(cudaEventSynchronize(b));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, a, b));
+    *ms = t / reps;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return st;
+}
+
+int tune_stencils(baorec_ctx* ctx) {
+  CKS(mg_setup(ctx));
+  const int nl = level_count(ctx);
+  for (int l = 0; l < nl && l < 16; ++l) {
+    Level& L = ctx->lev[l];
+    if (!tile_ok(L.n) || L.n[1] % 16 || L.n[2] % 16) continue;
+    CK(cudaMemsetAsync(L.f, 0, L.N * 4 * 4, ctx->stream));   // f, v, r, t
+    float best = 1e30f;
+    int pick = -1;
+    for (int choice = 0; choice < 2; ++choice) {
+      ctx->tune.big_tiles[l] = choice;
+      const LG Gc = level_geom_public(ctx, l, kClamp);
+      const LG G0 = level_geom_public(ctx, l, 0.0f);
+      float* t = L.r + L.N;
+      auto launch = [&]() -> int {
+        CK(launch_rb_sweep(ctx->stream, L.v, t, L.f, Gc, 0.0f, L.needs_clamp));
+        if (l == 0) {
+          int np = 0;
+          CK(launch_resid_acc(ctx->stream, L.v, ctx->phi_lo, nullptr, L.f, ctx->phi_hi2, ctx->phi_lo2, L.r, G0, 0.0f,
+                              ctx->dred, &np));
+          CK(launch_resid_diff(ctx->stream, L.v, L.f, t, G0, L.r));
+        }
+        return BAOREC_OK;
+      };
+      CK(cudaMemsetAsync(ctx->phi_lo, 0, L.N * 4 * 3, ctx->stream));
+      float ms = 0.0f;
+      CKS(time_ms(ctx, launch, 5, &ms));
+      ctx->launches += 6 * (l == 0 ? 3 : 1);
+      if (ms < best) { best = ms; pick = choice; }
+    }
+    ctx->tune.big_tiles[l] = pick;
+  }
+  return BAOREC_OK;
+}
+
+int tune_paint(baorec_ctx* ctx) {
+  const int64_t n = 1 << 21;
+  float* p = nullptr;
+  CK(cudaMalloc(&p, (size_t)n * 4 * sizeof(float)));
+  float3 lo = make_float3(ctx->cfg.box_min[0], ctx->cfg.box_min[1], ctx->cfg.box_min[2]);
+  float3 span = make_float3(ctx->cfg.box_size[0], ctx->cfg.box_size[1], ctx->cfg.box_size[2]);
+  uniform_particles_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(p, n, lo, span, 12345u);
+  int st = cudaGetLastError() == cudaSuccess ? BAOREC_OK : set_error(ctx, BAOREC_ERR_CUDA, "autotune: particle kernel");
+  float* mesh = ctx->psi;   // scratch
+  ctx->psi_valid = false;
+  const int cand[3] = {4, 8, 16};
+  float best = 1e30f;
+  int pick = ctx->tune.paint_tile;
+  for (int c = 0; c < 3 && st == BAOREC_OK; ++c) {
+    ctx->tune.paint_tile = cand[c];
+    auto launch = [&]() -> int {
+      return paint_sorted(ctx, mesh, p, p + n, p + 2 * n, p + 3 * n, n, 1, ctx->cfg.mas, BAOREC_ASYNC);
+    };
+    float ms = 0.0f;
+    st = time_ms(ctx, launch, 3, &ms);
+    if (st == BAOREC_OK && ms < best) { best = ms; pick = cand[c]; }
+  }
+  ctx->tune.paint_tile = pick;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(p);
+  return st;
+}
+
+}  // namespace
+}  // namespace baorec
+
+using namespace baorec;
+
+extern "C" int baorec_autotune(baorec_ctx* ctx, uint32_t what, int32_t* paint_tile, int32_t* big_tiles) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if ((what & BAOREC_TUNE_STENCIL) && ctx->cfg.method == BAOREC_MULTIGRID) CKS(tune_stencils(ctx));
+  if (what & BAOREC_TUNE_PAINT) CKS(tune_paint(ctx));
+  ctx->tune.tuned = true;
+  if (paint_tile) *paint_tile = ctx->tune.paint_tile;
+  if (big_tiles)
+    for (int l = 0; l < 16; ++l) big_tiles[l] = ctx->tune.big_tiles[l];
+  return finish(ctx, 0);
+}
+
+extern "C" int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tiles) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (paint_tile < 1 || paint_tile > 16) return set_error(ctx, BAOREC_ERR_ARG, "paint tile %d outside [1, 16]", paint_tile);
+  if (big_tiles)
+    for (int l = 0; l < 16; ++l)
+      if (big_tiles[l] < -1 || big_tiles[l] > 1) return set_error(ctx, BAOREC_ERR_ARG, "tile choice %d", big_tiles[l]);
+  ctx->tune.paint_tile = paint_tile;
+  if (big_tiles)
+    for (int l = 0; l < 16; ++l) ctx->tune.big_tiles[l] = big_tiles[l];
+  return BAOREC_OK;
+}

@@ -306,6 +306,10 @@ def run_gb300(args):
     ctx = make(args.start)
     # the other starts are timed the same way and reported beside the headline
     others = {} if args.only_start else {s: make(s) for s in ("zero", "spectral", "learned") if s != args.start}
+    # launch shapes chosen by the autotuner (per-level stencil tiles, deterministic-paint tile)
+    tune = ctx.autotune()
+    for c_ in others.values():
+        c_.autotune(paint=False)
     nd, nr = len(m.x), len(m.rx)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
@@ -428,7 +432,7 @@ def run_gb300(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"lightcone MG reconstruction {args.mesh}^3 to 1e-6 relative residual, "
                                    f"{nd} data + {nr} randoms, CIC, R=15, b=2, f=0.8, local LOS, 2+2 RB sweeps",
-                       "mesh": args.mesh, "start": args.start,
+                       "mesh": args.mesh, "start": args.start, "autotune": tune,
                        "l2": "working set per step > 1 GB >> 126 MB L2 (inputs larger than L2)",
                        "parallelism": f"replicas x{ws}"},
             "solver": {"start": args.start, "cycles": stats["cycles"], "spectral_steps": stats["spectral_steps"],

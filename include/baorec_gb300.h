@@ -353,6 +353,18 @@ int64_t baorec_batch_kernel_launches(const baorec_batch* b);
 const char* baorec_batch_last_error(const baorec_batch* b);
 int baorec_batch_destroy(baorec_batch* b);
 
+/* ---- Autotuner (no reference counterpart) ---------------------------------
+ * Times candidate launch shapes on this context's meshes and keeps the
+ * fastest for every later call: BAOREC_TUNE_STENCIL picks 32x8x8 or 32x16x16
+ * tiles per multigrid level (multigrid contexts); BAOREC_TUNE_PAINT picks the
+ * deterministic paint's tile edge (4, 8 or 16).  Outputs (may be NULL): the
+ * paint tile and 16 per-level tile choices (-1 = not tuned, 0 = 8x8, 1 = 16x16). */
+#define BAOREC_TUNE_STENCIL 0x1u
+#define BAOREC_TUNE_PAINT   0x2u
+int baorec_autotune(baorec_ctx* ctx, uint32_t what, int32_t* paint_tile, int32_t* big_tiles);
+/* Set the shapes explicitly (paint tile edge 1..16; per-level choices as above, NULL keeps them). */
+int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tiles);
+
 #ifdef __cplusplus
 }
 #endif
