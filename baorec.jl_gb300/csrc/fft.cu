@@ -449,30 +449,31 @@ SGeom sgeom_of(const baorec_ctx* c) {
 }
 
 // Per-axis tables sin²(π m/n) and sin(2π m/n) (m the signed frequency):
-// tab = hx2[n1h] | sx[n1h] | hy2[n2] | sy[n2] | hz2[n3] | sz[n3].  Two k-space
-// rows (fixed j, k) per 256-thread block, x along the threads.
-__global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, SGeom g, const float* __restrict__ tab) {
+// tab = hx2[n1h] | sx[n1h] | hy2[n2] | sy[n2] | hz2[n3] | sz[n3].  Each block
+// holds `rpb` k-space rows (fixed j, k) of n1h threads each, x along the threads.
+__global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, SGeom g, const float* __restrict__ tab,
+                                        int rpb) {
   const float* hx2 = tab;
   const float* sx = hx2 + g.n1h;
   const float* hy2 = sx + g.n1h;
   const float* sy = hy2 + g.n2;
   const float* hz2 = sy + g.n2;
   const float* sz = hz2 + g.n3;
-  // 32-bit row arithmetic (n2 n3 < 2^31); one reciprocal per mode (a preconditioner)
-  const int rows = g.n2 * g.n3;
-  for (int row = 2 * (int)blockIdx.x + (int)(threadIdx.x >> 7); row < rows; row += 2 * (int)gridDim.x) {
+  const int rows = g.n2 * g.n3;   // 32-bit row arithmetic (n2 n3 < 2^31)
+  const int slot = (int)threadIdx.x / g.n1h, i = (int)threadIdx.x - slot * g.n1h;
+  if (slot >= rpb) return;
+  const float hxi = __ldg(hx2 + i), sxi = __ldg(sx + i);
+  for (int row = (int)blockIdx.x * rpb + slot; row < rows; row += (int)gridDim.x * rpb) {
     const int k = row / g.n2, j = row - k * g.n2;
     const float syj = __ldg(sy + j), szk = __ldg(sz + k);
-    const float ryz = g.diag[1] * __ldg(hy2 + j) + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk;
-    const float cx = g.cross[0] * syj + g.cross[1] * szk;
-    cufftComplex* ar = a + (size_t)row * g.n1h;
-    for (int i = threadIdx.x & 127; i < g.n1h; i += 128) {
-      const float A = ryz + g.diag[0] * __ldg(hx2 + i) + cx * __ldg(sx + i);
-      const float s = (row == 0 && i == 0) ? 0.0f : g.invN * __frcp_rn(A);
-      cufftComplex v = ar[i];
-      v.x *= s; v.y *= s;
-      ar[i] = v;
-    }
+    const float A = g.diag[1] * __ldg(hy2 + j) + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk +
+                    g.diag[0] * hxi + (g.cross[0] * syj + g.cross[1] * szk) * sxi;
+    // one reciprocal per mode (a preconditioner); the k = 0 mode is dropped
+    const float s = (row == 0 && i == 0) ? 0.0f : g.invN * __frcp_rn(A);
+    cufftComplex* e = a + (size_t)row * g.n1h + i;
+    cufftComplex v = *e;
+    v.x *= s; v.y *= s;
+    *e = v;
   }
 }
 
@@ -506,9 +507,12 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   SGeom g = sgeom_of(ctx);
   CKS(spectral_tables(ctx));
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));
+  // rows of n1h threads per block (n1h <= 1024, as the mesh-size limit guarantees up to n1 = 2046)
+  if (ctx->n1h > 1024) return set_error(ctx, BAOREC_ERR_ARG, "FFT start: n1 above 2046");
+  const int rpb = std::max(1, 1024 / ctx->n1h);
   const size_t rows = (size_t)ctx->n2 * ctx->n3;
-  const unsigned blocks = (unsigned)std::min<size_t>((rows + 1) / 2, 16 * kNumSMs);
-  spectral_inverse_kernel<<<blocks, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab);
+  const unsigned blocks = (unsigned)std::min<size_t>((rows + rpb - 1) / rpb, 16 * kNumSMs);
+  spectral_inverse_kernel<<<blocks, rpb * ctx->n1h, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, rpb);
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, e));
   return BAOREC_OK;

@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched box-mock measurement")
     ap.add_argument("--only-start", action="store_true", help="time only the --start solve (no other starts)")
+    ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel roofline and paint timings")
     ap.add_argument("--batch-mocks", type=int, default=64)
     ap.add_argument("--start", default="spectral", choices=["zero", "spectral", "learned"],
                     help="start of the headline solve: zero (plain multigrid), spectral (FFT-preconditioned "
@@ -380,7 +381,7 @@ def run_gb300(args):
     N = int(np.prod(n))
     names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: "resid_kernel (difference form)"}
     meas = {}
-    for which in (0, 1, 3):
+    for which in (() if args.no_kernels else (0, 1, 3)):
         avg, nbytes = C.c_float(), C.c_double()
         ctx.call("baorec_profile_kernel", which, 30, C.byref(avg), C.byref(nbytes))
         ach = nbytes.value / (avg.value * 1e-3) / 1e9
@@ -389,9 +390,11 @@ def run_gb300(args):
                        "traffic": traffic_per_launch(names[which].split()[0], N),
                        "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
     head = 0 if args.start == "zero" else 1
-    roofline = dict(meas[head])
-    roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
-    aux = {names[w]: meas[w] for w in meas if w != head}
+    roofline, aux = None, {}
+    if meas:
+        roofline = dict(meas[head])
+        roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
+        aux = {names[w]: meas[w] for w in meas if w != head}
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -415,6 +418,26 @@ def run_gb300(args):
                # potential: x,y,z,w of both catalogs; each read-out stages x,y,z again
                "h2d_bytes_per_step": 16 * (nd + nr) + 12 * nd + 24 * nr,
                "d2h_bytes_per_step": 12 * nd + 24 * nr, "ms_per_step": te * 1e3}
+
+    # particles painted/s: the 5e6 randoms into a 256^3 mesh, float-atomic and deterministic paints
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    scratch = torch.zeros(N, device="cuda")
+    for label, fl in (() if args.no_kernels else
+                      (("cic_paint (atomic)", 0), ("cic_paint (deterministic, tile sort)", _lib.DETERMINISTIC))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 10
+        ctx.call("baorec_cic", scratch.data_ptr(), *ptr(R), nr, 0, fl)
+        e0.record(stream)
+        for _ in range(reps):
+            ctx.call("baorec_cic", scratch.data_ptr(), *ptr(R), nr, 0, fl | _lib.ASYNC)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1) / reps
+        pbytes = 16.0 * nr + 4.0 * N
+        aux[label] = {"particles_per_s": nr * 1e3 / pms, "avg_launch_ms": pms, "algorithmic_bytes": pbytes,
+                      "achieved": pbytes / (pms * 1e-3) / 1e9, "unit": "GB/s", "peak": peak,
+                      "frac": pbytes / (pms * 1e-3) / 1e9 / peak}
+    del scratch
 
     batch = None if args.no_batch else run_batch(args, torch, np)
 
