@@ -31,6 +31,11 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+def lto_sources():
+    d = os.path.join(CSRC, "lto")
+    return sorted(os.path.join(d, f) for f in os.listdir(d) if f.endswith(".cu")) if os.path.isdir(d) else []
+
+
 def _stale(obj, deps):
     if not os.path.exists(obj):
         return True
@@ -62,9 +67,31 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(r.stdout, r.stderr, flush=True)
         return r
 
+    # cuFFT callbacks: LTO IR fatbins embedded as byte arrays (linked by cuFFT at plan creation)
+    # (two IR targets: the arch-specific sm_103a and the portable sm_103; the
+    # library tries them in that order)
+    for src in lto_sources():
+        base = os.path.basename(src)[:-3]
+        blob = os.path.join(BUILD_DIR, base + "_blob.cpp")
+        obj = os.path.join(BUILD_DIR, base + "_blob.o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            with open(blob, "w") as fh:
+                fh.write("#include <stddef.h>\n")
+                for tag, arch in (("a", "arch=compute_103a,code=lto_103a"), ("p", "arch=compute_103,code=lto_103")):
+                    fat = os.path.join(BUILD_DIR, f"{base}_{tag}.fatbin")
+                    run([nvcc(), "-gencode", arch, "-O3", "-std=c++17", "-dc", "-fatbin", src, "-o", fat])
+                    data = open(fat, "rb").read()
+                    sym = f"baorec_lto_{base}_{tag}"
+                    fh.write(f'extern "C" const unsigned char {sym}[] = {{')
+                    fh.write(",".join(str(b) for b in data))
+                    fh.write("};\n")
+                    fh.write(f'extern "C" const size_t {sym}_size = {len(data)};\n')
+            jobs.append([nvcc(), *ARCH, "-O2", "-Xcompiler", "-fPIC", "-c", blob, "-o", obj])
+
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
     if jobs or force or _stale(LIB_PATH, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcufft", "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcufft", "-lnvJitLink", "-lcudart"]
         run(cmd)
     return LIB_PATH

@@ -106,6 +106,8 @@ _SIGS = {
     "baorec_last_solve_stats": (C.c_int, [P, C.POINTER(SolveStats)]),
     "baorec_solve_history": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int]),
     "baorec_start_residual": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_double)]),
+    "baorec_fft_callbacks": (C.c_int, [P, C.POINTER(C.c_char_p)]),
+    "baorec_set_fft_callbacks": (C.c_int, [P, C.c_int]),
     "baorec_profile_kernel": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_reconstructed_overdensity": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
     "baorec_reconstructed_potential": (C.c_int, [P, P, P, P, P, I64, P, P, P, P, I64, U32]),
@@ -237,6 +239,12 @@ class Context:
         bt = (C.c_int32 * 16)()
         self.call("baorec_autotune", (1 if stencil else 0) | (2 if paint else 0), C.byref(pt), bt)
         return {"paint_tile": pt.value, "tile16_per_level": list(bt)}
+
+    def fft_callbacks(self) -> dict:
+        """State of the FFT start's cuFFT load callback (baorec_fft_callbacks)."""
+        note = C.c_char_p()
+        st = self.lib.baorec_fft_callbacks(self.h, C.byref(note))
+        return {"state": int(st), "note": (note.value or b"").decode()}
 
     def solve_history(self) -> list:
         """[(relative residual, correction that followed)] of the last solve:

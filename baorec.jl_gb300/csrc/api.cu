@@ -205,6 +205,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
       (st = make_plan(ctx, &ctx->plan_c2r6, CUFFT_C2R, 6, &maxw)))
     return fail(st);
   CKC(cudaMalloc(&ctx->fft_work, maxw > 0 ? maxw : 256));
+  ctx->fft_work_bytes = maxw > 0 ? maxw : 256;
   cufftHandle plans[6] = {ctx->plan_r2c, ctx->plan_r2c2, ctx->plan_c2r, ctx->plan_c2r2, ctx->plan_c2r3, ctx->plan_c2r6};
   for (cufftHandle p : plans)
     if (cufftSetWorkArea(p, ctx->fft_work) != CUFFT_SUCCESS) return fail(set_error(ctx, BAOREC_ERR_CUFFT, "cufftSetWorkArea"));
@@ -221,6 +222,9 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   cufftHandle plans[6] = {ctx->plan_r2c, ctx->plan_r2c2, ctx->plan_c2r, ctx->plan_c2r2, ctx->plan_c2r3, ctx->plan_c2r6};
   for (cufftHandle p : plans)
     if (p) cufftDestroy(p);
+  if (ctx->plan_c2r_spec) cufftDestroy(ctx->plan_c2r_spec);
+  cudaFree(ctx->spec_work);
+  cudaFree(ctx->spec_cb);
   cudaFree(ctx->fft_work);
   cudaFree(ctx->mesh3);
   cudaFree(ctx->psi);

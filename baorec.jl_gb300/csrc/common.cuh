@@ -52,6 +52,15 @@ struct baorec_ctx {
   cudaStream_t stream;
   cufftHandle plan_r2c = 0, plan_c2r = 0, plan_r2c2 = 0, plan_c2r2 = 0, plan_c2r3 = 0, plan_c2r6 = 0;
   void* fft_work = nullptr;            // one work area shared by all plans
+  size_t fft_work_bytes = 0;
+  // FFT preconditioner: inverse transform with the k-space multiply as a cuFFT
+  // load callback (LTO, linked at plan creation); state 0 untried, 1 in use,
+  // -1 unavailable or not requested (the separate multiply kernel runs instead)
+  cufftHandle plan_c2r_spec = 0;
+  int spec_cb_state = -1;
+  void* spec_cb = nullptr;             // device copy of the callback's parameters
+  void* spec_work = nullptr;           // its own work area when the shared one is too small
+  char spec_cb_note[256] = "not requested (baorec_set_fft_callbacks)";
   // persistent meshes: mesh3 = three adjacent meshes A | B | C
   float* mesh3 = nullptr;
   float* result = nullptr;             // recon.result_cache (= A)

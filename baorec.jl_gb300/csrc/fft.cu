@@ -9,7 +9,15 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cufftXt.h>
+
 #include "common.cuh"
+
+// LTO IR of lto/spectral_cb.cu, embedded at build time (sm_103a and sm_103 targets)
+extern "C" const unsigned char baorec_lto_spectral_cb_a[];
+extern "C" const size_t baorec_lto_spectral_cb_a_size;
+extern "C" const unsigned char baorec_lto_spectral_cb_p[];
+extern "C" const size_t baorec_lto_spectral_cb_p_size;
 
 namespace baorec {
 namespace {
@@ -499,6 +507,99 @@ int spectral_tables(baorec_ctx* ctx) {
   return BAOREC_OK;
 }
 
+// Parameters of the LTO load callback (the same layout as in lto/spectral_cb.cu).
+struct SpecCallbackInfo {
+  const float* tab;
+  unsigned long long nk;
+  int n1h, n2, n3;
+  float diag[3], cross[3];
+  float invN;
+};
+
+// written by a kernel, so the update is ordered on the stream like the transforms
+__global__ void set_callback_info_kernel(SpecCallbackInfo* dst, SpecCallbackInfo v) { *dst = v; }
+
+// The inverse transform of the preconditioner with the k-space multiply as a
+// cuFFT load callback.  Any failure (a cuFFT without LTO callbacks, a JIT
+// link error) leaves the separate multiply kernel in use and notes why.
+// one attempt with one IR target; on failure *stage/*res say where
+bool try_callback_plan(baorec_ctx* ctx, const char* symbol, const unsigned char* ir, size_t ir_size, cufftHandle* out,
+                       size_t* work, const char** stage, cufftResult* res) {
+  cufftHandle p = 0;
+  long long dims[3] = {ctx->n3, ctx->n2, ctx->n1};
+  void* info[1] = {ctx->spec_cb};
+  *res = CUFFT_SUCCESS;
+  *stage = "cufftCreate";
+  if ((*res = cufftCreate(&p)) != CUFFT_SUCCESS) return false;
+  *stage = "cufftXtSetJITCallback";
+  if ((*res = cufftXtSetJITCallback(p, symbol, ir, ir_size, CUFFT_CB_LD_COMPLEX, info)) == CUFFT_SUCCESS) {
+    *stage = "cufftSetAutoAllocation";
+    if ((*res = cufftSetAutoAllocation(p, 0)) == CUFFT_SUCCESS) {
+      // 32-bit plan interface (the sizes of one spectrum fit)
+      int n[3] = {(int)dims[0], (int)dims[1], (int)dims[2]};
+      *stage = "cufftMakePlanMany";
+      if ((*res = cufftMakePlanMany(p, 3, n, nullptr, 1, (int)ctx->Nk, nullptr, 1, (int)ctx->N, CUFFT_C2R, 1,
+                                    work)) == CUFFT_SUCCESS) {
+        *out = p;
+        return true;
+      }
+    }
+  }
+  cufftDestroy(p);
+  return false;
+}
+
+// The inverse transform of the preconditioner with the k-space multiply as a
+// cuFFT load callback.  Any failure (a cuFFT without LTO callbacks, a JIT
+// link error) leaves the separate multiply kernel in use and notes why.
+void spectral_callback_plan(baorec_ctx* ctx) {
+  ctx->spec_cb_state = -1;
+  if (ctx->Nk >= (1ull << 32)) {
+    snprintf(ctx->spec_cb_note, sizeof(ctx->spec_cb_note), "spectrum above 2^32 modes");
+    return;
+  }
+  if (!ctx->spec_cb && cudaMalloc(&ctx->spec_cb, sizeof(SpecCallbackInfo)) != cudaSuccess) {
+    cudaGetLastError();
+    snprintf(ctx->spec_cb_note, sizeof(ctx->spec_cb_note), "callback parameters: cudaMalloc failed");
+    return;
+  }
+  const unsigned char* irs[2] = {baorec_lto_spectral_cb_a, baorec_lto_spectral_cb_p};
+  const size_t sizes[2] = {baorec_lto_spectral_cb_a_size, baorec_lto_spectral_cb_p_size};
+  const char* names[2] = {"sm_103a", "sm_103"};
+  const char* symbols[2] = {"baorec_spectral_load", "_Z21baorec_spectral_load2PvyS_S_"};
+  char why[4][48] = {{0}, {0}, {0}, {0}};
+  for (int t = 0; t < 4; ++t) {
+    const int v = t / 2, sy = t % 2;
+    cufftHandle p = 0;
+    size_t w = 0;
+    const char* stage = "";
+    cufftResult r = CUFFT_SUCCESS;
+    if (!try_callback_plan(ctx, symbols[sy], irs[v], sizes[v], &p, &w, &stage, &r)) {
+      snprintf(why[t], sizeof(why[t]), "%s/%d: %s %d", names[v], sy, stage + 4, (int)r);
+      continue;
+    }
+    if (w > ctx->fft_work_bytes && !ctx->spec_work && cudaMalloc(&ctx->spec_work, w) != cudaSuccess) {
+      cudaGetLastError();
+      cufftDestroy(p);
+      snprintf(why[t], sizeof(why[t]), "%s: work area", names[v]);
+      continue;
+    }
+    if (cufftSetWorkArea(p, ctx->spec_work ? ctx->spec_work : ctx->fft_work) != CUFFT_SUCCESS ||
+        cufftSetStream(p, ctx->stream) != CUFFT_SUCCESS) {
+      cufftDestroy(p);
+      snprintf(why[t], sizeof(why[t]), "%s: work area / stream", names[v]);
+      continue;
+    }
+    ctx->plan_c2r_spec = p;
+    ctx->spec_cb_state = 1;
+    snprintf(ctx->spec_cb_note, sizeof(ctx->spec_cb_note), "k-space multiply fused as a cuFFT LTO load callback (%s IR)",
+             names[v]);
+    return;
+  }
+  snprintf(ctx->spec_cb_note, sizeof(ctx->spec_cb_note), "callback plan unavailable (%s; %s; %s; %s)", why[0], why[1],
+           why[2], why[3]);
+}
+
 }  // namespace
 
 // e = S⁻¹ r (zero mean), S the operator with the box's mean line of sight.
@@ -506,7 +607,20 @@ int spectral_tables(baorec_ctx* ctx) {
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   SGeom g = sgeom_of(ctx);
   CKS(spectral_tables(ctx));
+  if (ctx->spec_cb_state == 0) spectral_callback_plan(ctx);
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));
+  if (ctx->spec_cb_state == 1) {
+    SpecCallbackInfo info;
+    info.tab = ctx->stab;
+    info.nk = ctx->Nk;
+    info.n1h = g.n1h; info.n2 = g.n2; info.n3 = g.n3;
+    for (int a = 0; a < 3; ++a) { info.diag[a] = g.diag[a]; info.cross[a] = g.cross[a]; }
+    info.invN = g.invN;
+    set_callback_info_kernel<<<1, 1, 0, ctx->stream>>>((SpecCallbackInfo*)ctx->spec_cb, info);
+    CKLAUNCH();
+    CKFFT(cufftExecC2R(ctx->plan_c2r_spec, ctx->ck, e));
+    return BAOREC_OK;
+  }
   // rows of n1h threads per block (n1h <= 1024, as the mesh-size limit guarantees up to n1 = 2046)
   if (ctx->n1h > 1024) return set_error(ctx, BAOREC_ERR_ARG, "FFT start: n1 above 2046");
   const int rpb = std::max(1, 1024 / ctx->n1h);
@@ -524,4 +638,23 @@ extern "C" int baorec_smooth(baorec_ctx* ctx, float* mesh) {
   if (!ctx || !mesh) return BAOREC_ERR_ARG;
   CKS(baorec::smooth(ctx, mesh));
   return baorec::finish(ctx, 0);
+}
+
+extern "C" int baorec_fft_callbacks(const baorec_ctx* ctx, const char** note) {
+  if (!ctx) return -1;
+  if (note) *note = ctx->spec_cb_note;
+  return ctx->spec_cb_state;
+}
+
+extern "C" int baorec_set_fft_callbacks(baorec_ctx* ctx, int enable) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (!enable) {
+    ctx->spec_cb_state = -1;
+    snprintf(ctx->spec_cb_note, sizeof(ctx->spec_cb_note), "callbacks disabled by the caller");
+  } else if (ctx->plan_c2r_spec) {
+    ctx->spec_cb_state = 1;
+  } else {
+    ctx->spec_cb_state = 0;   // build the callback plan at the next correction
+  }
+  return BAOREC_OK;
 }

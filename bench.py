@@ -456,6 +456,7 @@ def run_gb300(args):
             "config": {"workload": f"lightcone MG reconstruction {args.mesh}^3 to 1e-6 relative residual, "
                                    f"{nd} data + {nr} randoms, CIC, R=15, b=2, f=0.8, local LOS, 2+2 RB sweeps",
                        "mesh": args.mesh, "start": args.start, "autotune": tune,
+                       "fft_callback": ctx.fft_callbacks(),
                        "l2": "working set per step > 1 GB >> 126 MB L2 (inputs larger than L2)",
                        "parallelism": f"replicas x{ws}"},
             "solver": {"start": args.start, "cycles": stats["cycles"], "spectral_steps": stats["spectral_steps"],

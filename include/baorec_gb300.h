@@ -232,6 +232,13 @@ int baorec_solve_history(const baorec_ctx* ctx, double* rho, int32_t* kind, int 
 /* Relative residual |r - mean r| / |f - mean f| of the start of kind
  * BAOREC_START_* (zero, FFT, learned) for the right-hand side f (device mesh). */
 int baorec_start_residual(baorec_ctx* ctx, const float* f, int start, double* rel_residual);
+/* Whether the FFT start's k-space multiply runs as a cuFFT LTO load callback
+ * (1), as a separate kernel (-1: not requested or unavailable, *note says
+ * which) or is requested and not set up yet (0). */
+int baorec_fft_callbacks(const baorec_ctx* ctx, const char** note);
+/* Request (1) or drop (0, the default) the callback form; a request that
+ * cuFFT cannot honour leaves the kernel form in use. */
+int baorec_set_fft_callbacks(baorec_ctx* ctx, int enable);
 
 /* reconstructed_overdensity! (src/recon.jl:93-132): overdensity then n_iter
  * iterations into the context result.  rx.. may be NULL (data only). */

@@ -123,3 +123,28 @@ def test_spectral_start_reaches_same_solution_with_fewer_cycles(los):
         # one line of sight: the FFT inverse is exact, no V-cycle is needed
         assert s1["cycles"] == 0, s1
     assert max(rel_l2(g1[a], g0[a]) for a in range(3)) < 2e-5
+
+
+def test_fft_start_callback_and_kernel_forms_agree():
+    """The preconditioner multiply as a cuFFT LTO load callback (when cuFFT
+    can build that plan) and as a separate kernel: same converged solution;
+    a request cuFFT cannot honour falls back to the kernel and says why."""
+    import baorec
+    f, bs, bm = _problem(n=64, seed=7)
+    ff = np.asfortranarray(f)
+    grads, states = [], []
+    for enable in (1, 0):
+        rec = _recon(bs, bm, None, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="spectral")
+        ctx = baorec.setup_fft_(rec, f.shape)
+        ctx.call("baorec_set_fft_callbacks", enable)
+        phi = baorec.zeros_mesh(f.shape, device=False)
+        st = baorec.solve_(phi, ff, rec)
+        assert st["rel_residual"] <= 1e-6
+        states.append(ctx.fft_callbacks())
+        grads.append(O.gradient_meshes(np.asarray(phi, np.float64), bs.astype(np.float64)))
+    print(states)
+    assert states[0]["state"] in (1, -1)
+    if states[0]["state"] == -1:
+        assert "unavailable" in states[0]["note"]
+    assert states[1]["state"] == -1
+    assert max(rel_l2(grads[0][a], grads[1][a]) for a in range(3)) < 2e-5
