@@ -124,6 +124,8 @@ _SIGS = {
     "baorec_batch_destroy": (C.c_int, [P]),
     "baorec_autotune": (C.c_int, [P, U32, I32P, I32P]),
     "baorec_set_tune": (C.c_int, [P, C.c_int32, I32P]),
+    "baorec_tune_stream": (C.c_int, [P]),
+    "baorec_set_tune_stream": (C.c_int, [P, C.c_int]),
     "baorec_guess_num_params": (I64, []),
     "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
     "baorec_guess_set_params": (C.c_int, [P, P, I64]),
@@ -238,7 +240,8 @@ class Context:
         pt = C.c_int32()
         bt = (C.c_int32 * 16)()
         self.call("baorec_autotune", (1 if stencil else 0) | (2 if paint else 0), C.byref(pt), bt)
-        return {"paint_tile": pt.value, "tile16_per_level": list(bt)}
+        return {"paint_tile": pt.value, "tile16_per_level": list(bt),
+                "stream_residuals": int(self.lib.baorec_tune_stream(self.h))}
 
     def fft_callbacks(self) -> dict:
         """State of the FFT start's cuFFT load callback (baorec_fft_callbacks)."""

@@ -752,6 +752,9 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   const bool aligned = (uintptr_t)phi % 16 == 0 && (uintptr_t)ctx->phi_lo % 16 == 0 && (uintptr_t)ctx->phi_hi2 % 16 == 0 &&
                        (uintptr_t)ctx->phi_lo2 % 16 == 0;
   const bool tile0 = aligned && tile_ok(L0.n) && (size_t)tile_blocks(G) <= kMaxPartials;
+  // the streaming residual kernels unless the autotuner chose the tile ones
+  const bool stream0 = aligned && stream_ok(L0.n) && ctx->tune.stream0 != 0 &&
+                       (size_t)stream_blocks(L0.n) <= kMaxPartials;
   int nparts = kResBlocks;
   // spectral corrections (FFT inverse of the operator with the box's mean line
   // of sight) run first, for as long as each one shrinks the residual by at
@@ -762,7 +765,11 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   int nspec = 0, m_last = 0;
   double rho_prev = 0.0, rate = 0.0;
   for (int it = 0;; ++it) {
-    if (tile0) {
+    if (stream0) {
+      CK(launch_resid_acc_stream(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
+                                 ctx->dred, &nparts));
+      ctx->launches++;
+    } else if (tile0) {
       CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
                           ctx->dred, &nparts));
       ctx->launches++;
@@ -818,7 +825,10 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       for (int q = 1; q < m; ++q) {
         const float* dprev = q == 1 ? L0.v : d;
         float* acc = q == 1 ? nullptr : L0.v;
-        if (tile0) {
+        if (stream0) {
+          CK(launch_resid_diff_stream(ctx->stream, dprev, rin, rout, G, acc));
+          ctx->launches++;
+        } else if (tile0) {
           CK(launch_resid_diff(ctx->stream, dprev, rin, rout, G, acc));
           ctx->launches++;
         } else {
@@ -880,6 +890,10 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else if (which == 1)
       resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, N,
                                                             0.0f, ctx->dred);
+    else if (which == 4)
+      launch_resid_acc_stream(ctx->stream, L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, 0.0f, ctx->dred, &np);
+    else if (which == 5)
+      launch_resid_diff_stream(ctx->stream, L.v, L.f, t, G, L.r);
     else if (which == 3 && tile_ok(L.n))
       launch_resid_diff(ctx->stream, L.v, L.f, t, G, L.r);
     else if (which == 3)
@@ -887,7 +901,8 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else
       jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
   };
-  if (which < 0 || which > 3) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  if (which < 0 || which > 5) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  if (which >= 4 && !stream_ok(L.n)) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: no streaming form here");
   launch();   // warm-up
   CK(cudaEventRecord(a, ctx->stream));
   for (int r = 0; r < reps; ++r) launch();
@@ -904,6 +919,7 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   // the one-cell kernel does one colour, half of that); the accurate residual
   // reads hi, lo, e, f and writes hi, lo, r (28 B/cell); the FP32 running
   // residual of the FFT corrections reads d, r, acc and writes r, acc (20 B/cell)
-  *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : which == 1 ? 28.0 * N : which == 3 ? 20.0 * N : 12.0 * N;
+  *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : (which == 1 || which == 4) ? 28.0 * N
+          : (which == 3 || which == 5) ? 20.0 * N : 12.0 * N;
   return BAOREC_OK;
 }

@@ -124,6 +124,14 @@ cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* e, const float* f,
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts);
 int tile_blocks(const LG& G);
+// streaming (2.5-D, cp.async-pipelined) forms of the finest-level residuals (mg_stream.cu)
+bool stream_ok(const int n[3]);
+int stream_blocks(const int n[3]);
+cudaError_t launch_resid_acc_stream(cudaStream_t s, const float* hi, const float* lo, const float* e, const float* f,
+                                    float* ohi, float* olo, float* r, const LG& G, float alpha, double* part,
+                                    int* nparts);
+cudaError_t launch_resid_diff_stream(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
+                                     float* acc);
 
 // ---- cooperative coarse tail (mg_tail.cu) -----------------------------------
 constexpr int kTailMaxCells = 64 * 64 * 64;   // levels at most this big run in the tail kernel

@@ -86,6 +86,31 @@ int tune_stencils(baorec_ctx* ctx) {
     }
     ctx->tune.big_tiles[l] = pick;
   }
+  // finest level: the streaming residual kernels against the tiled ones
+  Level& L0 = ctx->lev[0];
+  if (nl > 0 && tile_ok(L0.n) && stream_ok(L0.n)) {
+    const LG G0 = level_geom_public(ctx, 0, 0.0f);
+    float* t = L0.r + L0.N;
+    float ms[2] = {0.0f, 0.0f};
+    for (int form = 0; form < 2; ++form) {
+      auto launch = [&]() -> int {
+        int np = 0;
+        if (form == 1) {
+          CK(launch_resid_acc_stream(ctx->stream, L0.v, ctx->phi_lo, nullptr, L0.f, ctx->phi_hi2, ctx->phi_lo2, L0.r,
+                                     G0, 0.0f, ctx->dred, &np));
+          CK(launch_resid_diff_stream(ctx->stream, L0.v, L0.f, t, G0, L0.r));
+        } else {
+          CK(launch_resid_acc(ctx->stream, L0.v, ctx->phi_lo, nullptr, L0.f, ctx->phi_hi2, ctx->phi_lo2, L0.r, G0,
+                              0.0f, ctx->dred, &np));
+          CK(launch_resid_diff(ctx->stream, L0.v, L0.f, t, G0, L0.r));
+        }
+        return BAOREC_OK;
+      };
+      CKS(time_ms(ctx, launch, 5, &ms[form]));
+      ctx->launches += 12;
+    }
+    ctx->tune.stream0 = ms[1] <= ms[0] ? 1 : 0;
+  }
   return BAOREC_OK;
 }
 
@@ -121,6 +146,14 @@ int tune_paint(baorec_ctx* ctx) {
 }  // namespace baorec
 
 using namespace baorec;
+
+extern "C" int baorec_tune_stream(const baorec_ctx* ctx) { return ctx ? ctx->tune.stream0 : -1; }
+
+extern "C" int baorec_set_tune_stream(baorec_ctx* ctx, int stream) {
+  if (!ctx || stream < -1 || stream > 1) return BAOREC_ERR_ARG;
+  ctx->tune.stream0 = stream;
+  return BAOREC_OK;
+}
 
 extern "C" int baorec_autotune(baorec_ctx* ctx, uint32_t what, int32_t* paint_tile, int32_t* big_tiles) {
   if (!ctx) return BAOREC_ERR_ARG;

@@ -379,9 +379,10 @@ def run_gb300(args):
     # red-black sweep for the plain multigrid start
     peak, peak_src = measured_peak()
     N = int(np.prod(n))
-    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: "resid_kernel (difference form)"}
+    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: "resid_kernel (difference form)",
+             4: "resid_acc_stream_kernel", 5: "resid_diff_stream_kernel"}
     meas = {}
-    for which in (() if args.no_kernels else (0, 1, 3)):
+    for which in (() if args.no_kernels else (0, 1, 3, 4, 5)):
         avg, nbytes = C.c_float(), C.c_double()
         ctx.call("baorec_profile_kernel", which, 30, C.byref(avg), C.byref(nbytes))
         ach = nbytes.value / (avg.value * 1e-3) / 1e9
@@ -389,7 +390,8 @@ def run_gb300(args):
                        "frac": ach / peak, "peak_source": peak_src,
                        "traffic": traffic_per_launch(names[which].split()[0], N),
                        "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
-    head = 0 if args.start == "zero" else 1
+    # the accurate residual in the form the solve uses (streaming unless the tuner chose the tiles)
+    head = 0 if args.start == "zero" else (4 if tune.get("stream_residuals", -1) != 0 else 1)
     roofline, aux = None, {}
     if meas:
         roofline = dict(meas[head])

@@ -371,6 +371,10 @@ int baorec_batch_destroy(baorec_batch* b);
 int baorec_autotune(baorec_ctx* ctx, uint32_t what, int32_t* paint_tile, int32_t* big_tiles);
 /* Set the shapes explicitly (paint tile edge 1..16; per-level choices as above, NULL keeps them). */
 int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tiles);
+/* Finest-level residual kernels of the convergent solve: 1 streaming (z-marching,
+ * cp.async-pipelined), 0 tiled, -1 not tuned (streaming where the mesh allows). */
+int baorec_tune_stream(const baorec_ctx* ctx);
+int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
 
 #ifdef __cplusplus
 }
