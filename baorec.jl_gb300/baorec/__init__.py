@@ -10,7 +10,8 @@ from .recon import *  # noqa: F401,F403
 from .recon import __all__ as _recon_all
 from . import mocks  # noqa: F401
 from . import guess  # noqa: F401
+from . import cosmo  # noqa: F401
 from .batch import Batch  # noqa: F401
 from ._lib import load as load_library, lib_path  # noqa: F401
 
-__all__ = list(_recon_all) + ["mocks", "guess", "Batch", "load_library", "lib_path"]
+__all__ = list(_recon_all) + ["mocks", "guess", "cosmo", "Batch", "load_library", "lib_path"]

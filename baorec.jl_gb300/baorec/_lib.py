@@ -126,6 +126,11 @@ _SIGS = {
     "baorec_set_tune": (C.c_int, [P, C.c_int32, I32P]),
     "baorec_tune_stream": (C.c_int, [P]),
     "baorec_set_tune_stream": (C.c_int, [P, C.c_int]),
+    "baorec_sky_to_cartesian": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
+                                          P, P, P, U32]),
+    "baorec_cartesian_to_sky": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
+                                          P, P, P, U32]),
+    "baorec_fkp_weights": (C.c_int, [P, P, I64, C.c_float, P, U32]),
     "baorec_guess_num_params": (I64, []),
     "baorec_guess_init": (C.c_int, [P, C.c_uint32]),
     "baorec_guess_set_params": (C.c_int, [P, P, I64]),

@@ -376,6 +376,22 @@ int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tile
 int baorec_tune_stream(const baorec_ctx* ctx);
 int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
 
+/* ---- Catalog coordinates (examples/lightcone.jl:30-82) ------------------------
+ * sky_to_cartesian (lightcone.jl:30-47): ra, dec in degrees and redshift z ->
+ * comoving x, y, z in Mpc/h; cartesian_to_sky (lightcone.jl:50-80) the
+ * inverse, with the script's ra convention ((lon - 360) rem 360).  The host
+ * passes the comoving-distance table r(z) (Mpc, FP64, ntab values on a uniform
+ * grid z_min..z_max, as comoving_distance_interp of src/cosmo.jl:83-90 tabulates
+ * it) and h; values outside the table return BAOREC_ERR_OOB (the reference's
+ * interpolation throws).  fkp_weights (lightcone.jl:82): w = 1/(1 + nz P0). */
+int baorec_sky_to_cartesian(baorec_ctx* ctx, const float* ra, const float* dec, const float* z, int64_t n,
+                            const double* r_table, int32_t ntab, double z_min, double z_max, float h,
+                            float* x, float* y, float* zc, uint32_t flags);
+int baorec_cartesian_to_sky(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
+                            const double* r_table, int32_t ntab, double z_min, double z_max, float h,
+                            float* ra, float* dec, float* red, uint32_t flags);
+int baorec_fkp_weights(baorec_ctx* ctx, const float* nz, int64_t n, float P0, float* w, uint32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

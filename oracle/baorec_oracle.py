@@ -862,3 +862,43 @@ def solve_mg(f, box_size, box_min, beta, los=None, rtol=1e-6, max_cycles=50, nu1
 def coefs_f64(c):
     """Coefficient arrays promoted to FP64 (same values)."""
     return tuple(np.asarray(a, dtype=np.float64) for a in c)
+
+
+# ---- catalog coordinates (examples/lightcone.jl:30-82) ------------------------
+
+def _interp_uniform(zg, r, z):
+    """Gridded(Linear()) interpolation of r on the uniform grid zg (src/cosmo.jl:83-90)."""
+    return np.interp(np.asarray(z, np.float64), zg, r)
+
+
+def sky_to_cartesian(ra, dec, red, zg, r, h):
+    """examples/lightcone.jl:30-47: FP32 angles (x * Float32(π) / 180), FP32
+    trigonometry, FP64 distance products stored as FP32."""
+    F = np.float32
+    pi = F(np.pi)
+    a = (np.asarray(ra, F) * pi) / F(180)
+    d = (np.asarray(dec, F) * pi) / F(180)
+    dist = _interp_uniform(zg, r, red)
+    cd, sd, ca, sa = (np.cos(d).astype(np.float64), np.sin(d).astype(np.float64),
+                      np.cos(a).astype(np.float64), np.sin(a).astype(np.float64))
+    hh = float(F(h))
+    return ((dist * cd * ca * hh).astype(F), (dist * cd * sa * hh).astype(F), (dist * sd * hh).astype(F))
+
+
+def cartesian_to_sky(x, y, z, zg, r, h):
+    """examples/lightcone.jl:50-80, including ra = (lon - 360) rem 360."""
+    F = np.float32
+    x, y, z = (np.asarray(v, F) for v in (x, y, z))
+    rr = np.sqrt(x * x + y * y + z * z) / F(h)
+    s = np.sqrt(x * x + y * y)
+    lon = (np.arctan2(y, x) * F(180)) / F(np.pi)
+    lat = (np.arctan2(z, s) * F(180)) / F(np.pi)
+    lon = np.fmod(lon - F(360), F(360))
+    red = np.interp(rr.astype(np.float64), r, zg)
+    return lon.astype(F), lat.astype(F), red.astype(F)
+
+
+def fkp_weights(nz, P0):
+    """examples/lightcone.jl:82."""
+    F = np.float32
+    return (F(1) / (F(1) + np.asarray(nz, F) * F(P0))).astype(F)
