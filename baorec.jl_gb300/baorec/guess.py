@@ -78,6 +78,38 @@ def sample(ctx: _lib.Context, cfg: TrainConfig, index: int, f_ptr: int, phi_ptr:
     ctx.call("baorec_guess_sample", C.byref(c), int(index), f_ptr, phi_ptr)
 
 
+def set_conv_path(ctx: _lib.Context, tensor_core: bool) -> None:
+    """Run the covered 3x3x3 layers on the tcgen05 kernel (True, the default)
+    or every layer on the mma.sync kernels (False)."""
+    ctx.call("baorec_guess_set_conv_path", 1 if tensor_core else 0)
+
+
+def tc_layers(ctx: _lib.Context) -> int:
+    """Convolutions of the last network forward that ran on tcgen05."""
+    return int(ctx.lib.baorec_guess_tc_layers(ctx.h))
+
+
+def conv3(ctx: _lib.Context, x, w, bias=None, add=None, relu: bool = False, path: str = "tcgen05"):
+    """One 3x3x3 zero-padded convolution of the network on CUDA tensors:
+    x (n, n, n, cin) BF16 indexed [z, y, x, c]; w (27, cin, cout) FP32 with
+    tap t = dx + 3 dy + 9 dz; bias (cout,) FP32; add (n, n, n, cout) BF16.
+    Returns relu?(conv(x) + bias + add) as (n, n, n, cout) BF16.  path:
+    "mma" (mma.sync), "tcgen05" (TMA slab loads, the network's path),
+    "tcgen05_cpasync" (cp.async slab loads)."""
+    import torch
+    n, cin = int(x.shape[0]), int(x.shape[3])
+    cout = int(w.shape[2])
+    x = x.contiguous()
+    w = w.to(torch.float32).contiguous()
+    y = torch.empty((n, n, n, cout), dtype=torch.bfloat16, device=x.device)
+    b = bias.to(torch.float32).contiguous() if bias is not None else None
+    ad = add.contiguous() if add is not None else None
+    ctx.call("baorec_guess_conv3", cin, cout, n, x.data_ptr(), w.data_ptr(), b.data_ptr() if b is not None else None,
+             ad.data_ptr() if ad is not None else None, y.data_ptr(), 1 if relu else 0,
+             {"mma": 0, "tcgen05": 1, "tcgen05_cpasync": 2}[path])
+    return y
+
+
 def save(path: str, params) -> None:
     np.save(path, np.asarray(params, np.float32))
 

@@ -49,6 +49,8 @@ int finish(baorec_ctx* ctx, uint32_t flags) {
     CK(cudaStreamSynchronize(ctx->stream));
     if (e & kErrOOB)
       return set_error(ctx, BAOREC_ERR_OOB, "particle outside the mesh (the reference raises BoundsError)");
+    if (e & kErrTimeout)
+      return set_error(ctx, BAOREC_ERR_CUDA, "a device-side wait timed out (tensor-core convolution pipeline)");
   }
   return BAOREC_OK;
 }

@@ -19,6 +19,7 @@ constexpr size_t kRedCapacity = 1u << 17;   // FP64 entries of the reduction-par
 // Device-side error word bits (set by kernels, read after a sync).
 enum : unsigned {
   kErrOOB = 1u,        // particle index outside the mesh
+  kErrTimeout = 2u,    // a bounded device-side wait gave up (pipeline stalled)
 };
 
 struct Level {                        // one multigrid level

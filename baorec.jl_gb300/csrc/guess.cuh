@@ -35,6 +35,10 @@ struct ConvArgs {
   const float* bias;         // per output channel, or null
   int relu;
   int n_in, n_out;           // cube edge of the input and output grids
+  // tensor-core (tcgen05) path, taken for the shapes tc_supported() accepts:
+  const __nv_bfloat16* wimg = nullptr;   // weight image (weight_image), null = mma.sync path
+  unsigned* err = nullptr;               // device error word (kErrTimeout)
+  int tc_loader = 0;                     // slab loader: 0 TMA boxes, 1 cp.async warps
 };
 
 struct WgradArgs {
@@ -55,7 +59,24 @@ inline size_t frag_count(int kind, int cin, int cout) {
   return (size_t)taps_of(kind) * ks * (cout / 8) * 32;
 }
 
+// layer shapes with an mma.sync kernel (guess_kernels.cu)
+#define BAOREC_GUESS_SHAPES(X)                                                                     \
+  X(C3, 8, 16) X(C3, 16, 16) X(C3, 32, 32) X(C3, 64, 64) X(C3, 64, 32) X(C3, 32, 16) X(C3, 16, 32) \
+  X(C3, 32, 64) X(DN, 16, 32) X(DN, 32, 64) X(UP, 64, 32) X(UP, 32, 16)
+
+// C3 shapes with a tcgen05 kernel (guess_tc.cu); grids with n % 128 == 0
+#define BAOREC_GUESS_TC_SHAPES(X) X(16, 16) X(32, 32) X(32, 16) X(16, 32) X(32, 64)
+
+inline size_t image_count(int cin, int cout) { return (size_t)27 * cin * cout; }
+
+// Dispatches to the tcgen05 kernel when a.wimg is set and the shape is
+// covered, to the mma.sync kernel otherwise.
 cudaError_t conv_forward(cudaStream_t s, int kind, int cin, int cout, const ConvArgs& a);
+bool tc_supported(int kind, int cin, int cout, int n);
+cudaError_t conv_forward_tc(cudaStream_t s, int cin, int cout, const ConvArgs& a);
+// fp32 master W[t][ci][co] -> the tcgen05 weight image of the forward (or,
+// with backward, the backward-data) convolution of a C3 layer
+cudaError_t weight_image(cudaStream_t s, int cin, int cout, const float* w, __nv_bfloat16* img, bool backward);
 cudaError_t conv_wgrad(cudaStream_t s, int kind, int cin, int cout, const WgradArgs& a);
 // fp32 master W[t][ci][co] -> fragments; transpose_flip selects the backward
 // data weights (W'[t'][co][ci] = W[flip(t)][ci][co], flip only for C3).

@@ -286,11 +286,8 @@ cudaError_t wgrad_t(cudaStream_t s, const WgradArgs& a) {
 
 }  // namespace
 
-#define BAOREC_GUESS_SHAPES(X)                                                                     \
-  X(C3, 8, 16) X(C3, 16, 16) X(C3, 32, 32) X(C3, 64, 64) X(C3, 64, 32) X(C3, 32, 16) X(C3, 16, 32) \
-  X(C3, 32, 64) X(DN, 16, 32) X(DN, 32, 64) X(UP, 64, 32) X(UP, 32, 16)
-
 cudaError_t conv_forward(cudaStream_t s, int kind, int cin, int cout, const ConvArgs& a) {
+  if (a.wimg && a.n_in == a.n_out && tc_supported(kind, cin, cout, a.n_out)) return conv_forward_tc(s, cin, cout, a);
 #define X(K, I, O) \
   if (kind == K && cin == I && cout == O) return fwd_t<K, I, O>(s, a);
   BAOREC_GUESS_SHAPES(X)

@@ -388,6 +388,12 @@ struct GuessNet {
   uint2* ffrag[kLayers] = {};
   uint2* bfrag[kLayers] = {};
   void* frag_mem = nullptr;
+  // tcgen05 weight images of the layers whose shape has a tensor-core kernel
+  bf16* fimg[kLayers] = {};
+  bf16* bimg[kLayers] = {};
+  void* img_mem = nullptr;
+  bool use_tc = true;
+  int tc_layers = 0;         // convolutions of the last forward that ran on tcgen05
   bf16* act[T_COUNT] = {};
   bf16* grad[T_COUNT] = {};
   void* act_mem = nullptr;
@@ -433,6 +439,30 @@ int net_alloc(baorec_ctx* ctx) {
     const int k2 = L.kind == DN ? UP : L.kind == UP ? DN : C3;
     g->bfrag[l] = fp;
     fp += guess::frag_count(k2, L.cout, L.cin);
+  }
+  // weight images, 256-byte aligned each
+  size_t ni = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDef& L = kNet[l];
+    const int nl = g->n >> kTensors[L.out_t].level;
+    if (guess::tc_supported(L.kind, L.cin, L.cout, nl)) ni += (guess::image_count(L.cin, L.cout) * 2 + 255) / 256;
+    if (l > 0 && guess::tc_supported(L.kind, L.cout, L.cin, nl)) ni += (guess::image_count(L.cout, L.cin) * 2 + 255) / 256;
+  }
+  if (ni) {
+    CK(cudaMalloc(&g->img_mem, ni * 256));
+    char* ip = (char*)g->img_mem;
+    for (int l = 0; l < kLayers; ++l) {
+      const LayerDef& L = kNet[l];
+      const int nl = g->n >> kTensors[L.out_t].level;
+      if (guess::tc_supported(L.kind, L.cin, L.cout, nl)) {
+        g->fimg[l] = (bf16*)ip;
+        ip += (guess::image_count(L.cin, L.cout) * 2 + 255) / 256 * 256;
+      }
+      if (l > 0 && guess::tc_supported(L.kind, L.cout, L.cin, nl)) {
+        g->bimg[l] = (bf16*)ip;
+        ip += (guess::image_count(L.cout, L.cin) * 2 + 255) / 256 * 256;
+      }
+    }
   }
   size_t na = 0;
   for (int t = 0; t < T_COUNT; ++t) na += nvox(g, kTensors[t].level) * kTensors[t].ch;
@@ -484,6 +514,14 @@ int net_frags(baorec_ctx* ctx) {
       CK(guess::weight_frags(ctx->stream, L.kind, L.cin, L.cout, g->params + kP.w[l], g->bfrag[l], true));
       ctx->launches++;
     }
+    if (g->fimg[l]) {
+      CK(guess::weight_image(ctx->stream, L.cin, L.cout, g->params + kP.w[l], g->fimg[l], false));
+      ctx->launches++;
+    }
+    if (g->bimg[l]) {
+      CK(guess::weight_image(ctx->stream, L.cin, L.cout, g->params + kP.w[l], g->bimg[l], true));
+      ctx->launches++;
+    }
   }
   g->frags_ok = true;
   return BAOREC_OK;
@@ -493,6 +531,7 @@ int net_frags(baorec_ctx* ctx) {
 int net_forward(baorec_ctx* ctx) {
   GuessNet* g = ctx->net;
   CKS(net_frags(ctx));
+  g->tc_layers = 0;
   for (int l = 0; l < kLayers; ++l) {
     const LayerDef& L = kNet[l];
     guess::ConvArgs a;
@@ -507,6 +546,9 @@ int net_forward(baorec_ctx* ctx) {
     a.relu = 1;
     a.n_in = g->n >> kTensors[L.in_t].level;
     a.n_out = g->n >> kTensors[L.out_t].level;
+    a.wimg = g->use_tc ? g->fimg[l] : nullptr;
+    a.err = ctx->derr;
+    if (a.wimg) g->tc_layers++;
     CK(guess::conv_forward(ctx->stream, L.kind, L.cin, L.cout, a));
     ctx->launches++;
   }
@@ -581,6 +623,8 @@ int net_backward(baorec_ctx* ctx) {
     a.relu = 0;
     a.n_in = w.n_out;
     a.n_out = w.n_in;
+    a.wimg = g->use_tc ? g->bimg[l] : nullptr;
+    a.err = ctx->derr;
     const int k2 = L.kind == DN ? UP : L.kind == UP ? DN : C3;
     CK(guess::conv_forward(ctx->stream, k2, L.cout, L.cin, a));
     ctx->launches++;
@@ -691,6 +735,7 @@ void guess_free(baorec_ctx* ctx) {
   cudaFree(g->adam_m);
   cudaFree(g->adam_v);
   cudaFree(g->frag_mem);
+  cudaFree(g->img_mem);
   cudaFree(g->act_mem);
   cudaFree(g->grad_mem);
   cudaFree(g->out);
@@ -848,4 +893,60 @@ extern "C" int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_conf
   CKS(baorec_set_box(ctx, ctx->cfg.box_size, saved_box));
   ctx->has_result = false;
   return finish(ctx, 0);
+}
+
+extern "C" int baorec_guess_set_conv_path(baorec_ctx* ctx, int32_t tensor_core) {
+  if (!ctx || tensor_core < 0 || tensor_core > 1) return BAOREC_ERR_ARG;
+  CKS(net_alloc(ctx));
+  ctx->net->use_tc = tensor_core != 0;
+  return BAOREC_OK;
+}
+
+extern "C" int32_t baorec_guess_tc_layers(baorec_ctx* ctx) { return ctx && ctx->net ? ctx->net->tc_layers : -1; }
+
+extern "C" int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, const void* x,
+                                  const float* w, const float* bias, const void* add, void* y, int32_t relu,
+                                  int32_t path) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (!x || !w || !y || n < 1 || path < 0 || path > 2)
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_conv3: bad arguments");
+  bool known = false;
+#define X(K, I, O) \
+  if (K == C3 && cin == I && cout == O) known = true;
+  BAOREC_GUESS_SHAPES(X)
+#undef X
+  if (!known) return set_error(ctx, BAOREC_ERR_ARG, "guess_conv3: no kernel for %d -> %d channels", cin, cout);
+  if (path >= 1 && !guess::tc_supported(C3, cin, cout, n))
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_conv3: no tcgen05 kernel for %d -> %d channels at n = %d", cin, cout, n);
+  uint2* frag = nullptr;
+  bf16* img = nullptr;
+  int rc = BAOREC_OK;
+  cudaError_t e = cudaMalloc(&frag, guess::frag_count(C3, cin, cout) * sizeof(uint2));
+  if (e == cudaSuccess && path >= 1) e = cudaMalloc(&img, guess::image_count(cin, cout) * sizeof(bf16));
+  if (e == cudaSuccess) e = guess::weight_frags(ctx->stream, C3, cin, cout, w, frag, false);
+  if (e == cudaSuccess && img) e = guess::weight_image(ctx->stream, cin, cout, w, img, false);
+  if (e == cudaSuccess) {
+    guess::ConvArgs a;
+    a.in = (const bf16*)x;
+    a.in_cs = cin;
+    a.out = (bf16*)y;
+    a.out_cs = cout;
+    a.add = (const bf16*)add;
+    a.add_cs = cout;
+    a.w = frag;
+    a.bias = bias;
+    a.relu = relu ? 1 : 0;
+    a.n_in = a.n_out = n;
+    a.wimg = img;
+    a.err = ctx->derr;
+    a.tc_loader = path == 2 ? 1 : 0;   // 1: TMA boxes, 2: cp.async warps
+    e = guess::conv_forward(ctx->stream, C3, cin, cout, a);
+    ctx->launches++;
+  }
+  if (e != cudaSuccess) rc = set_error(ctx, BAOREC_ERR_CUDA, "guess_conv3: %s", cudaGetErrorString(e));
+  else rc = finish(ctx, 0);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(frag);
+  cudaFree(img);
+  return rc;
 }

@@ -324,6 +324,22 @@ int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, in
                         float* f, float* phi);
 /* Train on the device; loss_history (host, steps values) may be NULL. */
 int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history);
+/* Convolution kernels of the network: tensor_core 1 (default) runs the 3x3x3
+ * layers whose shape has one on the tcgen05 kernel (TMA-staged operands, TMEM
+ * accumulators; 16/32 input channels, grids with n % 128 == 0), 0 runs every
+ * layer on the mma.sync kernels. */
+int baorec_guess_set_conv_path(baorec_ctx* ctx, int32_t tensor_core);
+/* Convolutions of the last network forward that ran on tcgen05 (-1: no network). */
+int32_t baorec_guess_tc_layers(baorec_ctx* ctx);
+/* One 3x3x3 zero-padded convolution of the network on device arrays: x is
+ * n^3 x cin BF16 (channels fastest, x fastest among voxels), w FP32
+ * [27][cin][cout] with tap t = dx + 3 dy + 9 dz, bias FP32 [cout] or NULL,
+ * add n^3 x cout BF16 or NULL; y = relu?(conv(x) + bias + add) as BF16.
+ * path 0: mma.sync kernel, 1: tcgen05 kernel with TMA-box slab loads (the
+ * network's path), 2: tcgen05 kernel with cp.async slab loads
+ * (BAOREC_ERR_ARG for 1 and 2 if the shape or n has none). */
+int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, const void* x, const float* w,
+                       const float* bias, const void* add, void* y, int32_t relu, int32_t path);
 
 /* ---- Batched box reconstructions in one CUDA graph (no reference counterpart) ----
  * Each item is one periodic-box mock (device arrays; positions in [0, box),
