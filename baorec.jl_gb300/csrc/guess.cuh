@@ -65,9 +65,11 @@ inline size_t frag_count(int kind, int cin, int cout) {
   X(C3, 32, 64) X(DN, 16, 32) X(DN, 32, 64) X(UP, 64, 32) X(UP, 32, 16)
 
 // C3 shapes with a tcgen05 kernel (guess_tc.cu); grids with n % 128 == 0
-#define BAOREC_GUESS_TC_SHAPES(X) X(16, 16) X(32, 32) X(32, 16) X(16, 32) X(32, 64)
+#define BAOREC_GUESS_TC_SHAPES(X) X(8, 16) X(16, 16) X(32, 32) X(32, 16) X(16, 32) X(32, 64) X(64, 32)
 
-inline size_t image_count(int cin, int cout) { return (size_t)27 * cin * cout; }
+// BF16 entries of a tcgen05 weight image: one 16-wide K step per MMA of a
+// slab (9 taps x cin/16 steps, or 6 tap pairs for 8 channels), 3 dz blocks
+inline size_t image_count(int cin, int cout) { return (size_t)(cin == 8 ? 6 : 9 * (cin / 16)) * 16 * 3 * cout; }
 
 // Dispatches to the tcgen05 kernel when a.wimg is set and the shape is
 // covered, to the mma.sync kernel otherwise.

@@ -80,15 +80,22 @@ constexpr int kRing = 8;                 // TMEM accumulators (output rows in fl
 
 template <int CIN, int COUT>
 struct Tc {
-  static constexpr int KS = CIN / 16;                // K steps of 16 channels per tap
+  // 8 input channels: one K=16 MMA covers the tap pair (dx, dx+1) of a
+  // (dy, dz), the A operand's second K chunk being the next voxel (LBO 16 B);
+  // pairs (0, 1) and (2, 3), tap 3 with zero weights
+  static constexpr bool PAIRED = CIN == 8;
+  static constexpr int KS = PAIRED ? 1 : CIN / 16;   // K steps of 16 channels per tap
+  static constexpr int NMMA = PAIRED ? 6 : 9 * KS;   // MMAs per slab and dz group
   static constexpr int CH = CIN / 8;                 // 16-byte chunks per voxel
   static constexpr int SLAB = CH * kPlane;
-  static constexpr int WB = 27 * CIN * COUT * 2;     // weight image bytes
+  static constexpr int WB = NMMA * 2 * 3 * COUT * 16; // weight image bytes
   static constexpr int S0 = (kSmemBudget - WB) / SLAB;
   static constexpr int S = S0 > 6 ? 6 : S0;          // slab ring depth
   static constexpr int SMEM = WB + S * SLAB + 1024;  // + alignment slack
   static constexpr int TCOLS = kRing * COUT;         // TMEM columns: the accumulator ring
-  static_assert(S >= 3, "slab ring too shallow for this shape");
+  // S >= 2: a slab is freed as soon as its own MMAs complete, so the loader
+  // refills one slot while the MMAs read the other
+  static_assert(S >= 2, "slab ring too shallow for this shape");
   static_assert(WB % 128 == 0 && SLAB % 128 == 0, "128-byte aligned regions");
   static_assert(TCOLS >= 32 && TCOLS <= 512 && (TCOLS & (TCOLS - 1)) == 0, "TMEM allocation: power of 2 in [32, 512]");
   static_assert(3 * COUT <= 256 && COUT % 16 == 0, "MMA N = 3 COUT in [16, 256], multiple of 16");
@@ -308,6 +315,16 @@ __device__ __forceinline__ void load_slab(const TcArgs& a, const Unit& t, int z_
   }
 }
 
+// Descriptor offset (16-byte units) of the A window of MMA k of a slab: k =
+// (dy*3 + dx)*KS + ks, or for 8 channels k = dy*2 + q (taps dx = 2q, 2q+1).
+// The B image holds the matching weights at k * 2 * 3*COUT*16 bytes.
+template <bool PAIRED, int KS>
+__device__ __forceinline__ uint64_t a_off(int k) {
+  if (PAIRED) return (uint64_t)(((k >> 1) * kRowBytes + (k & 1) * 32) >> 4);
+  const int ks = k % KS, dx = (k / KS) % 3, dy = k / (3 * KS);
+  return (uint64_t)((2 * ks * kPlane + dy * kRowBytes + dx * 16) >> 4);
+}
+
 // TMEM accumulator of output row i (rows counted across the CTA's columns):
 // consecutive rows take descending slots, so rows z+1, z, z-1 sit in
 // ascending, mostly adjacent column blocks.
@@ -343,6 +360,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // the 32-byte pad after each chunk of a slab is never loaded; an 8-channel
+  // MMA reads it (times zero weights), so it must hold finite values
+  for (int q = threadIdx.x; q < S * P::CH * 2; q += blockDim.x)
+    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(ssm + (uint32_t)(q >> 1) * kPlane + kBoxBytes + (q & 1) * 16),
+                 "r"(0u)
+                 : "memory");
+  fence_proxy_async();
   if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                  "r"((uint32_t)P::TCOLS)
@@ -470,23 +494,21 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           const uint32_t id2 = idesc0 | ((uint32_t)(n2 * COUT >> 3) << 17);
           // descriptors are linear in the start address (14-bit field, smem
           // below 256 KB): per MMA only compile-time offsets are added
-          const uint64_t a_base = sdesc(ssm + (uint32_t)slot * P::SLAB, kPlane, 128);
+          const uint64_t a_base = sdesc(ssm + (uint32_t)slot * P::SLAB, P::PAIRED ? 16u : (uint32_t)kPlane, 128);
           const uint64_t b_base1 = sdesc(wsm + (uint32_t)dz_lo * kBlk, kLboB, 128);
           const uint64_t b_base2 = sdesc(wsm + (uint32_t)(dz_lo + n1) * kBlk, kLboB, 128);
           if (n2 == 0) {
 #pragma unroll
-            for (int k = 0; k < 9 * P::KS; ++k) {
-              const int ks = k % P::KS, dx = (k / P::KS) % 3, dy = k / (3 * P::KS);
-              const uint64_t ad = a_base + (uint64_t)((2 * ks * kPlane + dy * kRowBytes + dx * 16) >> 4);
-              const uint64_t bo = (uint64_t)((((dx + 3 * dy) * P::KS + ks) * 2 * kLboB) >> 4);
+            for (int k = 0; k < P::NMMA; ++k) {
+              const uint64_t ad = a_base + a_off<P::PAIRED, P::KS>(k);
+              const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
               mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
             }
           } else {
 #pragma unroll
-            for (int k = 0; k < 9 * P::KS; ++k) {
-              const int ks = k % P::KS, dx = (k / P::KS) % 3, dy = k / (3 * P::KS);
-              const uint64_t ad = a_base + (uint64_t)((2 * ks * kPlane + dy * kRowBytes + dx * 16) >> 4);
-              const uint64_t bo = (uint64_t)((((dx + 3 * dy) * P::KS + ks) * 2 * kLboB) >> 4);
+            for (int k = 0; k < P::NMMA; ++k) {
+              const uint64_t ad = a_base + a_off<P::PAIRED, P::KS>(k);
+              const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
               mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
               mma_bf16(d2, ad, b_base2 + bo, id2, 1u);
             }
@@ -572,13 +594,17 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
   }
 }
 
-// img[(((tap9*(CI/8) + kc)*3 + dz)*CO + n)*8 + e] = W(tap9 + 9dz, 8kc + e, n)
-// with tap9 = dx + 3dy: the three dz blocks of one (dx, dy, k chunk) are
-// adjacent, as the fused MMA's N dimension reads them.  The backward-data
-// weights of a layer are W'(t, k, n) = W[26-t][n][k].
+// img[(((k*2 + c)*3 + dz)*CO + n)*8 + e] for MMA k of a slab and its K
+// chunk c: for 16+ channels k = (dy*3 + dx)*KS + ks holds W(dx + 3dy + 9dz,
+// 16ks + 8c + e, n); for 8 channels k = dy*2 + q holds W(tap of dx = 2q + c,
+// e, n), zero for dx = 3.  The backward-data weights of a layer are
+// W'(t, k, n) = W[26-t][n][k].
 __global__ void image_kernel(int cin, int cout, const float* __restrict__ w, bf16* __restrict__ img, int backward) {
   const int ci2 = backward ? cout : cin, co2 = backward ? cin : cout;
-  const size_t total = (size_t)27 * ci2 * co2;
+  const bool paired = ci2 == 8;
+  const int ks_n = paired ? 1 : ci2 / 16;
+  const int nmma = paired ? 6 : 9 * ks_n;
+  const size_t total = (size_t)nmma * 2 * 3 * co2 * 8;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int e = (int)(i % 8);
     size_t r = i / 8;
@@ -586,10 +612,24 @@ __global__ void image_kernel(int cin, int cout, const float* __restrict__ w, bf1
     r /= co2;
     const int dz = (int)(r % 3);
     r /= 3;
-    const int kc = (int)(r % (ci2 / 8));
-    const int tap9 = (int)(r / (ci2 / 8));
-    const int k = 8 * kc + e, t = tap9 + 9 * dz;
-    const float v = backward ? w[((size_t)(26 - t) * cin + nn) * cout + k] : w[((size_t)t * cin + k) * cout + nn];
+    const int c = (int)(r % 2);
+    const int k = (int)(r / 2);
+    int dx, dy, ch;
+    if (paired) {
+      dy = k >> 1;
+      dx = 2 * (k & 1) + c;
+      ch = e;
+    } else {
+      const int ks = k % ks_n;
+      dx = (k / ks_n) % 3;
+      dy = k / (3 * ks_n);
+      ch = 16 * ks + 8 * c + e;
+    }
+    float v = 0.0f;
+    if (dx < 3) {
+      const int t = dx + 3 * dy + 9 * dz;
+      v = backward ? w[((size_t)(26 - t) * cin + nn) * cout + ch] : w[((size_t)t * cin + ch) * cout + nn];
+    }
     img[i] = __float2bfloat16(v);
   }
 }

@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TC_SHAPES = [(16, 16), (32, 32), (32, 16), (16, 32), (32, 64)]
+TC_SHAPES = [(8, 16), (16, 16), (32, 32), (32, 16), (16, 32), (32, 64), (64, 32)]
 
 
 def _ctx(n, box=1000.0, bmin=(500.0, 300.0, 200.0)):
@@ -134,14 +134,14 @@ def test_conv3_tcgen05_rejects_uncovered():
     x = torch.zeros((128, 128, 128, 64), dtype=torch.bfloat16, device="cuda")
     w = torch.zeros((27, 64, 64), device="cuda")
     with pytest.raises(_lib.BaorecError):
-        guess.conv3(ctx, x, w, path="tcgen05")       # 64 input channels: mma.sync only
+        guess.conv3(ctx, x, w, path="tcgen05")       # 64 -> 64 channels: mma.sync only
 
 
 def test_network_tcgen05_matches_mma_forward_and_gradients():
     """The whole network at n = 256 with the trained weights: output and
     parameter gradients with the tcgen05 layers on and off agree to the BF16
-    noise of the activations; the forward ran the six covered layers (three
-    at 256^3, three at 128^3) on tcgen05."""
+    noise of the activations; the forward ran the eight covered layers (four
+    at 256^3, four at 128^3) on tcgen05."""
     import torch
     from baorec import guess
     n = 256
@@ -161,7 +161,7 @@ def test_network_tcgen05_matches_mma_forward_and_gradients():
         res[tc] = (out.cpu().numpy(), grads, lval.value, guess.tc_layers(ctx))
     o1, g1, l1, k1 = res[True]
     o0, g0, l0, k0 = res[False]
-    assert k1 == 6 and k0 == 0, (k1, k0)
+    assert k1 == 8 and k0 == 0, (k1, k0)
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     assert rel(o1, o0) < 1e-2, rel(o1, o0)
     assert abs(l1 - l0) / l0 < 1e-3
