@@ -142,6 +142,8 @@ _SIGS = {
     "baorec_guess_set_conv_path": (C.c_int, [P, C.c_int32]),
     "baorec_guess_tc_layers": (C.c_int32, [P]),
     "baorec_guess_conv3": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, C.c_int32, C.c_int32]),
+    "baorec_guess_profile_conv": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                            C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_read_cic": (C.c_int, [P, P, P, P, P, I64, P, U32]),
     "baorec_read_shifts": (C.c_int, [P, P, P, P, I64, C.c_int, P, P, P, U32]),
     "baorec_reconstructed_positions": (C.c_int, [P, P, P, P, I64, C.c_int, P, P, P, U32]),

@@ -950,3 +950,67 @@ extern "C" int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, in
   cudaFree(img);
   return rc;
 }
+
+extern "C" int baorec_guess_profile_conv(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, int32_t path,
+                                         int32_t reps, float* avg_ms, double* flops) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (n < 1 || reps < 1 || path < 0 || path > 2 || !avg_ms || !flops)
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_profile_conv: bad arguments");
+  if (path >= 1 && !guess::tc_supported(C3, cin, cout, n))
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_profile_conv: no tcgen05 kernel for %d -> %d at n = %d", cin, cout, n);
+  const size_t nv = (size_t)n * n * n;
+  bf16 *x = nullptr, *y = nullptr, *img = nullptr;
+  float *w = nullptr, *b = nullptr;
+  uint2* frag = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = BAOREC_OK;
+  cudaError_t e = cudaMalloc(&x, nv * cin * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&y, nv * cout * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&w, (size_t)27 * cin * cout * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&b, (size_t)cout * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&frag, guess::frag_count(C3, cin, cout) * sizeof(uint2));
+  if (e == cudaSuccess && path >= 1) e = cudaMalloc(&img, guess::image_count(cin, cout) * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(x, 0x3c, nv * cin * sizeof(bf16), ctx->stream);   // finite BF16 values
+  if (e == cudaSuccess) e = cudaMemsetAsync(w, 0, (size_t)27 * cin * cout * sizeof(float), ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b, 0, (size_t)cout * sizeof(float), ctx->stream);
+  if (e == cudaSuccess) e = guess::weight_frags(ctx->stream, C3, cin, cout, w, frag, false);
+  if (e == cudaSuccess && img) e = guess::weight_image(ctx->stream, cin, cout, w, img, false);
+  guess::ConvArgs a;
+  a.in = x;
+  a.in_cs = cin;
+  a.out = y;
+  a.out_cs = cout;
+  a.add = nullptr;
+  a.add_cs = 0;
+  a.w = frag;
+  a.bias = b;
+  a.relu = 1;
+  a.n_in = a.n_out = n;
+  a.wimg = img;
+  a.err = ctx->derr;
+  a.tc_loader = path == 2 ? 1 : 0;
+  if (e == cudaSuccess) e = guess::conv_forward(ctx->stream, C3, cin, cout, a);   // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) e = guess::conv_forward(ctx->stream, C3, cin, cout, a);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  ctx->launches += reps + 1;
+  if (e != cudaSuccess) rc = set_error(ctx, BAOREC_ERR_CUDA, "guess_profile_conv: %s", cudaGetErrorString(e));
+  else rc = finish(ctx, 0);
+  *avg_ms = ms / (float)reps;
+  *flops = 2.0 * 27.0 * cin * cout * (double)nv;
+  cudaStreamSynchronize(ctx->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(w);
+  cudaFree(b);
+  cudaFree(frag);
+  cudaFree(img);
+  return rc;
+}

@@ -33,6 +33,7 @@ sys.path.insert(0, os.path.join(ROOT, "baorec.jl_gb300"))
 METRIC = "recons/s at 1e-6 residual, learned-start MG vs plain MG, 256^3, one GB300"
 UNIT = "recons/s"
 FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
 
 
 def parse():
@@ -51,6 +52,9 @@ def parse():
     ap.add_argument("--only-start", action="store_true", help="time only the --start solve (no other starts)")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel roofline and paint timings")
     ap.add_argument("--batch-mocks", type=int, default=64)
+    ap.add_argument("--conv-only", action="store_true",
+                    help="only time the learned guess's tensor-core convolutions, every shape on a --mesh grid "
+                         "(a small case for profilers)")
     ap.add_argument("--start", default="spectral", choices=["zero", "spectral", "learned"],
                     help="start of the headline solve: zero (plain multigrid), spectral (FFT-preconditioned "
                          "corrections, V-cycles if they stall) or learned (CNN guess, then as spectral); "
@@ -126,6 +130,41 @@ def measured_peak():
             return float(json.load(fh)["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def measured_peak_tensor():
+    """Dense BF16 tensor peak (TFLOP/s, burst: the convolution is timed alone)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured"
+    except Exception:
+        return FALLBACK_BF16_TFLOPS, "fallback"
+
+
+GUESS_CONV_SHAPES = ((8, 16, 256), (16, 16, 256), (32, 16, 256), (32, 32, 128), (64, 32, 128))
+
+
+def guess_conv_rooflines(ctx, C, shapes=GUESS_CONV_SHAPES):
+    """Tensor-core roofline of the learned guess's 3x3x3 convolutions: each
+    tcgen05 shape of the network at its grid (256^3 level 0, 128^3 level 1)
+    timed alone with CUDA events, beside the mma.sync kernel of the same shape."""
+    peak, src = measured_peak_tensor()
+    out = {}
+    for cin, cout, n in shapes:
+        row = {}
+        for path, label in ((1, "tcgen05"), (0, "mma.sync")):
+            avg, fl = C.c_float(), C.c_double()
+            ctx.call("baorec_guess_profile_conv", cin, cout, n, path, 10, C.byref(avg), C.byref(fl))
+            tf = fl.value / (avg.value * 1e-3) / 1e12
+            row[label] = {"avg_launch_ms": avg.value, "achieved": tf}
+        tc = row["tcgen05"]
+        out[f"guess conv3 {cin}->{cout} at {n}^3"] = {
+            "kernel": "conv_tc_kernel (tcgen05.mma, TMA slabs, TMEM accumulators)", "bound": "tensor",
+            "achieved": tc["achieved"], "peak": peak, "unit": "TFLOP/s", "frac": tc["achieved"] / peak,
+            "peak_source": src, "algorithmic_flops_per_launch": 2.0 * 27 * cin * cout * n ** 3,
+            "avg_launch_ms": tc["avg_launch_ms"], "mma_sync": row["mma.sync"]}
+    return out
 
 
 def workload(args, seed):
@@ -280,12 +319,31 @@ def run_reference(args):
     return 0
 
 
+def run_conv_only(args):
+    """The network's convolutions alone on a --mesh grid (one JSON line)."""
+    import ctypes as C
+    import torch
+    from baorec import _lib
+    cfg = _lib.default_config()
+    cfg.method = _lib.MULTIGRID
+    for a in range(3):
+        cfg.n[a] = args.mesh
+        cfg.box_size[a] = 1000.0
+    ctx = _lib.Context(cfg)
+    torch.cuda.synchronize()
+    rows = guess_conv_rooflines(ctx, C, tuple((ci, co, args.mesh) for ci, co, _ in GUESS_CONV_SHAPES))
+    print(json.dumps({"metric": "guess convolution TFLOP/s", "mesh": args.mesh, "kernels": rows}), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import numpy as np
     import torch
     import ctypes as C
     import baorec
     from baorec import _lib
+    if args.conv_only:
+        return run_conv_only(args)
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -440,6 +498,9 @@ def run_gb300(args):
                       "achieved": pbytes / (pms * 1e-3) / 1e9, "unit": "GB/s", "peak": peak,
                       "frac": pbytes / (pms * 1e-3) / 1e9 / peak}
     del scratch
+
+    if not args.no_kernels and args.mesh % 128 == 0:
+        aux.update(guess_conv_rooflines(ctx, C))
 
     batch = None if args.no_batch else run_batch(args, torch, np)
 

@@ -341,6 +341,11 @@ int32_t baorec_guess_tc_layers(baorec_ctx* ctx);
  * (BAOREC_ERR_ARG for 1 and 2 if the shape or n has none). */
 int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, const void* x, const float* w,
                        const float* bias, const void* add, void* y, int32_t relu, int32_t path);
+/* Average device time (CUDA events on the context's stream) of `reps`
+ * launches of one network convolution cin -> cout on an n^3 grid (path as in
+ * baorec_guess_conv3) and its algorithmic FLOPs, 2 * 27 * cin * cout * n^3. */
+int baorec_guess_profile_conv(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, int32_t path, int32_t reps,
+                              float* avg_ms, double* flops);
 
 /* ---- Batched box reconstructions in one CUDA graph (no reference counterpart) ----
  * Each item is one periodic-box mock (device arrays; positions in [0, box),
