@@ -139,6 +139,7 @@ _SIGS = {
     "baorec_guess_apply": (C.c_int, [P, P, P]),
     "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
     "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),
+    "baorec_set_gradient": (C.c_int, [P, C.c_int32]),
     "baorec_guess_set_conv_path": (C.c_int, [P, C.c_int32]),
     "baorec_guess_tc_layers": (C.c_int32, [P]),
     "baorec_guess_conv3": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, C.c_int32, C.c_int32]),

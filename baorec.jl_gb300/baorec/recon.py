@@ -92,6 +92,7 @@ class MultigridRecon:
     start: str = "zero"                  # convergent mode: "zero" | "spectral" | "learned"
     start_rate: float = 0.5
     guess_params: object = None          # learned start: network parameters (baorec.guess)
+    gradient: str = "fft"                # displacement from φ: "fft" (reference) | "fd" (central differences)
     solve_stats: dict = dc_field(default_factory=dict)
 
     def __post_init__(self):
@@ -101,6 +102,8 @@ class MultigridRecon:
             raise ValueError(f"start must be one of {sorted(_STARTS)}, got {self.start!r}")
         if self.start == "learned" and self.guess_params is None:
             raise ValueError("start='learned' needs guess_params (see baorec.guess)")
+        if self.gradient not in ("fft", "fd"):
+            raise ValueError(f"gradient must be 'fft' or 'fd', got {self.gradient!r}")
 
 
 # ----------------------------------------------------------------------------
@@ -292,6 +295,8 @@ def _ctx(recon, shape, ran_min=0.01) -> _lib.Context:
         bs, bm = ctx.box()
         if list(bs) != [float(F32(v)) for v in recon.box_size] or list(bm) != [float(F32(v)) for v in recon.box_min]:
             ctx.set_box(recon.box_size, recon.box_min)
+    if isinstance(recon, MultigridRecon):
+        ctx.call("baorec_set_gradient", 1 if recon.gradient == "fd" else 0)
     return ctx
 
 

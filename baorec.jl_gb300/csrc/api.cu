@@ -617,6 +617,19 @@ static int ensure_psi(baorec_ctx* ctx) {
   return BAOREC_OK;
 }
 
+extern "C" int baorec_set_gradient(baorec_ctx* ctx, int32_t mode) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (mode != BAOREC_GRADIENT_FFT && mode != BAOREC_GRADIENT_FD)
+    return set_error(ctx, BAOREC_ERR_ARG, "set_gradient: mode must be BAOREC_GRADIENT_FFT or BAOREC_GRADIENT_FD");
+  if (mode == BAOREC_GRADIENT_FD && ctx->cfg.method != BAOREC_MULTIGRID)
+    return set_error(ctx, BAOREC_ERR_ARG, "set_gradient: the finite-difference gradient is for multigrid contexts");
+  if (mode != ctx->grad_mode) {
+    ctx->grad_mode = mode;
+    ctx->psi_valid = false;
+  }
+  return BAOREC_OK;
+}
+
 extern "C" int baorec_displacement_meshes(baorec_ctx* ctx, float* px, float* py, float* pz) {
   if (!ctx || !px || !py || !pz) return set_error(ctx, BAOREC_ERR_ARG, "displacement_meshes: missing output");
   CKS(ensure_psi(ctx));

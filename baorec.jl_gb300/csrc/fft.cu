@@ -389,9 +389,42 @@ __global__ void interleave3_kernel(const float* __restrict__ p, float4* __restri
     out[e] = make_float4(p[e], p[e + N], p[e + 2 * N], 0.0f);
 }
 
-// Ψ (iterative: i k δ_k / k²; multigrid: i k φ_k) as an interleaved mesh at
-// psi4[0, 4N); psi4[4N, 7N) holds the three planes on the way.
+// Finite-difference gradient of φ (the reference's read_grad_cic,
+// src/mas.jl:388-466, as a mesh): Ψ_a = (φ[c + e_a] - φ[c - e_a]) / cell2_a
+// with periodic neighbours and cell2_a = T(2 L_a) / n_a as the reference
+// spells it.  CIC-reading this mesh at a particle gives the reference's
+// weighted sum of node differences divided by cell2 (up to FP32 rounding
+// order).  One pass: read φ (neighbours from L1/L2), write 16 B per cell.
+__global__ void fd_grad_kernel(const float* __restrict__ phi, float4* __restrict__ out, int n1, int n2, int n3,
+                               float c2x, float c2y, float c2z) {
+  const size_t N = (size_t)n1 * n2 * n3;
+  const size_t plane = (size_t)n1 * n2;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n1);
+    const size_t r = e / n1;
+    const int j = (int)(r % n2), k = (int)(r / n2);
+    const size_t xp = i + 1 < n1 ? e + 1 : e + 1 - n1, xm = i > 0 ? e - 1 : e + n1 - 1;
+    const size_t yp = j + 1 < n2 ? e + n1 : e + n1 - plane, ym = j > 0 ? e - n1 : e + plane - n1;
+    const size_t zp = k + 1 < n3 ? e + plane : e + plane - N, zm = k > 0 ? e - plane : e + N - plane;
+    out[e] = make_float4(__fdiv_rn(__fsub_rn(__ldg(phi + xp), __ldg(phi + xm)), c2x),
+                         __fdiv_rn(__fsub_rn(__ldg(phi + yp), __ldg(phi + ym)), c2y),
+                         __fdiv_rn(__fsub_rn(__ldg(phi + zp), __ldg(phi + zm)), c2z), 0.0f);
+  }
+}
+
+// Ψ (iterative: i k δ_k / k²; multigrid: i k φ_k, or its finite-difference
+// form) as an interleaved mesh at psi4[0, 4N); psi4[4N, 7N) holds the three
+// planes on the way.
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
+  if (ctx->cfg.method == BAOREC_MULTIGRID && ctx->grad_mode == BAOREC_GRADIENT_FD) {
+    const int n[3] = {ctx->n1, ctx->n2, ctx->n3};
+    float c2[3];
+    for (int a = 0; a < 3; ++a) c2[a] = (2.0f * ctx->cfg.box_size[a]) / (float)n[a];   // FP32, as T(2L)/n
+    fd_grad_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(field, reinterpret_cast<float4*>(psi4), n[0], n[1], n[2],
+                                                         c2[0], c2[1], c2[2]);
+    CKLAUNCH();
+    return BAOREC_OK;
+  }
   KGeom g = kgeom_of(ctx);
   // cuFFT's R2C reads but does not modify its input
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));

@@ -270,6 +270,17 @@ int baorec_set_result(baorec_ctx* ctx, const float* in, uint32_t flags);
  * device outputs. */
 int baorec_displacement_meshes(baorec_ctx* ctx, float* psi_x, float* psi_y, float* psi_z);
 
+/* Gradient of the multigrid potential for the displacements and shifts:
+ * BAOREC_GRADIENT_FFT (default, compute_displacements of
+ * src/multigrid.jl:755-773) or BAOREC_GRADIENT_FD, the periodic
+ * central-difference gradient that read_grad_cic (src/mas.jl:388-466, not
+ * wired into the reference) interpolates: one stencil pass instead of one R2C
+ * and three C2R transforms; the results differ from the FFT gradient by the
+ * discretisation error.  Multigrid contexts only. */
+#define BAOREC_GRADIENT_FFT 0
+#define BAOREC_GRADIENT_FD  1
+int baorec_set_gradient(baorec_ctx* ctx, int32_t mode);
+
 /* read_cic! (src/mas.jl:218-269): trilinear read of a device mesh at n
  * particles (wrap = true as the reference's callers use). */
 int baorec_read_cic(baorec_ctx* ctx, const float* mesh, const float* x, const float* y,

@@ -344,6 +344,54 @@ def read_cic(field, x, y, z, box_size, box_min, wrap=True):
     return acc.astype(T)
 
 
+def fd_gradient_mesh(phi, box_size):
+    """Periodic central-difference gradient mesh of the finite-difference
+    read-out: component a is ``(φ[c + e_a] - φ[c - e_a]) / cell2_a`` with
+    ``cell2_a = T(2 L_a) / n_a`` as ``src/mas.jl:390`` spells the doubled cell
+    (``cell = 2 * box_size / dims``); evaluated in T, so an FP32 mesh is
+    bit-exact with the device's."""
+    T = phi.dtype.type
+    out = []
+    for a in range(3):
+        c2 = T(T(T(2) * T(box_size[a])) / T(phi.shape[a]))
+        diff = (np.roll(phi, -1, axis=a) - np.roll(phi, 1, axis=a)).astype(T)
+        out.append((diff / c2).astype(T))
+    return tuple(out)
+
+
+def read_grad_cic(field, x, y, z, box_size, box_min):
+    """The finite-difference read-out ``read_grad_cic`` of ``src/mas.jl:388-466``
+    (commented out in the reference; pyrecon's finite-difference read-out) in
+    FP64: for each particle, the CIC-weighted sum over its 8 surrounding nodes
+    of the node's central differences ``φ[n + e_a] - φ[n - e_a]`` (periodic),
+    divided by ``2 L_a / n_a``.  The particle's grid coordinate uses the cell
+    ``L / n``: the commented-out code divides the position by the doubled cell
+    as well, which places a particle at half its grid coordinate; pyrecon and
+    this restatement do not."""
+    f = np.asarray(field, dtype=np.float64)
+    n = f.shape
+    base, frac = [], []
+    for a, p in enumerate((x, y, z)):
+        d = (np.asarray(p, dtype=np.float64) - float(box_min[a])) / (float(box_size[a]) / n[a])
+        i = np.floor(d).astype(np.int64)
+        base.append(i)
+        frac.append(d - i)
+    out = [np.zeros(len(base[0])) for _ in range(3)]
+    for cx in (0, 1):
+        for cy in (0, 1):
+            for cz in (0, 1):
+                w = ((frac[0] if cx else 1 - frac[0]) * (frac[1] if cy else 1 - frac[1])
+                     * (frac[2] if cz else 1 - frac[2]))
+                node = [(base[0] + cx) % n[0], (base[1] + cy) % n[1], (base[2] + cz) % n[2]]
+                for a in range(3):
+                    up = list(node)
+                    dn = list(node)
+                    up[a] = (node[a] + 1) % n[a]
+                    dn[a] = (node[a] - 1) % n[a]
+                    out[a] += w * (f[tuple(up)] - f[tuple(dn)])
+    return tuple(out[a] / (2.0 * float(box_size[a]) / n[a]) for a in range(3))
+
+
 # ----------------------------------------------------------------------------
 # Overdensity — src/recon.jl:42-91
 # ----------------------------------------------------------------------------
