@@ -11,7 +11,8 @@ from .recon import __all__ as _recon_all
 from . import mocks  # noqa: F401
 from . import guess  # noqa: F401
 from . import cosmo  # noqa: F401
+from . import power  # noqa: F401
 from .batch import Batch  # noqa: F401
 from ._lib import load as load_library, lib_path  # noqa: F401
 
-__all__ = list(_recon_all) + ["mocks", "guess", "cosmo", "Batch", "load_library", "lib_path"]
+__all__ = list(_recon_all) + ["mocks", "guess", "cosmo", "power", "Batch", "load_library", "lib_path"]

@@ -57,6 +57,14 @@ class GuessTrainConfig(C.Structure):
                 ("rtol", C.c_float), ("loss", C.c_int32)]
 
 
+class PowerConfig(C.Structure):
+    _fields_ = [("geometry", C.c_int32), ("mas", C.c_int32), ("interlace", C.c_int32), ("nbins", C.c_int32),
+                ("kmin", C.c_float), ("dk", C.c_float), ("los", C.c_float * 3), ("reserved", C.c_int32)]
+
+
+POWER_BOX, POWER_SURVEY = 0, 1
+
+
 class BatchItem(C.Structure):
     _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("w", C.c_void_p), ("n", C.c_int64),
                 ("mesh", C.c_int32), ("box_size", C.c_float), ("mas", C.c_int32), ("smoothing_radius", C.c_float),
@@ -140,6 +148,8 @@ _SIGS = {
     "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
     "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),
     "baorec_set_gradient": (C.c_int, [P, C.c_int32]),
+    "baorec_power_multipoles": (C.c_int, [P, C.POINTER(PowerConfig), P, P, P, P, I64, P, P, P, P, P, I64,
+                                          P, P, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32]),
     "baorec_guess_set_conv_path": (C.c_int, [P, C.c_int32]),
     "baorec_guess_tc_layers": (C.c_int32, [P]),
     "baorec_guess_conv3": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, C.c_int32, C.c_int32]),

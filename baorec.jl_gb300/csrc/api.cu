@@ -245,7 +245,9 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   cudaFree(ctx->derr);
   cudaFreeHost(ctx->herr);
   for (auto& b : ctx->stage) cudaFree(b.p);
-  for (DevBuf* b : {&ctx->sort_keys, &ctx->sort_perm, &ctx->sort_tiles, &ctx->fix_mesh}) cudaFree(b->p);
+  for (DevBuf* b : {&ctx->sort_keys, &ctx->sort_perm, &ctx->sort_tiles, &ctx->fix_mesh, &ctx->pw_mesh, &ctx->pw_spec,
+                    &ctx->pw_part, &ctx->pw_nz})
+    cudaFree(b->p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return BAOREC_OK;

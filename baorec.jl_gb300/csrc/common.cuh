@@ -84,6 +84,7 @@ struct baorec_ctx {
   baorec::GuessNet* net = nullptr;     // learned initial guess (weights, workspace)
   // deterministic paint scratch: tile keys, permutation, tile counts/offsets, fixed-point mesh
   baorec::DevBuf sort_keys, sort_perm, sort_tiles, fix_mesh;
+  baorec::DevBuf pw_mesh, pw_spec, pw_part, pw_nz;   // power-spectrum scratch (power.cu)
   struct Tune {                        // launch shapes (defaults, or chosen by baorec_autotune)
     int paint_tile = 8;                // tile edge of the deterministic paint
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming

@@ -296,6 +296,51 @@ int baorec_reconstructed_positions(baorec_ctx* ctx, const float* x, const float*
                                    const float* z, int64_t n, int field,
                                    float* ox, float* oy, float* oz, uint32_t flags);
 
+/* ---- Power-spectrum multipoles (the science check of the reference's test
+ * helpers, which call the external pypowspec: compute_auto_box,
+ * compute_auto_box_rand, compute_auto_lc in test_helpers/simulation.py:40-55
+ * and test_helpers/lightcone.py:48-75) ------------------------------------
+ * On this context's mesh and box.  The catalogs are painted (CIC or TSC,
+ * nodes at box_min + i L/n, periodic) into F = Σ w_d - α Σ w_r with
+ * α = Σw_d / Σw_r (F = Σ w_d without randoms), transformed, compensated for
+ * the assignment window Π sinc(k_a Δ_a / 2)^p and binned in |k| shells
+ * [kmin + b dk, kmin + (b+1) dk).
+ *   BAOREC_POWER_BOX     periodic box, fixed unit line of sight `los`;
+ *                        P(k, μ) = |F_k|² / I - shot, I = (Σw_d)² / V,
+ *                        shot = (Σw_d² + α² Σw_r²) / I; optional interlacing
+ *                        (a second paint shifted by half a cell).
+ *   BAOREC_POWER_SURVEY  local line of sight from the origin (Yamamoto
+ *                        estimator through FFTs: A_0 = FFT[F],
+ *                        A_2 = k̂_i k̂_j FFT[r̂_i r̂_j F],
+ *                        A_4 = k̂_i k̂_j k̂_k k̂_l FFT[r̂_i r̂_j r̂_k r̂_l F] with r̂
+ *                        at the mesh nodes); P_0 = <|A_0|²>/I - shot,
+ *                        P_2 = 5/2 <Re A_0 (3 A_2 - A_0)*>/I,
+ *                        P_4 = 9/8 <Re A_0 (35 A_4 - 30 A_2 + 3 A_0)*>/I with
+ *                        I = α Σ_r n(z)_r w_r² from the randoms' n(z) (rnz);
+ *                        weights are the total (e.g. FKP) weights.
+ * Outputs (host, nbins each): mean |k| of the modes in the bin, P_0, P_2,
+ * P_4 and the mode count; *shot and *norm get the shot noise and I.  Shot
+ * noise is subtracted from P_0 only.  Particles outside the box are an error
+ * for the survey geometry (BAOREC_ERR_OOB) and wrap for the box. */
+#define BAOREC_POWER_BOX    0
+#define BAOREC_POWER_SURVEY 1
+typedef struct {
+  int32_t geometry;          /* BAOREC_POWER_BOX | BAOREC_POWER_SURVEY */
+  int32_t mas;               /* BAOREC_MAS_CIC | BAOREC_MAS_TSC */
+  int32_t interlace;         /* 0 | 1 (box geometry) */
+  int32_t nbins;
+  float kmin, dk;            /* h/Mpc */
+  float los[3];              /* box geometry: line of sight (normalised internally) */
+  int32_t reserved;
+} baorec_power_config;
+
+int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_config* pc,
+                            const float* x, const float* y, const float* z, const float* w, int64_t n,
+                            const float* rx, const float* ry, const float* rz, const float* rw,
+                            const float* rnz, int64_t nr,
+                            double* k_mean, double* p0, double* p2, double* p4, int64_t* nmodes,
+                            double* shot, double* norm, uint32_t flags);
+
 /* ---- Learned initial guess (no reference counterpart) ----------------------
  * A 3-level 3-D U-Net (16/32/64 channels, BF16 weights and activations, FP32
  * accumulation) predicts the error of the FFT start of the residual-driven
