@@ -12,7 +12,8 @@ from . import mocks  # noqa: F401
 from . import guess  # noqa: F401
 from . import cosmo  # noqa: F401
 from . import power  # noqa: F401
+from . import catalog  # noqa: F401
 from .batch import Batch  # noqa: F401
 from ._lib import load as load_library, lib_path  # noqa: F401
 
-__all__ = list(_recon_all) + ["mocks", "guess", "cosmo", "power", "Batch", "load_library", "lib_path"]
+__all__ = list(_recon_all) + ["mocks", "guess", "cosmo", "power", "catalog", "Batch", "load_library", "lib_path"]

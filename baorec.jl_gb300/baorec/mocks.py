@@ -45,7 +45,7 @@ def lognormal_field(n, L, bias=2.0, seed=0, amp=2.0e4):
     vol = L ** 3
     cellv = vol / n ** 3
     # ξ on the grid: ξ(r) = (1/V) Σ_k P(k) e^{ikr}
-    xi = np.fft.irfftn(pk / vol, s=(n, n, n)) * n ** 3
+    xi = np.fft.irfftn(pk / vol, s=(n, n, n), axes=(0, 1, 2)) * n ** 3
     xig = np.log1p(np.clip(xi, -0.99, None))
     pg = np.fft.rfftn(xig).real * vol / n ** 3
     pg = np.clip(pg, 0.0, None)
@@ -54,7 +54,7 @@ def lognormal_field(n, L, bias=2.0, seed=0, amp=2.0e4):
     white = rng.standard_normal((n, n, n))
     wk = np.fft.rfftn(white)
     gk = wk * np.sqrt(pg / cellv)
-    g = np.fft.irfftn(gk, s=(n, n, n))
+    g = np.fft.irfftn(gk, s=(n, n, n), axes=(0, 1, 2))
     sig2 = g.var()
     delta = np.exp(g - sig2 / 2.0) - 1.0
     return delta  # indexed [a,b,c] with the last axis halved in k; isotropic, so axis order is immaterial

@@ -156,6 +156,15 @@ static_assert(sizeof(baorec_solve_stats) == 32, "baorec_solve_stats layout is pa
 
 static thread_local char g_create_msg[512];
 
+// error of a call made without a context (baorec_last_error(NULL) reads it)
+int baorec::set_error_noctx(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_create_msg, sizeof(g_create_msg), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
 extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
   if (!cfg || !out) return BAOREC_ERR_ARG;
   *out = nullptr;

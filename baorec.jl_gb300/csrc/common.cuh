@@ -109,6 +109,7 @@ struct baorec_ctx {
 namespace baorec {
 
 int set_error(baorec_ctx* c, int code, const char* fmt, ...);
+int set_error_noctx(int code, const char* fmt, ...);
 int cuda_fail(baorec_ctx* c, cudaError_t e, const char* what);
 int cufft_fail(baorec_ctx* c, cufftResult e, const char* what);
 int ensure(baorec_ctx* c, DevBuf& b, size_t bytes);

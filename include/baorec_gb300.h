@@ -296,6 +296,28 @@ int baorec_reconstructed_positions(baorec_ctx* ctx, const float* x, const float*
                                    const float* z, int64_t n, int field,
                                    float* ox, float* oy, float* oz, uint32_t flags);
 
+/* ---- Catalog I/O (examples/lightcone.jl:22-23, examples/simulation.jl:13
+ * read catalogs with CSV.jl; examples/simulation.jl:38-40 write the shifted
+ * positions with npzwrite) ----------------------------------------------
+ * Both work without a context (ctx NULL; baorec_last_error(NULL) holds the
+ * message) for host arrays; device arrays need one.
+ *
+ * baorec_read_ascii: whitespace-delimited numbers, one row per line; the
+ * first `skip` lines are dropped, then blank lines and lines whose first
+ * non-blank character is `comment` (0: none).  Columns `cols` (0-based) of
+ * every row go to out[0..ncols) as FP32, correctly rounded (strtof in the C
+ * locale).  With out NULL only *n_rows is set (the row count); with out, the
+ * columns need room for n_max rows (BAOREC_ERR_TOO_LARGE otherwise).  A row
+ * with too few fields or a field that is not a number is BAOREC_ERR_ARG,
+ * with the file line in the message. */
+int baorec_read_ascii(baorec_ctx* ctx, const char* path, const int32_t* cols, int32_t ncols, int32_t skip,
+                      int32_t comment, float** out, int64_t n_max, int64_t* n_rows, uint32_t flags);
+/* baorec_write_npy: an (n, ncols) float32 .npy file with fortran_order True
+ * (columns stored one after the other, as npzwrite writes hcat(x, y, z));
+ * cols on the device unless BAOREC_HOST. */
+int baorec_write_npy(baorec_ctx* ctx, const char* path, const float* const* cols, int32_t ncols, int64_t n,
+                     uint32_t flags);
+
 /* ---- Power-spectrum multipoles (the science check of the reference's test
  * helpers, which call the external pypowspec: compute_auto_box,
  * compute_auto_box_rand, compute_auto_lc in test_helpers/simulation.py:40-55
