@@ -257,6 +257,7 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   for (DevBuf* b : {&ctx->sort_keys, &ctx->sort_perm, &ctx->sort_tiles, &ctx->fix_mesh, &ctx->pw_mesh, &ctx->pw_spec,
                     &ctx->pw_part, &ctx->pw_nz})
     cudaFree(b->p);
+  if (ctx->ev_red) cudaEventDestroy(ctx->ev_red);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return BAOREC_OK;

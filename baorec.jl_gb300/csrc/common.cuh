@@ -68,6 +68,7 @@ struct baorec_ctx {
   bool has_result = false;
   float* psi = nullptr;                // 6 real meshes (displacements / iterative parts)
   bool psi_valid = false;              // psi[0..2] hold the displacement of `result`
+  cudaEvent_t ev_red = nullptr;          // the solve's partial sums have reached the host
   int grad_mode = BAOREC_GRADIENT_FFT;  // multigrid displacement: spectral or finite-difference gradient
   cufftComplex* ck = nullptr;          // complex work: 6 spectra
   float* xvec[3] = {nullptr, nullptr, nullptr};   // x_vec of the mesh (device)

@@ -779,7 +779,24 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       CKLAUNCH();
     }
     CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    // While the host reads the partial sums, the GPU already computes the
+    // first FFT correction of the next outer step, d_0 = S⁻¹ r, which needs
+    // nothing the host decides (it writes only the correction lev[0].v; a
+    // V-cycle zeroes that first).  Skipped when the last step's rate says
+    // this residual is already below rtol.
+    bool speculative = false;
+    if (spectral && nspec < ctx->cfg.max_cycles) {
+      const double predicted = m_last > 0 ? rho_prev * pow(std::max(rate, 0.0), (double)m_last) : 1.0;
+      speculative = !(m_last > 0 && rate > 0.0 && predicted <= (double)ctx->cfg.rtol);
+    }
+    if (speculative) {
+      if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
+      CK(cudaEventRecord(ctx->ev_red, ctx->stream));
+      CKS(spectral_correction(ctx, L0.f, L0.v));
+      CK(cudaEventSynchronize(ctx->ev_red));
+    } else {
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
     double s1 = 0.0, s2 = 0.0;
     for (int q = 0; q < nparts; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
     double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;
@@ -821,7 +838,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       float* rin = L0.f;
       float* rout = L0.r + N;
       float* d = L0.r;
-      CKS(spectral_correction(ctx, rin, L0.v));
+      if (!speculative) CKS(spectral_correction(ctx, rin, L0.v));
       for (int q = 1; q < m; ++q) {
         const float* dprev = q == 1 ? L0.v : d;
         float* acc = q == 1 ? nullptr : L0.v;

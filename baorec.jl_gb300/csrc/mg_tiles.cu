@@ -23,6 +23,26 @@ constexpr int TX = 32, XH = 4, WX = TX + 2 * XH;   // tile width, x-halo, window
 constexpr int NT = 512, NWARP = NT / 32;           // threads per block
 constexpr int CH = WX / 4;                         // 16-byte chunks per window row
 
+// The right-hand side of a warp's output rows (row = warp + i NWARP, interior
+// cells, no wrap) is read through a ring of PF registers filled PF rows
+// ahead, so those loads overlap the window loads and the stencil work
+// instead of stalling the row that consumes them.
+template <int TY, int TZ>
+struct RowPrefetch {
+  static constexpr int RPW = (TY * TZ + NWARP - 1) / NWARP;   // rows per warp
+  static constexpr int PF = RPW < 4 ? RPW : 4;
+  float v[PF];
+  __device__ __forceinline__ static int offset(int i, int warp, int lane, int x0, int y0, int z0, const int* n) {
+    const int row = warp + i * NWARP;
+    const int ly = row % TY, lz = row / TY;
+    return ((z0 + lz) * n[1] + (y0 + ly)) * n[0] + x0 + lane;
+  }
+  __device__ __forceinline__ void issue(int i, const float* __restrict__ src, int warp, int lane, int x0, int y0,
+                                        int z0, const int* n) {
+    if (i < RPW && warp + i * NWARP < TY * TZ) v[i % PF] = __ldg(src + offset(i, warp, lane, x0, y0, z0, n));
+  }
+};
+
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 // Row offsets (ix = 0 of the row) of the periodic window rows
@@ -139,6 +159,14 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
   int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);
   float* sp = reinterpret_cast<float*>(ro + SY * SZ);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  using RP = RowPrefetch<TY, TZ>;
+  RP pr, pa;
+#pragma unroll
+  for (int i = 0; i < RP::PF; ++i) {
+    pr.issue(i, rhs, warp, lane, x0, y0, z0, G.n);
+    if (acc) pa.issue(i, acc, warp, lane, x0, y0, z0, G.n);
+  }
   row_table<1, TY, TZ>(ro, y0, z0, G.n);
   if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
   __syncthreads();
@@ -146,17 +174,23 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
   Cf cu;
   if (!LOCAL) cu = coef_fast<false, false>(G.pg[0], G.pg[1], G.pg[2], G);
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int row = warp; row < TY * TZ; row += NWARP) {
+#pragma unroll
+  for (int i = 0; i < RP::RPW; ++i) {
+    const int row = warp + i * NWARP;
+    if (row >= TY * TZ) break;
+    const float rv = pr.v[i % RP::PF];
+    const float av = acc ? pa.v[i % RP::PF] : 0.0f;
+    pr.issue(i + RP::PF, rhs, warp, lane, x0, y0, z0, G.n);
+    if (acc) pa.issue(i + RP::PF, acc, warp, lane, x0, y0, z0, G.n);
     const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
     const int q = lx + WX * ly + SXY * lz;
     const Cf cf = LOCAL ? coef_fast<true, CLAMP>(sp[lx], sp[WX + ly], sp[2 * WX + lz], G) : cu;
     const int o = ro[ly + SY * lz] + x0 + lane;
     if (DIFF)
-      r[o] = (__ldg(rhs + o) - shift) + nbr_diff<LOCAL, SXY>(sv, q, cf);
+      r[o] = (rv - shift) + nbr_diff<LOCAL, SXY>(sv, q, cf);
     else
-      r[o] = (__ldg(rhs + o) - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
-    if (acc) acc[o] += sv[q];   // optional: accumulate the operand into a running sum
+      r[o] = (rv - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
+    if (acc) acc[o] = av + sv[q];   // optional: accumulate the operand into a running sum
   }
 }
 
@@ -368,6 +402,11 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
   int* ro = reinterpret_cast<int*>(smem + 2 * SN);
   float* sp = reinterpret_cast<float*>(ro + SY * SZ);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  using RP = RowPrefetch<TY, TZ>;
+  RP pf;
+#pragma unroll
+  for (int i = 0; i < RP::PF; ++i) pf.issue(i, f, warp, lane, x0, y0, z0, G.n);
   row_table<1, TY, TZ>(ro, y0, z0, G.n);
   if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
   __syncthreads();
@@ -406,9 +445,13 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
   }
   __syncthreads();
   float s1 = 0.0f, s2 = 0.0f;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int SX = WX;
-  for (int row = warp; row < TY * TZ; row += NWARP) {
+#pragma unroll
+  for (int i = 0; i < RP::RPW; ++i) {
+    const int row = warp + i * NWARP;
+    if (row >= TY * TZ) break;
+    const float fv = pf.v[i % RP::PF];
+    pf.issue(i + RP::PF, f, warp, lane, x0, y0, z0, G.n);
     const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
     const int q = lx + SX * ly + SXY * lz;
     const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1], pz = LOCAL ? sp[2 * WX + lz] : G.pg[2];
@@ -433,7 +476,7 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
                     __fmul_rn(py, pz) * ((D(q + SX + SXY) + D(q - SX - SXY)) - (D(q - SX + SXY) + D(q + SX - SXY))));
     if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
     const int o = ro[ly + SY * lz] + x0 + lane;
-    const float rv = (__ldg(f + o) - alpha) + br;
+    const float rv = (fv - alpha) + br;
     float h0, l0;
     U2(c0, h0, l0);
     ohi[o] = h0;
