@@ -148,6 +148,7 @@ _SIGS = {
     "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
     "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),
     "baorec_set_gradient": (C.c_int, [P, C.c_int32]),
+    "baorec_reconstructed_positions2": (C.c_int, [P, P, P, P, I64, C.c_int, P, P, P, C.c_int, P, P, P, C.c_uint32]),
     "baorec_read_ascii": (C.c_int, [P, C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, P, I64,
                                     C.POINTER(C.c_int64), C.c_uint32]),
     "baorec_write_npy": (C.c_int, [P, C.c_char_p, P, C.c_int32, I64, C.c_uint32]),

@@ -24,7 +24,7 @@ from ._lib import BaorecError, BoundsError, NotConverged  # noqa: F401
 __all__ = [
     "IterativeRecon", "MultigridRecon", "run_", "setup_fft_", "setup_overdensity_",
     "reconstructed_overdensity_", "reconstructed_potential_", "read_shifts",
-    "reconstructed_positions", "k_vec", "x_vec", "setup_box", "cic_", "tsc_", "cell_bins",
+    "reconstructed_positions", "reconstructed_positions2", "k_vec", "x_vec", "setup_box", "cic_", "tsc_", "cell_bins",
     "read_cic_", "smooth_", "iterate_", "jacobi_", "residual_", "reduce_", "prolong_",
     "vcycle_", "fmg", "solve_", "compute_displacements", "zeros_mesh", "BaorecError",
     "BoundsError", "NotConverged",
@@ -575,6 +575,28 @@ def read_shifts(recon, x, y, z, delta_r=None, field="disp"):
 def reconstructed_positions(recon, x, y, z, delta_r=None, field="disp"):
     """``reconstructed_positions`` (``src/recon.jl:366-388``) → new arrays p - shift."""
     return _shifts("baorec_reconstructed_positions", recon, x, y, z, delta_r, field)
+
+
+def reconstructed_positions2(recon, x, y, z, delta_r=None, fields=("sum", "disp")):
+    """Two ``reconstructed_positions`` of the same particles from one gather
+    of the displacement (the examples' ``:sum`` and ``:disp`` randoms);
+    returns (positions for fields[0], positions for fields[1]), each
+    bit-identical to its single call."""
+    for fl in fields:
+        if fl not in _lib.FIELD:
+            raise ValueError(f"field must be :disp, :rsd or :sum, got {fl!r}")
+    mesh = delta_r if delta_r is not None else recon.result_cache
+    if mesh is None:
+        raise BaorecError(_lib.ERR_STATE, "no reconstruction result (run! first)")
+    ctx = _ctx(recon, mesh.shape)
+    _set_field(ctx, mesh)
+    p = _Particles(x, y, z)
+    a = [_vec_out(p.n, p.device) for _ in range(3)]
+    b = [_vec_out(p.n, p.device) for _ in range(3)]
+    _sync_torch()
+    ctx.call("baorec_reconstructed_positions2", *p.ptrs, p.n, _lib.FIELD[fields[0]], *[_vptr(o) for o in a],
+             _lib.FIELD[fields[1]], *[_vptr(o) for o in b], p.flags)
+    return tuple(a), tuple(b)
 
 
 def compute_displacements(field_mesh, recon):

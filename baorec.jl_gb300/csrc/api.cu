@@ -690,6 +690,28 @@ static int shifts_common(baorec_ctx* ctx, const float* x, const float* y, const 
   return finish(ctx, (flags & BAOREC_HOST) ? (flags & ~BAOREC_ASYNC) : flags);
 }
 
+extern "C" int baorec_reconstructed_positions2(baorec_ctx* ctx, const float* x, const float* y, const float* z,
+                                               int64_t n, int field_a, float* oxa, float* oya, float* oza,
+                                               int field_b, float* oxb, float* oyb, float* ozb, uint32_t flags) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (n < 0 || (n > 0 && (!x || !y || !z || !oxa || !oya || !oza || !oxb || !oyb || !ozb)))
+    return set_error(ctx, BAOREC_ERR_ARG, "reconstructed_positions2: bad arguments");
+  for (int fl : {field_a, field_b})
+    if (fl < BAOREC_FIELD_DISP || fl > BAOREC_FIELD_SUM) return set_error(ctx, BAOREC_ERR_ARG, "unknown field %d", fl);
+  CKS(ensure_psi(ctx));
+  const float *dx, *dy, *dz;
+  CKS(stage_in(ctx, 0, x, n, flags, &dx));
+  CKS(stage_in(ctx, 1, y, n, flags, &dy));
+  CKS(stage_in(ctx, 2, z, n, flags, &dz));
+  float* outs[6] = {oxa, oya, oza, oxb, oyb, ozb};
+  const int slots[6] = {4, 5, 6, 8, 9, 10};
+  float* dev[6];
+  for (int k = 0; k < 6; ++k) CKS(stage_out_alloc(ctx, slots[k], n, flags, outs[k], &dev[k]));
+  CKS(readout(ctx, ctx->psi, dx, dy, dz, n, field_a, 1, dev[0], dev[1], dev[2], field_b, dev[3], dev[4], dev[5]));
+  for (int k = 0; k < 6; ++k) CKS(stage_out_copy(ctx, outs[k], dev[k], n, flags));
+  return finish(ctx, (flags & BAOREC_HOST) ? (flags & ~BAOREC_ASYNC) : flags);
+}
+
 extern "C" int baorec_read_shifts(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
                                   int field, float* sx, float* sy, float* sz, uint32_t flags) {
   return shifts_common(ctx, x, y, z, n, field, sx, sy, sz, flags, 0);

@@ -98,7 +98,7 @@ struct baorec_ctx {
   unsigned* derr = nullptr;            // device error word
   unsigned* herr = nullptr;            // pinned host copy
   // particle staging (host inputs)
-  baorec::DevBuf stage[8];
+  baorec::DevBuf stage[11];
   // statistics
   int64_t launches = 0;
   baorec_solve_stats last_stats;
@@ -211,7 +211,10 @@ int mg_vcycle_ref(baorec_ctx* ctx, int lvl, float* v, const float* f);
 int mg_fmg(baorec_ctx* ctx, const float* f, float* phi);
 int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st);
 // readout.cu
+// mode 0: shifts, 1: shifted positions, 2: one plain mesh; with p0 set a
+// second field (field2) of the same gather goes to p0..p2
 int readout(baorec_ctx* ctx, const float* psi3, const float* x, const float* y, const float* z,
-            int64_t n, int field, int mode, float* o0, float* o1, float* o2);
+            int64_t n, int field, int mode, float* o0, float* o1, float* o2, int field2 = 0,
+            float* p0 = nullptr, float* p1 = nullptr, float* p2 = nullptr);
 
 }  // namespace baorec

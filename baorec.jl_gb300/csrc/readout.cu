@@ -53,7 +53,8 @@ __device__ __forceinline__ float tri(const float* __restrict__ m, const size_t o
 __global__ void readout_kernel(const float* __restrict__ psi, size_t N, const float* __restrict__ x,
                                const float* __restrict__ y, const float* __restrict__ z, int64_t n, RGeom G,
                                int field, int mode, float* __restrict__ o0, float* __restrict__ o1,
-                               float* __restrict__ o2, unsigned* err) {
+                               float* __restrict__ o2, int field2, float* __restrict__ p0, float* __restrict__ p1,
+                               float* __restrict__ p2, unsigned* err) {
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
     float px = x[q], py = y[q], pz = z[q];
     int xl, xh, yl, yh, zl, zh;
@@ -66,6 +67,7 @@ __global__ void readout_kernel(const float* __restrict__ psi, size_t N, const fl
       const float nan = __int_as_float(0x7fc00000);
       o0[q] = nan;
       if (mode != 2) { o1[q] = nan; o2[q] = nan; }
+      if (p0) { p0[q] = nan; p1[q] = nan; p2[q] = nan; }
       continue;
     }
     const size_t n0 = (size_t)G.n[0], n01 = (size_t)G.n[0] * G.n[1];
@@ -92,29 +94,35 @@ __global__ void readout_kernel(const float* __restrict__ psi, size_t N, const fl
       s[a] = t;
     }
     (void)N;
-    if (field != 0) {
-      float l0, l1, l2;
-      if (G.local) {
-        float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), __fmul_rn(pz, pz)));
-        l0 = __fdiv_rn(px, dist); l1 = __fdiv_rn(py, dist); l2 = __fdiv_rn(pz, dist);
-      } else {
-        l0 = G.los[0]; l1 = G.los[1]; l2 = G.los[2];
+    // one gathered Ψ, one or two fields out (the same arithmetic either way)
+    auto emit = [&](int fld, float* __restrict__ a0, float* __restrict__ a1, float* __restrict__ a2) {
+      float t[3] = {s[0], s[1], s[2]};
+      if (fld != 0) {
+        float l0, l1, l2;
+        if (G.local) {
+          float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), __fmul_rn(pz, pz)));
+          l0 = __fdiv_rn(px, dist); l1 = __fdiv_rn(py, dist); l2 = __fdiv_rn(pz, dist);
+        } else {
+          l0 = G.los[0]; l1 = G.los[1]; l2 = G.los[2];
+        }
+        float dot = __fadd_rn(__fadd_rn(__fmul_rn(t[0], l0), __fmul_rn(t[1], l1)), __fmul_rn(t[2], l2));
+        float fd = __fmul_rn(G.f, dot);
+        float r0 = __fmul_rn(fd, l0), r1 = __fmul_rn(fd, l1), r2 = __fmul_rn(fd, l2);
+        if (fld == 1) { t[0] = r0; t[1] = r1; t[2] = r2; }
+        else { t[0] = __fadd_rn(t[0], r0); t[1] = __fadd_rn(t[1], r1); t[2] = __fadd_rn(t[2], r2); }
       }
-      float dot = __fadd_rn(__fadd_rn(__fmul_rn(s[0], l0), __fmul_rn(s[1], l1)), __fmul_rn(s[2], l2));
-      float fd = __fmul_rn(G.f, dot);
-      float r0 = __fmul_rn(fd, l0), r1 = __fmul_rn(fd, l1), r2 = __fmul_rn(fd, l2);
-      if (field == 1) { s[0] = r0; s[1] = r1; s[2] = r2; }
-      else { s[0] = __fadd_rn(s[0], r0); s[1] = __fadd_rn(s[1], r1); s[2] = __fadd_rn(s[2], r2); }
-    }
-    if (mode == 1) { s[0] = __fsub_rn(px, s[0]); s[1] = __fsub_rn(py, s[1]); s[2] = __fsub_rn(pz, s[2]); }
-    o0[q] = s[0]; o1[q] = s[1]; o2[q] = s[2];
+      if (mode == 1) { t[0] = __fsub_rn(px, t[0]); t[1] = __fsub_rn(py, t[1]); t[2] = __fsub_rn(pz, t[2]); }
+      a0[q] = t[0]; a1[q] = t[1]; a2[q] = t[2];
+    };
+    emit(field, o0, o1, o2);
+    if (p0) emit(field2, p0, p1, p2);
   }
 }
 
 }  // namespace
 
 int readout(baorec_ctx* ctx, const float* psi3, const float* x, const float* y, const float* z, int64_t n,
-            int field, int mode, float* o0, float* o1, float* o2) {
+            int field, int mode, float* o0, float* o1, float* o2, int field2, float* p0, float* p1, float* p2) {
   if (n <= 0) return BAOREC_OK;
   RGeom G;
   const int nn[3] = {ctx->n1, ctx->n2, ctx->n3};
@@ -128,7 +136,8 @@ int readout(baorec_ctx* ctx, const float* psi3, const float* x, const float* y, 
   G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
   unsigned grid = grid_for((size_t)n, 256);
   if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;
-  readout_kernel<<<grid, 256, 0, ctx->stream>>>(psi3, ctx->N, x, y, z, n, G, field, mode, o0, o1, o2, ctx->derr);
+  readout_kernel<<<grid, 256, 0, ctx->stream>>>(psi3, ctx->N, x, y, z, n, G, field, mode, o0, o1, o2, field2, p0, p1,
+                                                 p2, ctx->derr);
   CKLAUNCH();
   return BAOREC_OK;
 }

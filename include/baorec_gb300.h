@@ -295,6 +295,12 @@ int baorec_read_shifts(baorec_ctx* ctx, const float* x, const float* y, const fl
 int baorec_reconstructed_positions(baorec_ctx* ctx, const float* x, const float* y,
                                    const float* z, int64_t n, int field,
                                    float* ox, float* oy, float* oz, uint32_t flags);
+/* Two reconstructed_positions calls on the same particles (the examples'
+ * :sum and :disp randoms, test_helpers' "sym" and "iso" catalogs) from one
+ * gather of the displacement: outputs bit-identical to the two calls. */
+int baorec_reconstructed_positions2(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
+                                    int field_a, float* oxa, float* oya, float* oza,
+                                    int field_b, float* oxb, float* oyb, float* ozb, uint32_t flags);
 
 /* ---- Catalog I/O (examples/lightcone.jl:22-23, examples/simulation.jl:13
  * read catalogs with CSV.jl; examples/simulation.jl:38-40 write the shifted

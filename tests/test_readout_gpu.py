@@ -52,3 +52,25 @@ def test_shifts_and_positions_bit_exact(los, field):
     rpos = O.reconstructed_positions(ref, x, y, z)
     for a in range(3):
         np.testing.assert_array_equal(pos[a], rpos[a])
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_positions2_equals_two_calls(device):
+    """The fused two-field read-out gives exactly the two single calls."""
+    import torch
+    import baorec
+    n, L = 32, F32(900.0)
+    bm = [F32(100.0), F32(200.0), F32(300.0)]
+    rng = np.random.default_rng(9)
+    fld = O.smooth(rng.standard_normal((n, n, n)).astype(F32), 30.0, [L] * 3)
+    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=[L] * 3, box_min=bm)
+    x, y, z, _ = uniform_box(10000, L, seed=10)
+    x, y, z = (x + bm[0]).astype(F32), (y + bm[1]).astype(F32), (z + bm[2]).astype(F32)
+    if device:
+        x, y, z = (torch.from_numpy(a).cuda() for a in (x, y, z))
+    a, b = baorec.reconstructed_positions2(rec, x, y, z, np.asfortranarray(fld), fields=("sum", "disp"))
+    ra = baorec.reconstructed_positions(rec, x, y, z, np.asfortranarray(fld), field="sum")
+    rb = baorec.reconstructed_positions(rec, x, y, z, np.asfortranarray(fld), field="disp")
+    conv = (lambda t: t.cpu().numpy()) if device else (lambda t: t)
+    for u, v in zip(a + b, ra + rb):
+        np.testing.assert_array_equal(conv(u), conv(v))
