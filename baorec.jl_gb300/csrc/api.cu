@@ -3,6 +3,7 @@
 #include <math.h>
 #include <stdarg.h>
 
+#include <algorithm>
 #include <new>
 
 #include "common.cuh"
@@ -258,6 +259,14 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
                     &ctx->pw_part, &ctx->pw_nz})
     cudaFree(b->p);
   if (ctx->ev_red) cudaEventDestroy(ctx->ev_red);
+  for (int s = 0; s < 2; ++s)
+    for (cudaEvent_t e : {ctx->ev_in[s], ctx->ev_k[s], ctx->ev_out[s]})
+      if (e) cudaEventDestroy(e);
+  if (ctx->ev_begin) cudaEventDestroy(ctx->ev_begin);
+  if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+  if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
+  if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
+  cudaFree(ctx->pipe_buf.p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return BAOREC_OK;
@@ -668,6 +677,62 @@ extern "C" int baorec_read_cic(baorec_ctx* ctx, const float* mesh, const float* 
   return finish(ctx, (flags & BAOREC_HOST) ? (flags & ~BAOREC_ASYNC) : flags);
 }
 
+// Read-out of host particles to host outputs in chunks of kPipeChunk: the
+// copy-in of chunk c+1 (stream s_in), the read-out of chunk c (the context
+// stream) and the copy-out of chunk c-1 (s_out) overlap, on two staging
+// slots guarded by events.  The same kernel on the same particles: results
+// are those of the unchunked call.
+static constexpr int64_t kPipeChunk = (int64_t)1 << 20;
+
+static int readout_pipelined(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
+                             int mode, float* const outs[6], int nout, int field2) {
+  if (!ctx->s_in) {
+    CK(cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+    for (int s = 0; s < 2; ++s) {
+      CK(cudaEventCreateWithFlags(&ctx->ev_in[s], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->ev_k[s], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->ev_out[s], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&ctx->ev_begin, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+  }
+  constexpr int kPer = 9;   // 3 inputs + up to 6 outputs per slot
+  CKS(ensure(ctx, ctx->pipe_buf, (size_t)2 * kPer * kPipeChunk * sizeof(float)));
+  float* base = (float*)ctx->pipe_buf.p;
+  auto buf = [&](int s, int k) { return base + ((size_t)s * kPer + k) * kPipeChunk; };
+  // nothing of this call starts before the work already on the context stream
+  CK(cudaEventRecord(ctx->ev_begin, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->s_in, ctx->ev_begin, 0));
+  CK(cudaStreamWaitEvent(ctx->s_out, ctx->ev_begin, 0));
+  const float* X[3] = {x, y, z};
+  const int64_t nch = (n + kPipeChunk - 1) / kPipeChunk;
+  for (int64_t c = 0; c < nch; ++c) {
+    const int s = (int)(c & 1);
+    const int64_t off = c * kPipeChunk, m = std::min(kPipeChunk, n - off);
+    if (c >= 2) CK(cudaStreamWaitEvent(ctx->s_in, ctx->ev_k[s], 0));   // chunk c-2 has read its inputs
+    for (int a = 0; a < 3; ++a)
+      CK(cudaMemcpyAsync(buf(s, a), X[a] + off, (size_t)m * 4, cudaMemcpyHostToDevice, ctx->s_in));
+    CK(cudaEventRecord(ctx->ev_in[s], ctx->s_in));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in[s], 0));
+    if (c >= 2) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_out[s], 0));   // chunk c-2's outputs are out
+    CKS(readout(ctx, ctx->psi, buf(s, 0), buf(s, 1), buf(s, 2), m, field, mode, buf(s, 3), buf(s, 4), buf(s, 5),
+                field2, nout == 6 ? buf(s, 6) : nullptr, nout == 6 ? buf(s, 7) : nullptr,
+                nout == 6 ? buf(s, 8) : nullptr));
+    CK(cudaEventRecord(ctx->ev_k[s], ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->s_out, ctx->ev_k[s], 0));
+    for (int k = 0; k < nout; ++k)
+      CK(cudaMemcpyAsync(outs[k] + off, buf(s, 3 + k), (size_t)m * 4, cudaMemcpyDeviceToHost, ctx->s_out));
+    CK(cudaEventRecord(ctx->ev_out[s], ctx->s_out));
+  }
+  // the context stream (and so the caller's synchronisation) covers the copies
+  CK(cudaEventRecord(ctx->ev_done, ctx->s_out));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_done, 0));
+  CK(cudaEventRecord(ctx->ev_done, ctx->s_in));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_done, 0));
+  return BAOREC_OK;
+}
+
 static int shifts_common(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
                          float* o0, float* o1, float* o2, uint32_t flags, int mode) {
   if (!ctx) return BAOREC_ERR_ARG;
@@ -675,6 +740,11 @@ static int shifts_common(baorec_ctx* ctx, const float* x, const float* y, const 
     return set_error(ctx, BAOREC_ERR_ARG, "read_shifts: bad arguments");
   if (field < BAOREC_FIELD_DISP || field > BAOREC_FIELD_SUM) return set_error(ctx, BAOREC_ERR_ARG, "unknown field %d", field);
   CKS(ensure_psi(ctx));
+  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk) {
+    float* const outs[6] = {o0, o1, o2, nullptr, nullptr, nullptr};
+    CKS(readout_pipelined(ctx, x, y, z, n, field, mode, outs, 3, 0));
+    return finish(ctx, flags & ~BAOREC_ASYNC);
+  }
   const float *dx, *dy, *dz;
   CKS(stage_in(ctx, 0, x, n, flags, &dx));
   CKS(stage_in(ctx, 1, y, n, flags, &dy));
@@ -699,6 +769,11 @@ extern "C" int baorec_reconstructed_positions2(baorec_ctx* ctx, const float* x, 
   for (int fl : {field_a, field_b})
     if (fl < BAOREC_FIELD_DISP || fl > BAOREC_FIELD_SUM) return set_error(ctx, BAOREC_ERR_ARG, "unknown field %d", fl);
   CKS(ensure_psi(ctx));
+  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk) {
+    float* const po[6] = {oxa, oya, oza, oxb, oyb, ozb};
+    CKS(readout_pipelined(ctx, x, y, z, n, field_a, 1, po, 6, field_b));
+    return finish(ctx, flags & ~BAOREC_ASYNC);
+  }
   const float *dx, *dy, *dz;
   CKS(stage_in(ctx, 0, x, n, flags, &dx));
   CKS(stage_in(ctx, 1, y, n, flags, &dy));

@@ -69,6 +69,11 @@ struct baorec_ctx {
   float* psi = nullptr;                // 6 real meshes (displacements / iterative parts)
   bool psi_valid = false;              // psi[0..2] hold the displacement of `result`
   cudaEvent_t ev_red = nullptr;          // the solve's partial sums have reached the host
+  // chunked host read-out: copy-in and copy-out streams beside `stream`, the
+  // events that order them per staging slot, and the double-buffered staging
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[2] = {}, ev_k[2] = {}, ev_out[2] = {}, ev_begin = nullptr, ev_done = nullptr;
+  baorec::DevBuf pipe_buf;
   int grad_mode = BAOREC_GRADIENT_FFT;  // multigrid displacement: spectral or finite-difference gradient
   cufftComplex* ck = nullptr;          // complex work: 6 spectra
   float* xvec[3] = {nullptr, nullptr, nullptr};   // x_vec of the mesh (device)
