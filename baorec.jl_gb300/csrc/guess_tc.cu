@@ -50,6 +50,8 @@
 // between the roles; every wait is bounded in time and on expiry sets
 // kErrTimeout and stops its role, and the block drains its copies and MMAs
 // before freeing TMEM.
+#include <algorithm>
+
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -65,8 +67,6 @@ typedef __nv_bfloat16 bf16;
 constexpr int kTM = 128;                 // voxels per tile (MMA M)
 constexpr int kSlots = kTM + 2;          // x slots of a slab row (halo of 1 each side)
 constexpr int kRowBytes = kSlots * 16;   // 2080: one dy row of one chunk
-constexpr int kBoxBytes = 3 * kRowBytes;  // 6240: bytes one TMA box delivers
-constexpr int kPlane = 6272;             // one chunk of a slab: the box padded to 128 B
 constexpr int kProducers = 64;           // warps 0-1 load slabs
 constexpr int kMmaWarp = 2;              // MMA issuer and TMEM owner
 constexpr int kEpiWarp0 = 3;             // warps 3-10: two epilogue teams of 4 warps
@@ -87,12 +87,24 @@ struct Tc {
   static constexpr int KS = PAIRED ? 1 : CIN / 16;   // K steps of 16 channels per tap
   static constexpr int NMMA = PAIRED ? 6 : 9 * KS;   // MMAs per slab and dz group
   static constexpr int CH = CIN / 8;                 // 16-byte chunks per voxel
-  static constexpr int SLAB = CH * kPlane;
   static constexpr int WB = NMMA * 2 * 3 * COUT * 16; // weight image bytes
-  static constexpr int S0 = (kSmemBudget - WB) / SLAB;
-  static constexpr int S = S0 > 6 ? 6 : S0;          // slab ring depth
+  // a unit covers YR output rows (y0 .. y0+YR-1) from a slab of YR+2 input
+  // rows; one chunk plane = the TMA box plus a zeroed 32-byte pad (the
+  // 8-channel MMAs read 16 bytes past the box), rounded to 128 bytes
+  static constexpr int plane_of(int yr) { return ((yr + 2) * kRowBytes + 32 + 127) / 128 * 128; }
+  static constexpr int s_of(int yr) {
+    return (kSmemBudget - WB) / (CH * plane_of(yr)) > 6 ? 6 : (kSmemBudget - WB) / (CH * plane_of(yr));
+  }
+  // the most rows whose accumulator rings fit the 512 TMEM columns and whose
+  // slabs still leave a ring of two in shared memory
+  static constexpr int YR = (4 * kRing * COUT <= 512 && s_of(4) >= 2) ? 4
+                            : (2 * kRing * COUT <= 512 && s_of(2) >= 2) ? 2 : 1;
+  static constexpr int BOX = (YR + 2) * kRowBytes;   // bytes one TMA box delivers
+  static constexpr int PLANE = plane_of(YR);
+  static constexpr int SLAB = CH * PLANE;
+  static constexpr int S = s_of(YR);                 // slab ring depth
   static constexpr int SMEM = WB + S * SLAB + 1024;  // + alignment slack
-  static constexpr int TCOLS = kRing * COUT;         // TMEM columns: the accumulator ring
+  static constexpr int TCOLS = YR * kRing * COUT;    // TMEM columns: one accumulator ring per output row
   // S >= 2: a slab is freed as soon as its own MMAs complete, so the loader
   // refills one slot while the MMAs read the other
   static_assert(S >= 2, "slab ring too shallow for this shape");
@@ -282,13 +294,14 @@ struct Unit {
   int x0, y, z0;
 };
 
-__device__ __forceinline__ Unit unit_of(long long u, int n, int zc) {
-  const int xsegs = n / kTM;
+// unit u = (x segment, group of yr rows, column of zc z planes), x fastest
+__device__ __forceinline__ Unit unit_of(long long u, int n, int zc, int yr) {
+  const int xsegs = n / kTM, ny = n / yr;
   Unit t;
   t.x0 = (int)(u % xsegs) * kTM;
   const long long r = u / xsegs;
-  t.y = (int)(r % n);
-  t.z0 = (int)(r / n) * zc;
+  t.y = (int)(r % ny) * yr;
+  t.z0 = (int)(r / ny) * zc;
   return t;
 }
 
@@ -297,11 +310,12 @@ __device__ __forceinline__ void give_up(volatile int* abort_flag, unsigned* err)
   atomicOr(err, kErrTimeout);
 }
 
-// One slab (plane z_in of unit t) into shared memory at dst: this producer
-// thread's share of the 16-byte pieces, piece q = (dy*130 + slot)*CH + chunk.
-template <int CH>
+// One slab (plane z_in of unit t, rows y0-1 .. y0+YR) into shared memory at
+// dst: this producer thread's share of the 16-byte pieces, piece
+// q = (row*130 + slot)*CH + chunk.
+template <int CH, int YR, int PLANE>
 __device__ __forceinline__ void load_slab(const TcArgs& a, const Unit& t, int z_in, uint32_t dst, int pt) {
-  constexpr int PIECES = 3 * kSlots * CH;
+  constexpr int PIECES = (YR + 2) * kSlots * CH;
   const int n = a.n;
   const bool zok = (unsigned)z_in < (unsigned)n;
 #pragma unroll 4
@@ -311,18 +325,18 @@ __device__ __forceinline__ void load_slab(const TcArgs& a, const Unit& t, int z_
     const int xx = t.x0 - 1 + sl, yy = t.y + dy - 1;
     const bool ok = zok && (unsigned)xx < (unsigned)n && (unsigned)yy < (unsigned)n;
     const bf16* src = ok ? a.in + (((size_t)z_in * n + yy) * n + xx) * a.in_cs + 8 * c : a.in;
-    cp_async16(dst + (uint32_t)(c * kPlane + dy * kRowBytes + sl * 16), src, ok ? 16u : 0u);
+    cp_async16(dst + (uint32_t)(c * PLANE + dy * kRowBytes + sl * 16), src, ok ? 16u : 0u);
   }
 }
 
 // Descriptor offset (16-byte units) of the A window of MMA k of a slab: k =
 // (dy*3 + dx)*KS + ks, or for 8 channels k = dy*2 + q (taps dx = 2q, 2q+1).
 // The B image holds the matching weights at k * 2 * 3*COUT*16 bytes.
-template <bool PAIRED, int KS>
+template <bool PAIRED, int KS, int PLANE>
 __device__ __forceinline__ uint64_t a_off(int k) {
   if (PAIRED) return (uint64_t)(((k >> 1) * kRowBytes + (k & 1) * 32) >> 4);
   const int ks = k % KS, dx = (k / KS) % 3, dy = k / (3 * KS);
-  return (uint64_t)((2 * ks * kPlane + dy * kRowBytes + dx * 16) >> 4);
+  return (uint64_t)((2 * ks * PLANE + dy * kRowBytes + dx * 16) >> 4);
 }
 
 // TMEM accumulator of output row i (rows counted across the CTA's columns):
@@ -344,7 +358,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
   const uint32_t wsm = base, ssm = base + P::WB;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = a.n, zc = a.zc;
-  const long long nunits = (long long)(n / kTM) * n * (n / zc);
+  constexpr int YR = P::YR;
+  const long long nunits = (long long)(n / kTM) * (n / YR) * (n / zc);
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
@@ -363,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
   // the 32-byte pad after each chunk of a slab is never loaded; an 8-channel
   // MMA reads it (times zero weights), so it must hold finite values
   for (int q = threadIdx.x; q < S * P::CH * 2; q += blockDim.x)
-    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(ssm + (uint32_t)(q >> 1) * kPlane + kBoxBytes + (q & 1) * 16),
+    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(ssm + (uint32_t)(q >> 1) * P::PLANE + P::BOX + (q & 1) * 16),
                  "r"(0u)
                  : "memory");
   fence_proxy_async();
@@ -402,7 +417,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         bool ok = true;
         long long j = 0;   // slab loads issued
         for (long long u = blockIdx.x; ok && u < nunits; u += gridDim.x) {
-          const Unit t = unit_of(u, n, zc);
+          const Unit t = unit_of(u, n, zc, YR);
           for (int p = 0; p < zc + 2; ++p, ++j) {
             const int slot = (int)(j % S);
             const long long use = j / S;
@@ -411,11 +426,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
               break;
             }
             const uint32_t full = smem_u32(&bar_full[slot]);
-            mbar_expect_tx(full, (uint32_t)(P::CH * kBoxBytes));
+            mbar_expect_tx(full, (uint32_t)(P::CH * P::BOX));
             const uint32_t dst = ssm + (uint32_t)slot * P::SLAB;
 #pragma unroll
             for (int c = 0; c < P::CH; ++c)
-              tma_load_4d(dst + c * kPlane, &tmap, full, 8 * c, t.x0 - 1, t.y - 1, t.z0 - 1 + p);
+              tma_load_4d(dst + c * P::PLANE, &tmap, full, 8 * c, t.x0 - 1, t.y - 1, t.z0 - 1 + p);
           }
         }
         if (!ok) give_up(&abort_flag, a.err);
@@ -434,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       bool ok = true;
       long long j = 0, signalled = 0;
       for (long long u = blockIdx.x; ok && u < nunits; u += gridDim.x) {
-        const Unit t = unit_of(u, n, zc);
+        const Unit t = unit_of(u, n, zc, YR);
         for (int p = 0; p < zc + 2; ++p, ++j) {
           if (j - signalled >= AHEAD) {
             cp_async_wait<AHEAD - 1>();
@@ -448,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
             ok = false;
             break;
           }
-          load_slab<P::CH>(a, t, t.z0 - 1 + p, ssm + (uint32_t)slot * P::SLAB, pt);
+          load_slab<P::CH, YR, P::PLANE>(a, t, t.z0 - 1 + p, ssm + (uint32_t)slot * P::SLAB, pt);
           cp_async_commit();
         }
       }
@@ -489,28 +504,35 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           const int s_lo = acc_slot(i0 + p - dz_lo);
           const int n1 = nd < kRing - s_lo ? nd : kRing - s_lo;   // blocks before the ring wraps
           const int n2 = nd - n1;
-          const uint32_t d1 = tm + (uint32_t)(s_lo * COUT), d2 = tm;
           const uint32_t id1 = idesc0 | ((uint32_t)(n1 * COUT >> 3) << 17);
           const uint32_t id2 = idesc0 | ((uint32_t)(n2 * COUT >> 3) << 17);
           // descriptors are linear in the start address (14-bit field, smem
           // below 256 KB): per MMA only compile-time offsets are added
-          const uint64_t a_base = sdesc(ssm + (uint32_t)slot * P::SLAB, P::PAIRED ? 16u : (uint32_t)kPlane, 128);
+          const uint64_t a_base = sdesc(ssm + (uint32_t)slot * P::SLAB, P::PAIRED ? 16u : (uint32_t)P::PLANE, 128);
           const uint64_t b_base1 = sdesc(wsm + (uint32_t)dz_lo * kBlk, kLboB, 128);
           const uint64_t b_base2 = sdesc(wsm + (uint32_t)(dz_lo + n1) * kBlk, kLboB, 128);
-          if (n2 == 0) {
+          // output row y0 + yy reads slab rows yy .. yy+2 and accumulates in
+          // its own ring (TMEM columns yy*kRing*COUT ..)
 #pragma unroll
-            for (int k = 0; k < P::NMMA; ++k) {
-              const uint64_t ad = a_base + a_off<P::PAIRED, P::KS>(k);
-              const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
-              mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
-            }
-          } else {
+          for (int yy = 0; yy < YR; ++yy) {
+            const uint32_t ring = tm + (uint32_t)(yy * kRing * COUT);
+            const uint32_t d1 = ring + (uint32_t)(s_lo * COUT), d2 = ring;
+            const uint64_t a_row = a_base + (uint64_t)((yy * kRowBytes) >> 4);
+            if (n2 == 0) {
 #pragma unroll
-            for (int k = 0; k < P::NMMA; ++k) {
-              const uint64_t ad = a_base + a_off<P::PAIRED, P::KS>(k);
-              const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
-              mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
-              mma_bf16(d2, ad, b_base2 + bo, id2, 1u);
+              for (int k = 0; k < P::NMMA; ++k) {
+                const uint64_t ad = a_row + a_off<P::PAIRED, P::KS, P::PLANE>(k);
+                const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
+                mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < P::NMMA; ++k) {
+                const uint64_t ad = a_row + a_off<P::PAIRED, P::KS, P::PLANE>(k);
+                const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
+                mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
+                mma_bf16(d2, ad, b_base2 + bo, id2, 1u);
+              }
             }
           }
           mma_commit(smem_u32(&bar_empty[slot]));
@@ -534,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
     bool ok = true;
     long long i = 0;
     for (long long u = blockIdx.x; ok && u < nunits; u += gridDim.x) {
-      const Unit t = unit_of(u, n, zc);
+      const Unit t = unit_of(u, n, zc, YR);
       for (int zl = 0; zl < zc; ++zl, ++i) {
         if ((int)(i & 1) != team) continue;
         const int s = acc_slot(i);
@@ -544,40 +566,43 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           break;
         }
         tc_fence_after();
-        const uint32_t acc = lane_addr + (uint32_t)(s * COUT);
-        float v[COUT];
-        tmem_ld_row<COUT>(acc, v);
-        // zero the accumulator for its next row; the wait comes after the stores
+#pragma unroll 1
+        for (int yy = 0; yy < YR; ++yy) {
+          const uint32_t acc = lane_addr + (uint32_t)((yy * kRing + s) * COUT);
+          float v[COUT];
+          tmem_ld_row<COUT>(acc, v);
+          // zero the accumulator for its next row; the wait comes after the stores
 #pragma unroll
-        for (int c = 0; c < COUT; c += 16) tmem_zero16(acc + (uint32_t)c);
-        const size_t vo = ((size_t)(t.z0 + zl) * n + t.y) * n + (t.x0 + m);
-        if (a.bias) {
+          for (int c = 0; c < COUT; c += 16) tmem_zero16(acc + (uint32_t)c);
+          const size_t vo = ((size_t)(t.z0 + zl) * n + (t.y + yy)) * n + (t.x0 + m);
+          if (a.bias) {
 #pragma unroll
-          for (int c = 0; c < COUT; ++c) v[c] += __ldg(a.bias + c);
-        }
-        if (a.add) {
-          const uint4* ap = reinterpret_cast<const uint4*>(a.add + vo * a.add_cs);
+            for (int c = 0; c < COUT; ++c) v[c] += __ldg(a.bias + c);
+          }
+          if (a.add) {
+            const uint4* ap = reinterpret_cast<const uint4*>(a.add + vo * a.add_cs);
 #pragma unroll
-          for (int g = 0; g < COUT / 8; ++g) {
-            const uint4 q = ap[g];
-            const uint32_t wd[4] = {q.x, q.y, q.z, q.w};
+            for (int g = 0; g < COUT / 8; ++g) {
+              const uint4 q = ap[g];
+              const uint32_t wd[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-              const __nv_bfloat162 p2 = *reinterpret_cast<const __nv_bfloat162*>(&wd[h]);
-              v[8 * g + 2 * h] += __bfloat162float(p2.x);
-              v[8 * g + 2 * h + 1] += __bfloat162float(p2.y);
+              for (int h = 0; h < 4; ++h) {
+                const __nv_bfloat162 p2 = *reinterpret_cast<const __nv_bfloat162*>(&wd[h]);
+                v[8 * g + 2 * h] += __bfloat162float(p2.x);
+                v[8 * g + 2 * h + 1] += __bfloat162float(p2.y);
+              }
             }
           }
-        }
-        if (a.relu) {
+          if (a.relu) {
 #pragma unroll
-          for (int c = 0; c < COUT; ++c) v[c] = fmaxf(v[c], 0.0f);
-        }
-        uint4* op = reinterpret_cast<uint4*>(a.out + vo * a.out_cs);
+            for (int c = 0; c < COUT; ++c) v[c] = fmaxf(v[c], 0.0f);
+          }
+          uint4* op = reinterpret_cast<uint4*>(a.out + vo * a.out_cs);
 #pragma unroll
-        for (int g = 0; g < COUT / 8; ++g)
-          op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
-                             pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+          for (int g = 0; g < COUT / 8; ++g)
+            op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
+                               pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+        }
         tmem_wait_st();
         tc_fence_before();
         mbar_arrive(smem_u32(&bar_acce[s]));
@@ -653,15 +678,15 @@ EncodeTiledFn encode_fn() {
 }
 
 // Input activations as a 4-D tensor {channels, x, y, z} (channels fastest,
-// voxel pitch in_cs elements); box {8, 130, 3, 1}.
-cudaError_t input_map(CUtensorMap* map, const bf16* in, int in_cs, int cin, int n) {
+// voxel pitch in_cs elements); box {8, 130, yr + 2, 1}.
+cudaError_t input_map(CUtensorMap* map, const bf16* in, int in_cs, int cin, int n, int yr) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
   if (((uintptr_t)in & 15) || (in_cs * 2) % 16) return cudaErrorInvalidValue;
   const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n};
   const cuuint64_t pitch = (cuuint64_t)in_cs * 2;
   const cuuint64_t strides[3] = {pitch, pitch * n, pitch * n * n};
-  const cuuint32_t box[4] = {8, (cuuint32_t)kSlots, 3, 1};
+  const cuuint32_t box[4] = {8, (cuuint32_t)kSlots, (cuuint32_t)(yr + 2), 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in), dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -683,14 +708,18 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
     int b = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, conv_tc_kernel<CIN, COUT, LOADER>, kThreads, P::SMEM);
     if (e != cudaSuccess) return e;
-    blocks_per_sm[dev] = b > 0 ? b : 1;
+    // every resident CTA holds TCOLS of the SM's 512 TMEM columns for its
+    // whole (persistent) life: a CTA that cannot allocate would wait for the
+    // others to finish
+    const int by_tmem = 512 / P::TCOLS;
+    blocks_per_sm[dev] = std::max(1, std::min(b, by_tmem));
   }
   // 16-byte pieces of every voxel: aligned base and pitch
   if (((uintptr_t)c.in & 15) || (c.in_cs * 2) % 16 || ((uintptr_t)c.wimg & 15)) return cudaErrorInvalidValue;
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   if (LOADER == kLoadTma) {
-    e = input_map(&map, c.in, c.in_cs, CIN, n);
+    e = input_map(&map, c.in, c.in_cs, CIN, n, P::YR);
     if (e != cudaSuccess) return e;
   }
   TcArgs a;
@@ -711,12 +740,12 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
   long long best_rows = 0;
   for (int zc = 16; zc >= 4; zc /= 2) {
     if (n % zc) continue;
-    const long long units = (long long)(n / kTM) * n * (n / zc);
+    const long long units = (long long)(n / kTM) * (n / P::YR) * (n / zc);
     const long long rows = ((units + ctas - 1) / ctas) * (zc + 2);   // slab loads of the busiest CTA
     if (!best || rows < best_rows) { best = zc; best_rows = rows; }
   }
   a.zc = best;
-  const long long units = (long long)(n / kTM) * n * (n / best);
+  const long long units = (long long)(n / kTM) * (n / P::YR) * (n / best);
   const unsigned grid = (unsigned)(units < ctas ? units : ctas);
   conv_tc_kernel<CIN, COUT, LOADER><<<grid, kThreads, P::SMEM, s>>>(map, a);
   return cudaGetLastError();

@@ -153,7 +153,7 @@ def guess_conv_rooflines(ctx, C, shapes=GUESS_CONV_SHAPES):
     out = {}
     for cin, cout, n in shapes:
         row = {}
-        for path, label in ((1, "tcgen05"), (0, "mma.sync")):
+        for path, label in ((1, "tcgen05"), (2, "tcgen05_cpasync"), (0, "mma.sync")):
             avg, fl = C.c_float(), C.c_double()
             ctx.call("baorec_guess_profile_conv", cin, cout, n, path, 10, C.byref(avg), C.byref(fl))
             tf = fl.value / (avg.value * 1e-3) / 1e12
@@ -163,7 +163,8 @@ def guess_conv_rooflines(ctx, C, shapes=GUESS_CONV_SHAPES):
             "kernel": "conv_tc_kernel (tcgen05.mma, TMA slabs, TMEM accumulators)", "bound": "tensor",
             "achieved": tc["achieved"], "peak": peak, "unit": "TFLOP/s", "frac": tc["achieved"] / peak,
             "peak_source": src, "algorithmic_flops_per_launch": 2.0 * 27 * cin * cout * n ** 3,
-            "avg_launch_ms": tc["avg_launch_ms"], "mma_sync": row["mma.sync"]}
+            "avg_launch_ms": tc["avg_launch_ms"], "mma_sync": row["mma.sync"],
+            "tcgen05_cpasync_loader": row["tcgen05_cpasync"]}
     return out
 
 
