@@ -117,13 +117,17 @@ __global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
       }
     }
   }
-  // epilogue: bias, addend, ReLU, BF16 store (two channels per thread and row)
+  // epilogue: bias, addend, ReLU, BF16.  C3 and DN: the warp's 32 output
+  // voxels are consecutive in x, so they are staged in shared memory and
+  // written as 16-byte vectors (a voxel's COUT channels are contiguous); UP
+  // (its own kernel in the network) keeps per-thread stores.
+  __shared__ __align__(16) __nv_bfloat16 stile[KIND == UP ? 1 : kWarps][KIND == UP ? 8 : 16 * kMT * COUT];
+  const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int m = 0; m < kMT; ++m)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int x = x0 + 16 * m + g + 8 * h;
-      if (x >= nx) continue;
       size_t vo;
       if (KIND == UP)
         vo = vox(a.n_out, 2 * x + (par & 1), 2 * y + ((par >> 1) & 1), 2 * z + (par >> 2));
@@ -134,15 +138,32 @@ __global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
         const int n = 8 * nb + 2 * q;
         float v0 = acc[m][nb][2 * h], v1 = acc[m][nb][2 * h + 1];
         if (a.bias) { v0 += __ldg(a.bias + n); v1 += __ldg(a.bias + n + 1); }
-        if (a.add) {
+        if (a.add && x < nx) {
           const __nv_bfloat162 ad = *reinterpret_cast<const __nv_bfloat162*>(a.add + vo * a.add_cs + n);
           v0 += __bfloat162float(ad.x);
           v1 += __bfloat162float(ad.y);
         }
         if (a.relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
-        *reinterpret_cast<__nv_bfloat162*>(a.out + vo * a.out_cs + n) = __floats2bfloat162_rn(v0, v1);
+        if (KIND == UP) {
+          if (x < nx) *reinterpret_cast<__nv_bfloat162*>(a.out + vo * a.out_cs + n) = __floats2bfloat162_rn(v0, v1);
+        } else {
+          *reinterpret_cast<__nv_bfloat162*>(&stile[warp][(16 * m + g + 8 * h) * COUT + n]) =
+              __floats2bfloat162_rn(v0, v1);
+        }
       }
     }
+  if (KIND != UP) {
+    constexpr int VPV = COUT / 8;   // 16-byte vectors per voxel
+    __syncwarp();
+    const uint4* sv = reinterpret_cast<const uint4*>(stile[warp]);
+    const size_t row0 = vox(a.n_out, x0, y, z);
+#pragma unroll
+    for (int k = 0; k < kMT * VPV / 2; ++k) {
+      const int vi = lane + 32 * k;   // 16 kMT voxels x VPV vectors
+      const int j = vi / VPV, part = vi - VPV * j;
+      if (x0 + j < nx) *reinterpret_cast<uint4*>(a.out + (row0 + j) * a.out_cs + 8 * part) = sv[vi];
+    }
+  }
 }
 
 // Weight gradient dW[t][ci][co] = Σ_v x[src(v,t)][ci] dy[v][co]: an MMA with
@@ -263,6 +284,115 @@ __global__ void frag_kernel(int kind, int cin, int cout, const float* __restrict
   }
 }
 
+// UP (2x2x2 transposed, stride 2) with coalesced stores: one warp takes 32
+// consecutive coarse voxels of a coarse row and one (py, pz) parity pair, and
+// computes both x parities, so the 64 fine voxels it produces are adjacent in
+// the fine row (2y + py, 2z + pz).  They are staged in shared memory and
+// written as 16-byte vectors (a voxel's COUT channels are contiguous).
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kWarps * 32) up_kernel(ConvArgs a) {
+  constexpr int NB = COUT / 8, KS = CIN / 16, VPV = COUT / 8;   // 16-byte vectors per fine voxel
+  __shared__ __align__(16) __nv_bfloat16 stile[kWarps][64 * COUT];
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3, warp = threadIdx.x >> 5;
+  const int nx = a.n_in;
+  const int chunks = (nx + 31) / 32;
+  const long long task = (long long)blockIdx.x * kWarps + warp;
+  if (task >= (long long)chunks * nx * nx * 4) return;   // warp-uniform; no block barrier below
+  const int cx = (int)(task % chunks);
+  long long r = task / chunks;
+  const int y = (int)(r % nx);
+  r /= nx;
+  const int z = (int)(r % nx);
+  const int pyz = (int)(r / nx), py = pyz & 1, pz = pyz >> 1;
+  const int x0 = 32 * cx;
+  float acc[2][2][NB][4];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int px = 0; px < 2; ++px)
+#pragma unroll
+      for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[m][px][b][e] = 0.0f;
+  const uint32_t* rows[2][2];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int x = x0 + 16 * m + g + 8 * h;
+      rows[m][h] = x < nx ? reinterpret_cast<const uint32_t*>(a.in + vox(nx, x, y, z) * a.in_cs) : nullptr;
+    }
+#pragma unroll
+  for (int ks = 0; ks < KS; ++ks) {
+    uint32_t av[2][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const uint32_t* p0 = rows[m][0];
+      const uint32_t* p1 = rows[m][1];
+      const int o = 8 * ks;
+      av[m][0] = p0 ? __ldg(p0 + o + q) : 0u;
+      av[m][1] = p1 ? __ldg(p1 + o + q) : 0u;
+      av[m][2] = p0 ? __ldg(p0 + o + 4 + q) : 0u;
+      av[m][3] = p1 ? __ldg(p1 + o + 4 + q) : 0u;
+    }
+#pragma unroll
+    for (int px = 0; px < 2; ++px) {
+      const int t = px + 2 * py + 4 * pz;
+#pragma unroll
+      for (int nb = 0; nb < NB; ++nb) {
+        const uint2 b = __ldg(a.w + ((size_t)(t * KS + ks) * NB + nb) * 32 + lane);
+#pragma unroll
+        for (int m = 0; m < 2; ++m) mma16(acc[m][px][nb], av[m][0], av[m][1], av[m][2], av[m][3], b.x, b.y);
+      }
+    }
+  }
+  // epilogue into the staging tile: fine-local voxel j = 2 (16 m + g + 8 h) + px
+  const int fy = 2 * y + py, fz = 2 * z + pz, nf = a.n_out;
+  __nv_bfloat16* st = stile[warp];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int px = 0; px < 2; ++px) {
+        const int j = 2 * (16 * m + g + 8 * h) + px;
+        const int fx = 2 * x0 + j;
+#pragma unroll
+        for (int nb = 0; nb < NB; ++nb) {
+          const int n = 8 * nb + 2 * q;
+          float v0 = acc[m][px][nb][2 * h], v1 = acc[m][px][nb][2 * h + 1];
+          if (a.bias) { v0 += __ldg(a.bias + n); v1 += __ldg(a.bias + n + 1); }
+          if (a.add && fx < nf) {
+            const __nv_bfloat162 ad =
+                *reinterpret_cast<const __nv_bfloat162*>(a.add + vox(nf, fx, fy, fz) * a.add_cs + n);
+            v0 += __bfloat162float(ad.x);
+            v1 += __bfloat162float(ad.y);
+          }
+          if (a.relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+          *reinterpret_cast<__nv_bfloat162*>(st + j * COUT + n) = __floats2bfloat162_rn(v0, v1);
+        }
+      }
+  __syncwarp();
+  const uint4* sv = reinterpret_cast<const uint4*>(st);
+  const size_t row0 = vox(nf, 2 * x0, fy, fz);
+#pragma unroll
+  for (int k = 0; k < 2 * VPV; ++k) {
+    const int vi = lane + 32 * k;            // 64 voxels x VPV vectors
+    const int j = vi / VPV, part = vi - VPV * j;
+    if (2 * x0 + j < nf)
+      *reinterpret_cast<uint4*>(a.out + (row0 + j) * a.out_cs + 8 * part) = sv[vi];
+  }
+}
+
+template <int CIN, int COUT>
+cudaError_t up_t(cudaStream_t s, const ConvArgs& a) {
+  const int nx = a.n_in;
+  const long long ntask = (long long)((nx + 31) / 32) * nx * nx * 4;
+  const unsigned blocks = (unsigned)((ntask + kWarps - 1) / kWarps);
+  up_kernel<CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int KIND, int CIN, int COUT>
 cudaError_t fwd_t(cudaStream_t s, const ConvArgs& a) {
   const int nx = KIND == UP ? a.n_in : a.n_out;
@@ -288,6 +418,8 @@ cudaError_t wgrad_t(cudaStream_t s, const WgradArgs& a) {
 
 cudaError_t conv_forward(cudaStream_t s, int kind, int cin, int cout, const ConvArgs& a) {
   if (a.wimg && a.n_in == a.n_out && tc_supported(kind, cin, cout, a.n_out)) return conv_forward_tc(s, cin, cout, a);
+  if (kind == UP && cin == 32 && cout == 16) return up_t<32, 16>(s, a);
+  if (kind == UP && cin == 64 && cout == 32) return up_t<64, 32>(s, a);
 #define X(K, I, O) \
   if (kind == K && cin == I && cout == O) return fwd_t<K, I, O>(s, a);
   BAOREC_GUESS_SHAPES(X)
