@@ -26,16 +26,20 @@
 //                 (consecutive threads read consecutive bytes of the
 //                 channels-last activations), zero-filling the padding.
 //
-// Each CTA is persistent and walks "columns" (x segment, y, zc consecutive
-// z), marching in z.  Output row z needs input planes z-1, z, z+1 (taps
-// dz = 0, 1, 2), so plane p feeds rows p+1, p, p-1; the MMA multiplies each
-// slab ONCE by the three dz weight blocks side by side (N = 3*COUT, B image
-// [dx,dy][k chunk][dz][n]) and the three N blocks land in the accumulators
-// of those three rows.  A TMEM ring of kRing accumulators in descending-row
-// order makes the three blocks adjacent columns (split in two MMAs where
-// the ring wraps).  Every MMA accumulates: the ring starts at zero and the
-// epilogue zeroes an accumulator after reading it.  Each slab is read by the
-// tensor core once per (dx, dy, k step) and freed right after its MMAs.
+// Each CTA is persistent and walks "columns" (x segment, YR rows y0 ..
+// y0+YR-1, zc consecutive z), marching in z.  Output row z needs input
+// planes z-1, z, z+1 (taps dz = 0, 1, 2), so plane p feeds rows p+1, p, p-1;
+// the MMA multiplies each slab ONCE by the three dz weight blocks side by
+// side (N = 3*COUT, B image [dx,dy][k chunk][dz][n]) and the three N blocks
+// land in the accumulators of those three rows.  Each output row y0+yy has
+// a TMEM ring of kRing accumulators in descending-row order, so the three
+// blocks are adjacent columns; the ring is followed by kShadow extra slots,
+// where blocks past its end land, and the epilogue adds a shadow slot to
+// ring slot 0 or 1 (one contiguous MMA per tap instead of two where the
+// ring wraps: split MMAs cost several times a plain one on GB300).  Every
+// MMA accumulates: the ring starts at zero and the epilogue zeroes what it
+// reads.  A slab of YR+2 rows serves YR output rows (fewer TMA rows per
+// output), and is freed right after its MMAs.
 //
 // Measured on GB300 (M=128, K=16, one issuing thread): an MMA costs
 // max(~45, N/2) cycles whatever the smem layout or alignment, so N = 3*COUT
@@ -76,7 +80,9 @@ constexpr int kSmemMax = 232448;         // opt-in dynamic shared memory per blo
 constexpr int kSmemBudget = kSmemMax - 1024 - 512;
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait
 constexpr uint32_t kSuspendNs = 20000;   // suspend hint of one try_wait
-constexpr int kRing = 8;                 // TMEM accumulators (output rows in flight)
+constexpr int kRing = 6;                 // TMEM accumulators (output rows in flight) per output-row ring
+constexpr int kShadow = 2;               // shadow slots past a ring's end: the MMA never wraps
+constexpr int kCols = kRing + kShadow;   // slots of TMEM columns per ring
 
 template <int CIN, int COUT>
 struct Tc {
@@ -97,14 +103,14 @@ struct Tc {
   }
   // the most rows whose accumulator rings fit the 512 TMEM columns and whose
   // slabs still leave a ring of two in shared memory
-  static constexpr int YR = (4 * kRing * COUT <= 512 && s_of(4) >= 2) ? 4
-                            : (2 * kRing * COUT <= 512 && s_of(2) >= 2) ? 2 : 1;
+  static constexpr int YR = (4 * kCols * COUT <= 512 && s_of(4) >= 2) ? 4
+                            : (2 * kCols * COUT <= 512 && s_of(2) >= 2) ? 2 : 1;
   static constexpr int BOX = (YR + 2) * kRowBytes;   // bytes one TMA box delivers
   static constexpr int PLANE = plane_of(YR);
   static constexpr int SLAB = CH * PLANE;
   static constexpr int S = s_of(YR);                 // slab ring depth
   static constexpr int SMEM = WB + S * SLAB + 1024;  // + alignment slack
-  static constexpr int TCOLS = YR * kRing * COUT;    // TMEM columns: one accumulator ring per output row
+  static constexpr int TCOLS = YR * kCols * COUT;    // TMEM columns: one accumulator ring per output row
   // S >= 2: a slab is freed as soon as its own MMAs complete, so the loader
   // refills one slot while the MMAs read the other
   static_assert(S >= 2, "slab ring too shallow for this shape");
@@ -502,37 +508,25 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           const int dz_hi = p < 2 ? p : 2;
           const int nd = dz_hi - dz_lo + 1;
           const int s_lo = acc_slot(i0 + p - dz_lo);
-          const int n1 = nd < kRing - s_lo ? nd : kRing - s_lo;   // blocks before the ring wraps
-          const int n2 = nd - n1;
-          const uint32_t id1 = idesc0 | ((uint32_t)(n1 * COUT >> 3) << 17);
-          const uint32_t id2 = idesc0 | ((uint32_t)(n2 * COUT >> 3) << 17);
+          // the nd blocks occupy slots s_lo .. s_lo+nd-1 <= kRing+1: past the
+          // ring's end they land in its shadow slots, which the epilogue adds
+          // to slots 0 and 1; every MMA is one contiguous N = nd*COUT
+          const uint32_t id = idesc0 | ((uint32_t)(nd * COUT >> 3) << 17);
           // descriptors are linear in the start address (14-bit field, smem
           // below 256 KB): per MMA only compile-time offsets are added
           const uint64_t a_base = sdesc(ssm + (uint32_t)slot * P::SLAB, P::PAIRED ? 16u : (uint32_t)P::PLANE, 128);
-          const uint64_t b_base1 = sdesc(wsm + (uint32_t)dz_lo * kBlk, kLboB, 128);
-          const uint64_t b_base2 = sdesc(wsm + (uint32_t)(dz_lo + n1) * kBlk, kLboB, 128);
+          const uint64_t b_base = sdesc(wsm + (uint32_t)dz_lo * kBlk, kLboB, 128);
           // output row y0 + yy reads slab rows yy .. yy+2 and accumulates in
-          // its own ring (TMEM columns yy*kRing*COUT ..)
+          // its own ring (TMEM columns yy*kCols*COUT ..)
 #pragma unroll
           for (int yy = 0; yy < YR; ++yy) {
-            const uint32_t ring = tm + (uint32_t)(yy * kRing * COUT);
-            const uint32_t d1 = ring + (uint32_t)(s_lo * COUT), d2 = ring;
+            const uint32_t d = tm + (uint32_t)((yy * kCols + s_lo) * COUT);
             const uint64_t a_row = a_base + (uint64_t)((yy * kRowBytes) >> 4);
-            if (n2 == 0) {
 #pragma unroll
-              for (int k = 0; k < P::NMMA; ++k) {
-                const uint64_t ad = a_row + a_off<P::PAIRED, P::KS, P::PLANE>(k);
-                const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
-                mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
-              }
-            } else {
-#pragma unroll
-              for (int k = 0; k < P::NMMA; ++k) {
-                const uint64_t ad = a_row + a_off<P::PAIRED, P::KS, P::PLANE>(k);
-                const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
-                mma_bf16(d1, ad, b_base1 + bo, id1, 1u);
-                mma_bf16(d2, ad, b_base2 + bo, id2, 1u);
-              }
+            for (int k = 0; k < P::NMMA; ++k) {
+              const uint64_t ad = a_row + a_off<P::PAIRED, P::KS, P::PLANE>(k);
+              const uint64_t bo = (uint64_t)((k * 2 * kLboB) >> 4);
+              mma_bf16(d, ad, b_base + bo, id, 1u);
             }
           }
           mma_commit(smem_u32(&bar_empty[slot]));
@@ -568,12 +562,21 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         tc_fence_after();
 #pragma unroll 1
         for (int yy = 0; yy < YR; ++yy) {
-          const uint32_t acc = lane_addr + (uint32_t)((yy * kRing + s) * COUT);
+          const uint32_t acc = lane_addr + (uint32_t)((yy * kCols + s) * COUT);
           float v[COUT];
           tmem_ld_row<COUT>(acc, v);
           // zero the accumulator for its next row; the wait comes after the stores
 #pragma unroll
           for (int c = 0; c < COUT; c += 16) tmem_zero16(acc + (uint32_t)c);
+          if (s < kShadow) {   // the part that landed past the ring's end
+            const uint32_t sh = lane_addr + (uint32_t)((yy * kCols + kRing + s) * COUT);
+            float w[COUT];
+            tmem_ld_row<COUT>(sh, w);
+#pragma unroll
+            for (int c = 0; c < COUT; ++c) v[c] += w[c];
+#pragma unroll
+            for (int c = 0; c < COUT; c += 16) tmem_zero16(sh + (uint32_t)c);
+          }
           const size_t vo = ((size_t)(t.z0 + zl) * n + (t.y + yy)) * n + (t.x0 + m);
           if (a.bias) {
 #pragma unroll

@@ -90,7 +90,10 @@ def test_conv3_tcgen05_matches_fp64_and_mma(cin, cout):
         tol = 2.0 ** -8 * np.abs(ref) + 1e-4
         assert np.all(np.abs(got - ref) <= tol), (path, float(np.max(np.abs(got - ref) - tol)))
         d = np.abs(y_tc - y_mma)
-        step = 2.0 ** -7 * np.maximum(np.abs(y_tc), np.abs(y_mma)) + 1e-6
+        # one BF16 step, plus the FP32 reassociation error of a 27*cin-term
+        # sum that cancels to a small output (the tensor core adds partial
+        # accumulators in another order than the mma.sync kernel)
+        step = 2.0 ** -7 * np.maximum(np.abs(y_tc), np.abs(y_mma)) + 1e-5
         assert np.all(d <= step), (path, float(np.max(d - step)))
         assert np.mean(d == 0) > 0.98, (path, np.mean(d == 0))
         outs[path] = y_tc
