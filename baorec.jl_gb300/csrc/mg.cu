@@ -81,6 +81,13 @@ __global__ void add_kernel(float* __restrict__ a, const float* __restrict__ b, s
     a[e] += b[e];
 }
 
+// r = f - shift: the residual of a zero solution, as the accurate residual
+// kernel would compute it ((f - α) + a bracket of zero differences).
+__global__ void shift_kernel(const float* __restrict__ f, float* __restrict__ r, float shift, size_t N) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    r[e] = f[e] - shift;
+}
+
 // Full-weighting restriction (src/multigrid.jl:586-640): coarse c centred on fine 2c+1.
 __global__ void reduce_kernel(const float* __restrict__ fine, float* __restrict__ coarse, int3 nf, int3 nc,
                               size_t Nc) {
@@ -741,6 +748,10 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   if (phi0 && phi0 != phi) CK(cudaMemcpyAsync(hiA, phi0, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
   if (!phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED) CKS(guess_apply(ctx, f, hiA));
   else if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
+  // The first residual of a zero solution needs no stencil: r = f - α with
+  // α = mean f, so Σr = 0 and |r| = |f - α| (relative residual 1), and the
+  // solution pair stays zero.
+  const bool zero_start = !phi0 && ctx->cfg.mg_start != BAOREC_START_LEARNED;
   CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
   double alpha = sf / (double)N;
   LG G = level_geom(ctx, 0, 0.0f);
@@ -764,47 +775,54 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   bool spectral = ctx->cfg.mg_start != BAOREC_START_ZERO;
   int nspec = 0, m_last = 0;
   double rho_prev = 0.0, rate = 0.0;
+  const double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;   // |f - α|² at the initial α
   for (int it = 0;; ++it) {
-    if (stream0) {
-      CK(launch_resid_acc_stream(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
-                                 ctx->dred, &nparts));
-      ctx->launches++;
-    } else if (tile0) {
-      CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
-                          ctx->dred, &nparts));
-      ctx->launches++;
-    } else {
-      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
-                                                            G, N, (float)alpha, ctx->dred);
-      CKLAUNCH();
-    }
-    CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    // While the host reads the partial sums, the GPU already computes the
-    // first FFT correction of the next outer step, d_0 = S⁻¹ r, which needs
-    // nothing the host decides (it writes only the correction lev[0].v; a
-    // V-cycle zeroes that first).  Skipped when the last step's rate says
-    // this residual is already below rtol.
-    bool speculative = false;
-    if (spectral && nspec < ctx->cfg.max_cycles) {
-      const double predicted = m_last > 0 ? rho_prev * pow(std::max(rate, 0.0), (double)m_last) : 1.0;
-      speculative = !(m_last > 0 && rate > 0.0 && predicted <= (double)ctx->cfg.rtol);
-    }
-    if (speculative) {
-      if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
-      CK(cudaEventRecord(ctx->ev_red, ctx->stream));
-      CKS(spectral_correction(ctx, L0.f, L0.v));
-      CK(cudaEventSynchronize(ctx->ev_red));
-    } else {
-      CK(cudaStreamSynchronize(ctx->stream));
-    }
     double s1 = 0.0, s2 = 0.0;
-    for (int q = 0; q < nparts; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
-    double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;
-    rho = fn2 > 0.0 ? sqrt(s2 / fn2) : 0.0;
+    bool speculative = false;
+    if (it == 0 && zero_start) {
+      shift_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(f, L0.f, (float)alpha, N);
+      CKLAUNCH();
+      s2 = fn2;
+    } else {
+      if (stream0) {
+        CK(launch_resid_acc_stream(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
+                                   ctx->dred, &nparts));
+        ctx->launches++;
+      } else if (tile0) {
+        CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
+                            ctx->dred, &nparts));
+        ctx->launches++;
+      } else {
+        resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
+                                                              G, N, (float)alpha, ctx->dred);
+        CKLAUNCH();
+      }
+      CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      // While the host reads the partial sums, the GPU already computes the
+      // first FFT correction of the next outer step, d_0 = S⁻¹ r, which needs
+      // nothing the host decides (it writes only the correction lev[0].v; a
+      // V-cycle zeroes that first).  Skipped when the last step's rate says
+      // this residual is already below rtol.
+      if (spectral && nspec < ctx->cfg.max_cycles) {
+        const double predicted = m_last > 0 ? rho_prev * pow(std::max(rate, 0.0), (double)m_last) : 1.0;
+        speculative = !(m_last > 0 && rate > 0.0 && predicted <= (double)ctx->cfg.rtol);
+      }
+      if (speculative) {
+        if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
+        CK(cudaEventRecord(ctx->ev_red, ctx->stream));
+        CKS(spectral_correction(ctx, L0.f, L0.v));
+        CK(cudaEventSynchronize(ctx->ev_red));
+      } else {
+        CK(cudaStreamSynchronize(ctx->stream));
+      }
+      for (int q = 0; q < nparts; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
+      { float* t = hiA; hiA = hiB; hiB = t; t = loA; loA = loB; loB = t; }
+    }
+    const double rn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;   // |f - α|² at the current α
+    rho = rn2 > 0.0 ? sqrt(s2 / rn2) : 0.0;
     if (it == 0) rho0 = rho;
     ctx->hist_rho.push_back(rho);
     ctx->hist_kind.push_back(-1);
-    { float* t = hiA; hiA = hiB; hiB = t; t = loA; loA = loB; loB = t; }
     if (!(rho == rho)) { status = set_error(ctx, BAOREC_ERR_NOT_CONVERGED, "multigrid solve produced NaN"); break; }
     if (rho <= (double)ctx->cfg.rtol) { status = BAOREC_OK; break; }
     if (cycles >= ctx->cfg.max_cycles) {

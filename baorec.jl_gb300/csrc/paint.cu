@@ -9,6 +9,28 @@
 namespace baorec {
 namespace {
 
+// Adds a to cell x0 and b to cell x1 of the mesh row starting at `row`.  With
+// VEC (16-byte aligned rows) a pair x1 = x0 + 1 inside one aligned group of
+// four cells is one 16-byte vector reduction (the other two lanes add +0,
+// which leaves every cell unchanged): 5 reductions per particle on average
+// instead of 8.
+template <bool VEC>
+__device__ __forceinline__ void red_pair(float* __restrict__ row, int x0, int x1, float a, float b) {
+  const int k = x0 & 3;
+  if (VEC && x1 == x0 + 1 && k != 3) {
+    float4 v;
+    v.x = k == 0 ? a : 0.0f;
+    v.y = k == 0 ? b : (k == 1 ? a : 0.0f);
+    v.z = k == 1 ? b : (k == 2 ? a : 0.0f);
+    v.w = k == 2 ? b : 0.0f;
+    atomicAdd(reinterpret_cast<float4*>(row + (x0 - k)), v);
+  } else {
+    atomicAdd(row + x0, a);
+    atomicAdd(row + x1, b);
+  }
+}
+
+template <bool VEC>
 __global__ void cic_paint_kernel(float* __restrict__ mesh, float* __restrict__ x, float* __restrict__ y,
                                  float* __restrict__ z, const float* __restrict__ w, int64_t n,
                                  PaintGeom g, int writeback, unsigned* err) {
@@ -30,14 +52,14 @@ __global__ void cic_paint_kernel(float* __restrict__ mesh, float* __restrict__ x
     wx1 = __fmul_rn(wx1, wt);
     float wy0 = __fsub_rn(1.0f, wy1), wz0 = __fsub_rn(1.0f, wz1);
     x0--; x1--; y0--; y1--; z0--; z1--;
-    atomicAdd(mesh + lin(x0, y0, z0, g), __fmul_rn(__fmul_rn(wx0, wy0), wz0));
-    atomicAdd(mesh + lin(x1, y0, z0, g), __fmul_rn(__fmul_rn(wx1, wy0), wz0));
-    atomicAdd(mesh + lin(x0, y1, z0, g), __fmul_rn(__fmul_rn(wx0, wy1), wz0));
-    atomicAdd(mesh + lin(x0, y0, z1, g), __fmul_rn(__fmul_rn(wx0, wy0), wz1));
-    atomicAdd(mesh + lin(x1, y1, z0, g), __fmul_rn(__fmul_rn(wx1, wy1), wz0));
-    atomicAdd(mesh + lin(x1, y0, z1, g), __fmul_rn(__fmul_rn(wx1, wy0), wz1));
-    atomicAdd(mesh + lin(x0, y1, z1, g), __fmul_rn(__fmul_rn(wx0, wy1), wz1));
-    atomicAdd(mesh + lin(x1, y1, z1, g), __fmul_rn(__fmul_rn(wx1, wy1), wz1));
+    red_pair<VEC>(mesh + lin(0, y0, z0, g), x0, x1, __fmul_rn(__fmul_rn(wx0, wy0), wz0),
+                  __fmul_rn(__fmul_rn(wx1, wy0), wz0));
+    red_pair<VEC>(mesh + lin(0, y1, z0, g), x0, x1, __fmul_rn(__fmul_rn(wx0, wy1), wz0),
+                  __fmul_rn(__fmul_rn(wx1, wy1), wz0));
+    red_pair<VEC>(mesh + lin(0, y0, z1, g), x0, x1, __fmul_rn(__fmul_rn(wx0, wy0), wz1),
+                  __fmul_rn(__fmul_rn(wx1, wy0), wz1));
+    red_pair<VEC>(mesh + lin(0, y1, z1, g), x0, x1, __fmul_rn(__fmul_rn(wx0, wy1), wz1),
+                  __fmul_rn(__fmul_rn(wx1, wy1), wz1));
   }
 }
 
@@ -133,8 +155,10 @@ int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const floa
   int wb = (flags & BAOREC_WRITEBACK) ? 1 : 0;
   if (mas == BAOREC_MAS_TSC)
     tsc_paint_kernel<<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
+  else if (g.n[0] % 4 == 0 && (uintptr_t)mesh % 16 == 0)
+    cic_paint_kernel<true><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
   else
-    cic_paint_kernel<<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
+    cic_paint_kernel<false><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
   CKLAUNCH();
   return BAOREC_OK;
 }

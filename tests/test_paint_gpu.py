@@ -108,6 +108,25 @@ def test_cic_device_arrays():
     np.testing.assert_allclose(rho.cpu().numpy(), orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
 
 
+@pytest.mark.parametrize("shape", [(36, 30, 32), (30, 32, 28), (4, 8, 8)])
+def test_cic_vector_and_scalar_reductions(shape):
+    """x rows of a multiple of 4 cells take the 16-byte vector reductions
+    (pairs inside an aligned group of four), others the scalar ones; every
+    x residue is hit, including the pair that wraps from n-1 to 0."""
+    import baorec
+    npart = 60000
+    L = [F32(300.0), F32(250.0), F32(200.0)]
+    rng = np.random.default_rng(sum(shape))
+    x, y, z = [(rng.random(npart) * float(L[a])).astype(F32) for a in range(3)]
+    for p, l in zip((x, y, z), L):
+        p[p >= l] = F32(0.0)
+    w = (0.5 + rng.random(npart)).astype(F32)
+    rho = baorec.zeros_mesh(shape, device=False)
+    baorec.cic_(rho, x.copy(), y.copy(), z.copy(), w, L, [0.0] * 3, wrap=True)
+    orho, _ = O.cic(np.zeros(shape, F32), x, y, z, w, L, [0.0] * 3, wrap=True)
+    np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
+
+
 @pytest.mark.parametrize("wrap", [True, False])
 def test_tsc_matches_oracle(wrap):
     import baorec
