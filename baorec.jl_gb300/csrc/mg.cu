@@ -305,6 +305,7 @@ LG level_geom(const baorec_ctx* ctx, int l, float clamp) {
   G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
   G.clamp = clamp;
   G.tile16 = l < 16 ? ctx->tune.big_tiles[l] : -1;
+  G.pairs = ctx->tune.pairs;
   return G;
 }
 

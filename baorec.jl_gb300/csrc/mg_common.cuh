@@ -16,6 +16,7 @@ struct LG {                           // level geometry passed to kernels
   int local;
   float clamp;                        // > 0: clamp derivative coefficients
   int tile16;                         // tile kernels: -1 heuristic, 0 = 32x8x8, 1 = 32x16x16 tiles
+  int pairs;                          // running residual on 32x16x16 tiles: 1 = two z-cells per thread, packed
 };
 
 struct Coef {

@@ -387,6 +387,143 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
 // becomes the updated double-float pair as it is loaded, held as interleaved
 // (hi, lo) pairs (one 8-byte shared load per neighbour and one packed
 // subtraction give both parts of a difference); then
+// The FP32 running residual of the FFT corrections on 32 x 16 x 16 tiles, two
+// z-adjacent cells per thread in packed FP32x2 arithmetic:
+//   r = (rhs - shift) + bracket(e_nb - e_0),  acc += e  (optional).
+// The window is stored as plane pairs: pair j interleaves window planes 2j
+// and 2j+1 per cell, so one 8-byte shared load at an in-plane offset gives a
+// cell column's values in two planes.  A thread computes window planes 2k+1
+// (cell A) and 2k+2 (cell B); pairs k and k+1 at the nine in-plane offsets
+// hold every value of both stencils: the z-1 and z+1 values of (A, B) are
+// the pairs themselves, the in-plane values one register move from a pair.
+// Warp w computes window row y = 1 + w, lane l column x = XH + l.
+template <bool LOCAL>
+__global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
+                                                          float* __restrict__ r, LG G, float shift,
+                                                          float* __restrict__ acc) {
+  constexpr int TY = 16, TZ = 16, SY = TY + 2, SZ = TZ + 2;
+  constexpr int NPR = SZ / 2;        // plane pairs in the window
+  constexpr int PR = 2 * WX;         // floats per row of a plane pair
+  constexpr int PP = SY * PR;        // floats per plane pair
+  constexpr int NK = TZ / 2;         // output pairs per thread
+  static_assert(NWARP == TY, "one warp per output row");
+  extern __shared__ __align__(16) float smem[];
+  float* sw = smem;
+  int* ro = reinterpret_cast<int*>(sw + NPR * PP);
+  float* sp = reinterpret_cast<float*>(ro + SY * SZ);
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ly = 1 + warp, lx = XH + lane;
+  const size_t plane = (size_t)G.n[0] * G.n[1];
+  const size_t col = (size_t)(y0 + warp) * G.n[0] + x0 + lane;   // (x, y) of the thread's cells at z = 0
+  // right-hand side (and acc) of the thread's cells: pair k in (r0, a0), pair
+  // k + 1 in (r1, a1), loaded two pairs ahead of use
+  float r0[2] = {0.0f, 0.0f}, r1[2] = {0.0f, 0.0f}, a0[2] = {0.0f, 0.0f}, a1[2] = {0.0f, 0.0f};
+  auto issue = [&](int k, float* rr, float* aa) {
+    if (k < NK) {
+      const size_t o = col + (size_t)(z0 + 2 * k) * plane;
+      rr[0] = __ldg(rhs + o);
+      rr[1] = __ldg(rhs + o + plane);
+      if (acc) { aa[0] = acc[o]; aa[1] = acc[o + plane]; }
+    }
+  };
+  issue(0, r0, a0);
+  issue(1, r1, a1);
+  row_table<1, TY, TZ>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  __syncthreads();
+  {
+    constexpr int TOT = NPR * SY * CH;
+    constexpr int K = (TOT + NT - 1) / NT, B = K;   // every chunk of the thread in flight at once
+#pragma unroll
+    for (int k0 = 0; k0 < K; k0 += B) {
+      float4 a[B], b[B];
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int t = threadIdx.x + (k0 + i) * NT;
+        if (k0 + i < K && t < TOT) {
+          const int row = t / CH, c = t - CH * row;   // row = pair * SY + y
+          const int j = row / SY, yy = row - SY * j;
+          const int xo = wrapi(x0 - XH + 4 * c, G.n[0]);
+          a[i] = __ldg(reinterpret_cast<const float4*>(e + ro[yy + SY * (2 * j)] + xo));
+          b[i] = __ldg(reinterpret_cast<const float4*>(e + ro[yy + SY * (2 * j + 1)] + xo));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int t = threadIdx.x + (k0 + i) * NT;
+        if (k0 + i < K && t < TOT) {
+          const int row = t / CH, c = t - CH * row;
+          float4* d = reinterpret_cast<float4*>(sw + row * PR + 8 * c);
+          d[0] = make_float4(a[i].x, b[i].x, a[i].y, b[i].y);
+          d[1] = make_float4(a[i].z, b[i].z, a[i].w, b[i].w);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1];
+  const float px2 = px * px, py2 = py * py;
+  const float dxy = G.cell2[0] * px2 + G.cell2[1] * py2;
+  auto L = [&](int q) { return *reinterpret_cast<const f2*>(sw + q); };
+  // (second plane of pair a, first plane of pair b): the in-plane values of (A, B)
+  auto C = [](f2 a, f2 b) {
+    float a0, a1, b0, b1;
+    U2(a, a0, a1);
+    U2(b, b0, b1);
+    return P2(a1, b0);
+  };
+  constexpr int OX = 2, OY = PR;
+#pragma unroll 1
+  for (int k = 0; k < NK; ++k) {
+    const float rA = r0[0], rB = r0[1], aA = a0[0], aB = a0[1];
+    r0[0] = r1[0]; r0[1] = r1[1]; a0[0] = a1[0]; a0[1] = a1[1];
+    issue(k + 2, r1, a1);
+    const f2 Pz = LOCAL ? P2(sp[2 * WX + 2 * k + 1], sp[2 * WX + 2 * k + 2]) : B2(G.pg[2]);
+    const f2 pz2 = mul2(Pz, Pz);
+    float dA, dB;
+    U2(fma2(B2(G.cell2[2]), pz2, B2(dxy)), dA, dB);
+    const f2 g = P2(__fdividef(G.beta, dA), __fdividef(G.beta, dB));
+    const f2 gpz = fma2(g, pz2, B2(G.icell2[2]));
+    const f2 hg = mul2(B2(0.5f), g);
+    const int q0 = (k * SY + ly) * PR + 2 * lx, q1 = q0 + PP;   // pairs k and k + 1 at (y, x)
+    // (A, B) one plane down is pair k, one plane up pair k + 1
+    const f2 zm = L(q0), zp = L(q1);
+    const f2 s0 = C(zm, zp);
+    f2 o = mul2(gpz, add2(sub2(zp, s0), sub2(zm, s0)));
+    if (LOCAL) o = fma2(mul2(g, Pz), sub2(zp, zm), o);
+    {   // x neighbours and the x-z diagonals
+      const f2 kp = L(q0 + OX), km = L(q0 - OX), lp = L(q1 + OX), lm = L(q1 - OX);
+      const f2 xp = C(kp, lp), xm = C(km, lm);
+      o = fma2(fma2(g, B2(px2), B2(G.icell2[0])), add2(sub2(xp, s0), sub2(xm, s0)), o);
+      o = fma2(mul2(hg, mul2(B2(px), Pz)), sub2(add2(sub2(lp, s0), sub2(km, s0)), add2(sub2(lm, s0), sub2(kp, s0))), o);
+      if (LOCAL) o = fma2(mul2(g, B2(px)), sub2(xp, xm), o);
+    }
+    {   // y neighbours and the y-z diagonals
+      const f2 kp = L(q0 + OY), km = L(q0 - OY), lp = L(q1 + OY), lm = L(q1 - OY);
+      const f2 yp = C(kp, lp), ym = C(km, lm);
+      o = fma2(fma2(g, B2(py2), B2(G.icell2[1])), add2(sub2(yp, s0), sub2(ym, s0)), o);
+      o = fma2(mul2(hg, mul2(B2(py), Pz)), sub2(add2(sub2(lp, s0), sub2(km, s0)), add2(sub2(lm, s0), sub2(kp, s0))), o);
+      if (LOCAL) o = fma2(mul2(g, B2(py)), sub2(yp, ym), o);
+    }
+    {   // x-y diagonals (in-plane)
+      const f2 pp = C(L(q0 + OX + OY), L(q1 + OX + OY)), mm = C(L(q0 - OX - OY), L(q1 - OX - OY));
+      const f2 mp = C(L(q0 - OX + OY), L(q1 - OX + OY)), pm = C(L(q0 + OX - OY), L(q1 + OX - OY));
+      o = fma2(mul2(hg, B2(px * py)), sub2(add2(sub2(pp, s0), sub2(mm, s0)), add2(sub2(mp, s0), sub2(pm, s0))), o);
+    }
+    float oA, oB, sA, sB;
+    U2(o, oA, oB);
+    U2(s0, sA, sB);
+    const size_t ga = col + (size_t)(z0 + 2 * k) * plane;
+    r[ga] = (rA - shift) + oA;
+    r[ga + plane] = (rB - shift) + oB;
+    if (acc) {
+      acc[ga] = aA + sA;
+      acc[ga + plane] = aB + sB;
+    }
+  }
+}
+
 // r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
 // operator, whose coefficients are evaluated with IEEE round-to-nearest
 // operations in the reference's order.  Per-block (Σr, Σr²) to part.
@@ -558,6 +695,16 @@ cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   return cudaGetLastError();
 }
 
+template <bool LOCAL>
+cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+  auto k = resid_pairs_kernel<LOCAL>;
+  constexpr size_t b = win_bytes<1, 16, 16>(1);
+  cudaError_t e = allow_smem(k, b);
+  if (e != cudaSuccess) return e;
+  k<<<grid_of<16, 16>(G.n), NT, b, s>>>(ec, rhs, r, G, 0.0f, acc);
+  return cudaGetLastError();
+}
+
 template <bool LOCAL, int TY, int TZ>
 cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f, float* ohi,
                   float* olo, float* r, const LG& G, float alpha, double* part) {
@@ -603,6 +750,7 @@ cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, floa
 
 cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
   const bool big = big_tiles(G);
+  if (big && G.pairs) return G.local ? pairs_t<true>(s, ec, rhs, r, G, acc) : pairs_t<false>(s, ec, rhs, r, G, acc);
   if (!G.local)
     return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
                : resid_t<false, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);

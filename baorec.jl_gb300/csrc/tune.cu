@@ -2,7 +2,9 @@
 // candidates on the context's own meshes with CUDA events.
 //   stencil: per multigrid level, 32x8x8 or 32x16x16 tiles for the tile
 //            kernels (sweep; at the finest level also the accurate and the
-//            running residual), where both are valid;
+//            running residual), where both are valid; at the finest level
+//            also the streaming against the tiled residual kernels and the
+//            running residual with two z-cells per thread against one;
 //   paint:   the tile edge (4, 8 or 16 cells) of the deterministic paint,
 //            on 2^21 uniform particles in the box.
 // Choices live in ctx->tune and apply to every later launch of the context.
@@ -111,6 +113,23 @@ int tune_stencils(baorec_ctx* ctx) {
     }
     ctx->tune.stream0 = ms[1] <= ms[0] ? 1 : 0;
   }
+  // finest level: the tiled running residual with two z-adjacent cells per
+  // thread (packed FP32x2) against one cell per thread
+  if (nl > 0 && tile_ok(L0.n)) {
+    float* t = L0.r + L0.N;
+    float ms[2] = {0.0f, 0.0f};
+    for (int form = 0; form < 2; ++form) {
+      ctx->tune.pairs = form;
+      const LG G0 = level_geom_public(ctx, 0, 0.0f);
+      auto launch = [&]() -> int {
+        CK(launch_resid_diff(ctx->stream, L0.v, L0.f, t, G0, L0.r));
+        return BAOREC_OK;
+      };
+      CKS(time_ms(ctx, launch, 10, &ms[form]));
+      ctx->launches += 11;
+    }
+    ctx->tune.pairs = ms[1] <= ms[0] ? 1 : 0;
+  }
   return BAOREC_OK;
 }
 
@@ -152,6 +171,14 @@ extern "C" int baorec_tune_stream(const baorec_ctx* ctx) { return ctx ? ctx->tun
 extern "C" int baorec_set_tune_stream(baorec_ctx* ctx, int stream) {
   if (!ctx || stream < -1 || stream > 1) return BAOREC_ERR_ARG;
   ctx->tune.stream0 = stream;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_tune_pairs(const baorec_ctx* ctx) { return ctx ? ctx->tune.pairs : -1; }
+
+extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
+  if (!ctx || pairs < 0 || pairs > 1) return BAOREC_ERR_ARG;
+  ctx->tune.pairs = pairs;
   return BAOREC_OK;
 }
 

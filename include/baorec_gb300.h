@@ -481,6 +481,11 @@ int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tile
  * cp.async-pipelined), 0 tiled, -1 not tuned (streaming where the mesh allows). */
 int baorec_tune_stream(const baorec_ctx* ctx);
 int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
+/* FP32 running residual of the FFT corrections on 32x16x16 tiles: 1 two
+ * z-adjacent cells per thread in packed FP32x2 arithmetic (default), 0 one cell
+ * per thread.  The stencil autotune times both. */
+int baorec_tune_pairs(const baorec_ctx* ctx);
+int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
 
 /* ---- Catalog coordinates (examples/lightcone.jl:30-82) ------------------------
  * sky_to_cartesian (lightcone.jl:30-47): ra, dec in degrees and redshift z ->

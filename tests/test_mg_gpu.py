@@ -191,3 +191,33 @@ def test_zero_start_first_residual_is_exact_one(start):
     coef = O.coefs_f64(O.stencil_coefficients(f.shape, bs, bm, rec.beta, None, F32))
     r = (f.astype(np.float64) - st["alpha"]) - O.apply_operator(np.asarray(phi, np.float64), coef, True)
     assert np.linalg.norm(r) / np.linalg.norm(f.astype(np.float64) - st["alpha"]) < 2e-6
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.0, 1.0], [0.6, 0.0, 0.8]])
+def test_pair_and_single_cell_running_residuals_agree(los):
+    """The FP32 running residual on 32x16x16 tiles with two z-adjacent cells
+    per thread (packed FP32x2, plane-pair window) and with one cell per
+    thread: the same residual of the FFT start to FP32 rounding, the same
+    solve history and the same converged gradient."""
+    import ctypes as C
+    import baorec
+    f, bs, bm = _problem(n=64, seed=12)
+    ff = np.asfortranarray(f)
+    out = []
+    for pairs in (0, 1):
+        rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="spectral")
+        ctx = baorec.setup_fft_(rec, f.shape)
+        ctx.call("baorec_set_tune", 8, (C.c_int32 * 16)(*([1] * 16)))   # 16x16 tiles wherever they fit
+        ctx.call("baorec_set_tune_stream", 0)
+        ctx.call("baorec_set_tune_pairs", pairs)
+        assert ctx.lib.baorec_tune_pairs(ctx.h) == pairs
+        phi = baorec.zeros_mesh(f.shape, device=False)
+        st = baorec.solve_(phi, ff, rec)
+        assert st["rel_residual"] <= 1e-6
+        out.append((st, ctx.solve_history(), O.gradient_meshes(np.asarray(phi, np.float64), bs.astype(np.float64))))
+    (s0, h0, g0), (s1, h1, g1) = out
+    print(h0, h1)
+    assert [k for _, k in h0] == [k for _, k in h1]
+    for (r0, _), (r1, _) in zip(h0, h1):
+        assert abs(r0 - r1) <= 1e-3 * r0 + 1e-9
+    assert max(rel_l2(g1[a], g0[a]) for a in range(3)) < 1e-5
