@@ -136,6 +136,8 @@ _SIGS = {
     "baorec_set_tune_stream": (C.c_int, [P, C.c_int]),
     "baorec_tune_pairs": (C.c_int, [P]),
     "baorec_set_tune_pairs": (C.c_int, [P, C.c_int]),
+    "baorec_tune_zpass": (C.c_int, [P]),
+    "baorec_set_tune_zpass": (C.c_int, [P, C.c_int]),
     "baorec_sky_to_cartesian": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
                                           P, P, P, U32]),
     "baorec_cartesian_to_sky": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
@@ -269,7 +271,8 @@ class Context:
         self.call("baorec_autotune", (1 if stencil else 0) | (2 if paint else 0), C.byref(pt), bt)
         return {"paint_tile": pt.value, "tile16_per_level": list(bt),
                 "stream_residuals": int(self.lib.baorec_tune_stream(self.h)),
-                "pair_residual": int(self.lib.baorec_tune_pairs(self.h))}
+                "pair_residual": int(self.lib.baorec_tune_pairs(self.h)),
+                "fft_zpass": int(self.lib.baorec_tune_zpass(self.h))}
 
     def fft_callbacks(self) -> dict:
         """State of the FFT start's cuFFT load callback (baorec_fft_callbacks)."""

@@ -235,6 +235,9 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   for (cufftHandle p : plans)
     if (p) cufftDestroy(p);
   if (ctx->plan_c2r_spec) cufftDestroy(ctx->plan_c2r_spec);
+  if (ctx->plan_r2c_xy) cufftDestroy(ctx->plan_r2c_xy);
+  if (ctx->plan_c2r_xy) cufftDestroy(ctx->plan_c2r_xy);
+  cudaFree(ctx->xy_work);
   cudaFree(ctx->spec_work);
   cudaFree(ctx->spec_cb);
   cudaFree(ctx->fft_work);

@@ -62,6 +62,12 @@ struct baorec_ctx {
   void* spec_cb = nullptr;             // device copy of the callback's parameters
   void* spec_work = nullptr;           // its own work area when the shared one is too small
   char spec_cb_note[256] = "not requested (baorec_set_fft_callbacks)";
+  // FFT preconditioner over 256 z planes: batched 2-D transforms of the xy
+  // planes around one kernel doing the z transform, the k-space multiply and
+  // the inverse z transform (state 0 untried, 1 ready, -1 unavailable)
+  cufftHandle plan_r2c_xy = 0, plan_c2r_xy = 0;
+  void* xy_work = nullptr;             // their own work area when the shared one is too small
+  int xy_state = 0;
   // persistent meshes: mesh3 = three adjacent meshes A | B | C
   float* mesh3 = nullptr;
   float* result = nullptr;             // recon.result_cache (= A)
@@ -95,6 +101,7 @@ struct baorec_ctx {
     int paint_tile = 8;                // tile edge of the deterministic paint
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming
     int pairs = 1;                     // running residual on 32x16x16 tiles: 1 packed z-pairs, 0 one cell per thread
+    int zpass = 1;                     // FFT preconditioner: 1 xy transforms + fused z pass where n3 = 256, 0 3-D transforms
     int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1
     bool tuned = false;
   } tune;

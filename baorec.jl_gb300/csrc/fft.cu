@@ -518,6 +518,172 @@ __global__ void spectral_inverse_kernel(cufftComplex* __restrict__ a, SGeom g, c
   }
 }
 
+// ---- the preconditioner's z pass (n3 = 256) --------------------------------
+// After batched 2-D R2C transforms of the xy planes, a column (kx, ky) of the
+// spectrum holds its 256 z planes at a stride of one plane.  One kernel
+// transforms each column along z (four-step: 256 = 16 x 16, two 16-point
+// DFTs in registers with the 256-point twiddles between them, one shared-
+// memory exchange), multiplies by the preconditioner S⁻¹(k) and transforms
+// back the same way, so the multiply costs no pass of its own and the 3-D
+// transforms' z passes are replaced by one read and one write of the spectrum.
+constexpr int kZLen = 256;   // z planes the z pass transforms (16 x 16)
+constexpr int kZCols = 16;   // columns per block; thread (column c, row r) = (t & 15, t >> 4)
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulf_conj(float2 a, float2 b) {   // a * conj(b)
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// 4-point DFT in place, natural order; INV uses e^{+2πi/4}.
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 t0 = make_float2(a0.x + a2.x, a0.y + a2.y), t1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+  const float2 t2 = make_float2(a1.x + a3.x, a1.y + a3.y), d = make_float2(a1.x - a3.x, a1.y - a3.y);
+  const float2 t3 = INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);   // d · (±i)
+  a0 = make_float2(t0.x + t2.x, t0.y + t2.y);
+  a2 = make_float2(t0.x - t2.x, t0.y - t2.y);
+  a1 = make_float2(t1.x + t3.x, t1.y + t3.y);
+  a3 = make_float2(t1.x - t3.x, t1.y - t3.y);
+}
+
+// e^{∓2πi m/16} for the products m = b c (b, c in 1..3) of the 4 x 4 split.
+template <bool INV>
+__device__ __forceinline__ float2 w16(int m) {
+  constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f, h = 0.70710678118654752f;
+  float c = 1.0f, sn = 0.0f;
+  switch (m) {
+    case 1: c = c1; sn = s1; break;
+    case 2: c = h; sn = h; break;
+    case 3: c = s1; sn = c1; break;
+    case 4: c = 0.0f; sn = 1.0f; break;
+    case 6: c = -h; sn = h; break;
+    case 9: c = -c1; sn = -s1; break;
+    default: break;
+  }
+  return make_float2(c, INV ? sn : -sn);
+}
+
+// 16-point DFT in registers, natural order in and out:
+// v[k] <- Σ_n v[n] e^{∓2πi nk/16}; n = 4a + b, k = c + 4d.
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b) dft4<INV>(v[b], v[4 + b], v[8 + b], v[12 + b]);   // v[4c + b] = y_b[c]
+#pragma unroll
+  for (int b = 1; b < 4; ++b)
+#pragma unroll
+    for (int c = 1; c < 4; ++c) v[4 * c + b] = cmulf(v[4 * c + b], w16<INV>(b * c));
+#pragma unroll
+  for (int c = 0; c < 4; ++c) dft4<INV>(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);   // v[4c + d] = X[c + 4d]
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int d = c + 1; d < 4; ++d) {
+      const float2 q = v[4 * c + d];
+      v[4 * c + d] = v[4 * d + c];
+      v[4 * d + c] = q;
+    }
+}
+
+// a: n3 = 256 planes of ncols = n1h * n2 modes (column i + n1h j), transformed
+// over x and y; tw: e^{-2πi m/256}.  In place: a <- IFFT_z(S⁻¹ FFT_z(a)), with
+// S⁻¹ and the 1/N of the unnormalised transforms as spectral_inverse_kernel.
+__global__ void __launch_bounds__(256) zpass_precond_kernel(cufftComplex* __restrict__ a, SGeom g,
+                                                            const float* __restrict__ tab,
+                                                            const float2* __restrict__ tw, int ncols) {
+  __shared__ float2 s[kZCols][kZLen + 1];
+  __shared__ float2 w[kZLen];
+  const int t = threadIdx.x, cl = t & (kZCols - 1), r = t >> 4;
+  const int col = (int)blockIdx.x * kZCols + cl;
+  const bool ok = col < ncols;
+  w[t] = __ldg(tw + t);
+  float2* base = reinterpret_cast<float2*>(a) + (ok ? col : 0);
+  const size_t plane = (size_t)ncols;
+  float2 v[16];
+  // x[16 n1 + r], n1 = 0..15 -> Σ_n1 x[16 n1 + r] W16^{n1 k1}, times W256^{r k1}
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? base[(size_t)(16 * n1 + r) * plane] : make_float2(0.0f, 0.0f);
+  dft16<false>(v);
+  __syncthreads();
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) s[cl][16 * k1 + r] = cmulf(v[k1], w[r * k1]);
+  __syncthreads();
+  // row k1 = r: X[r + 16 k2] = Σ_n2 Y[r][n2] W16^{n2 k2}
+#pragma unroll
+  for (int n2 = 0; n2 < 16; ++n2) v[n2] = s[cl][16 * r + n2];
+  dft16<false>(v);
+  {
+    const float* hx2 = tab;
+    const float* sx = hx2 + g.n1h;
+    const float* hy2 = sx + g.n1h;
+    const float* sy = hy2 + g.n2;
+    const float* hz2 = sy + g.n2;
+    const float* sz = hz2 + g.n3;
+    const int cc = ok ? col : 0;
+    const int j = cc / g.n1h, i = cc - j * g.n1h;
+    const float hxi = __ldg(hx2 + i), sxi = __ldg(sx + i), hyj = __ldg(hy2 + j), syj = __ldg(sy + j);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+      const int k = r + 16 * k2;
+      const float szk = __ldg(sz + k);
+      const float A = g.diag[1] * hyj + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk + g.diag[0] * hxi +
+                      (g.cross[0] * syj + g.cross[1] * szk) * sxi;
+      const float sc = (k == 0 && j == 0 && i == 0) ? 0.0f : g.invN * __frcp_rn(A);
+      v[k2].x *= sc;
+      v[k2].y *= sc;
+    }
+  }
+  // inverse: Z[r][n2] = W256^{-n2 r} Σ_k2 X[r + 16 k2] W16^{-n2 k2}
+  dft16<true>(v);
+#pragma unroll
+  for (int n2 = 0; n2 < 16; ++n2) s[cl][16 * r + n2] = cmulf_conj(v[n2], w[n2 * r]);
+  __syncthreads();
+  // x[16 n1 + r] = Σ_k1 Z[k1][r] W16^{-n1 k1}
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) v[k1] = s[cl][16 * k1 + r];
+  dft16<true>(v);
+  if (ok) {
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) base[(size_t)(16 * n1 + r) * plane] = v[n1];
+  }
+}
+
+// Batched 2-D transforms of the n3 xy planes (R2C and C2R) for the z pass,
+// built at the first correction; any failure leaves the 3-D transforms in use.
+bool xy_plans(baorec_ctx* ctx) {
+  if (ctx->xy_state != 0) return ctx->xy_state == 1;
+  ctx->xy_state = -1;
+  long long dims[2] = {ctx->n2, ctx->n1};
+  const long long nr = (long long)ctx->n1 * ctx->n2, nc = (long long)ctx->n1h * ctx->n2;
+  cufftHandle p[2] = {0, 0};
+  size_t w[2] = {0, 0};
+  bool ok = cufftCreate(&p[0]) == CUFFT_SUCCESS && cufftCreate(&p[1]) == CUFFT_SUCCESS &&
+            cufftSetAutoAllocation(p[0], 0) == CUFFT_SUCCESS && cufftSetAutoAllocation(p[1], 0) == CUFFT_SUCCESS &&
+            cufftMakePlanMany64(p[0], 2, dims, nullptr, 1, nr, nullptr, 1, nc, CUFFT_R2C, ctx->n3, &w[0]) ==
+                CUFFT_SUCCESS &&
+            cufftMakePlanMany64(p[1], 2, dims, nullptr, 1, nc, nullptr, 1, nr, CUFFT_C2R, ctx->n3, &w[1]) ==
+                CUFFT_SUCCESS;
+  const size_t need = std::max(w[0], w[1]);
+  if (ok && need > ctx->fft_work_bytes) {
+    ok = cudaMalloc(&ctx->xy_work, need) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+  }
+  void* work = ctx->xy_work ? ctx->xy_work : ctx->fft_work;
+  for (int q = 0; q < 2 && ok; ++q)
+    ok = cufftSetWorkArea(p[q], work) == CUFFT_SUCCESS && cufftSetStream(p[q], ctx->stream) == CUFFT_SUCCESS;
+  if (!ok) {
+    for (int q = 0; q < 2; ++q)
+      if (p[q]) cufftDestroy(p[q]);
+    return false;
+  }
+  ctx->plan_r2c_xy = p[0];
+  ctx->plan_c2r_xy = p[1];
+  ctx->xy_state = 1;
+  return true;
+}
+
 int spectral_tables(baorec_ctx* ctx) {
   if (ctx->stab) return BAOREC_OK;
   const int n[3] = {ctx->n1, ctx->n2, ctx->n3};
@@ -534,6 +700,13 @@ int spectral_tables(baorec_ctx* ctx) {
     }
     t.insert(t.end(), h.begin(), h.end());
     t.insert(t.end(), sn.begin(), sn.end());
+  }
+  // e^{-2πi m/256}, m = 0..255, for the four-step z transform (8-byte aligned:
+  // the per-axis tables above hold an even number of floats)
+  for (int m = 0; m < kZLen; ++m) {
+    const double th = 2.0 * 3.14159265358979323846 * (double)m / (double)kZLen;
+    t.push_back((float)cos(th));
+    t.push_back((float)-sin(th));
   }
   CK(cudaMalloc(&ctx->stab, t.size() * sizeof(float)));
   CK(cudaMemcpy(ctx->stab, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -641,6 +814,15 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   SGeom g = sgeom_of(ctx);
   CKS(spectral_tables(ctx));
   if (ctx->spec_cb_state == 0) spectral_callback_plan(ctx);
+  if (ctx->spec_cb_state != 1 && ctx->tune.zpass && ctx->n3 == kZLen && xy_plans(ctx)) {
+    const int ncols = ctx->n1h * ctx->n2;
+    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)r, ctx->ck));
+    const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
+    zpass_precond_kernel<<<(ncols + kZCols - 1) / kZCols, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, tw, ncols);
+    CKLAUNCH();
+    CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck, e));
+    return BAOREC_OK;
+  }
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));
   if (ctx->spec_cb_state == 1) {
     SpecCallbackInfo info;

@@ -4,7 +4,9 @@
 //            kernels (sweep; at the finest level also the accurate and the
 //            running residual), where both are valid; at the finest level
 //            also the streaming against the tiled residual kernels and the
-//            running residual with two z-cells per thread against one;
+//            running residual with two z-cells per thread against one, and
+//            (n3 = 256) the FFT preconditioner's xy transforms + z pass
+//            against its 3-D transforms;
 //   paint:   the tile edge (4, 8 or 16 cells) of the deterministic paint,
 //            on 2^21 uniform particles in the box.
 // Choices live in ctx->tune and apply to every later launch of the context.
@@ -130,6 +132,18 @@ int tune_stencils(baorec_ctx* ctx) {
     }
     ctx->tune.pairs = ms[1] <= ms[0] ? 1 : 0;
   }
+  // FFT preconditioner: batched xy transforms around the fused z pass against
+  // 3-D transforms with a separate multiply (n3 = 256 only)
+  if (nl > 0 && ctx->n3 == 256) {
+    float ms[2] = {0.0f, 0.0f};
+    for (int form = 0; form < 2; ++form) {
+      ctx->tune.zpass = form;
+      auto launch = [&]() -> int { return spectral_correction(ctx, L0.f, L0.v); };
+      CKS(time_ms(ctx, launch, 5, &ms[form]));
+      ctx->launches += 6;
+    }
+    ctx->tune.zpass = ms[1] <= ms[0] ? 1 : 0;
+  }
   return BAOREC_OK;
 }
 
@@ -179,6 +193,14 @@ extern "C" int baorec_tune_pairs(const baorec_ctx* ctx) { return ctx ? ctx->tune
 extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
   if (!ctx || pairs < 0 || pairs > 1) return BAOREC_ERR_ARG;
   ctx->tune.pairs = pairs;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_tune_zpass(const baorec_ctx* ctx) { return ctx ? ctx->tune.zpass : -1; }
+
+extern "C" int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass) {
+  if (!ctx || zpass < 0 || zpass > 1) return BAOREC_ERR_ARG;
+  ctx->tune.zpass = zpass;
   return BAOREC_OK;
 }
 

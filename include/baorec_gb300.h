@@ -486,6 +486,12 @@ int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
  * per thread.  The stencil autotune times both. */
 int baorec_tune_pairs(const baorec_ctx* ctx);
 int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
+/* FFT preconditioner of the residual-driven solve where n[2] = 256: 1 batched
+ * 2-D transforms of the xy planes around one kernel that transforms along z,
+ * multiplies by S^-1(k) and transforms back (default), 0 3-D transforms with a
+ * separate multiply.  The stencil autotune times both. */
+int baorec_tune_zpass(const baorec_ctx* ctx);
+int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass);
 
 /* ---- Catalog coordinates (examples/lightcone.jl:30-82) ------------------------
  * sky_to_cartesian (lightcone.jl:30-47): ra, dec in degrees and redshift z ->
