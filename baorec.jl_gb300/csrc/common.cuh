@@ -101,7 +101,7 @@ struct baorec_ctx {
     int paint_tile = 8;                // tile edge of the deterministic paint
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming
     int pairs = 1;                     // running residual on 32x16x16 tiles: 1 packed z-pairs, 0 one cell per thread
-    int zpass = 1;                     // FFT preconditioner: 1 xy transforms + fused z pass where n3 = 256, 0 3-D transforms
+    int zpass = 1;                     // FFT preconditioner: 1 (2: capped registers) xy transforms + fused z pass where n3 = 256, 0 3-D transforms
     int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1
     bool tuned = false;
   } tune;

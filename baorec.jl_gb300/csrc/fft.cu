@@ -590,7 +590,8 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
 // a: n3 = 256 planes of ncols = n1h * n2 modes (column i + n1h j), transformed
 // over x and y; tw: e^{-2πi m/256}.  In place: a <- IFFT_z(S⁻¹ FFT_z(a)), with
 // S⁻¹ and the 1/N of the unnormalised transforms as spectral_inverse_kernel.
-__global__ void __launch_bounds__(256) zpass_precond_kernel(cufftComplex* __restrict__ a, SGeom g,
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) zpass_precond_kernel(cufftComplex* __restrict__ a, SGeom g,
                                                             const float* __restrict__ tab,
                                                             const float2* __restrict__ tw, int ncols) {
   __shared__ float2 s[kZCols][kZLen + 1];
@@ -818,7 +819,9 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
     const int ncols = ctx->n1h * ctx->n2;
     CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)r, ctx->ck));
     const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
-    zpass_precond_kernel<<<(ncols + kZCols - 1) / kZCols, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, tw, ncols);
+    // form 2 caps the registers for three resident blocks per SM instead of two
+    auto k = ctx->tune.zpass == 2 ? zpass_precond_kernel<3> : zpass_precond_kernel<1>;
+    k<<<(ncols + kZCols - 1) / kZCols, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, tw, ncols);
     CKLAUNCH();
     CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck, e));
     return BAOREC_OK;

@@ -135,14 +135,17 @@ int tune_stencils(baorec_ctx* ctx) {
   // FFT preconditioner: batched xy transforms around the fused z pass against
   // 3-D transforms with a separate multiply (n3 = 256 only)
   if (nl > 0 && ctx->n3 == 256) {
-    float ms[2] = {0.0f, 0.0f};
-    for (int form = 0; form < 2; ++form) {
+    float best = 1e30f;
+    int pick = 1;
+    for (int form = 0; form < 3; ++form) {
       ctx->tune.zpass = form;
       auto launch = [&]() -> int { return spectral_correction(ctx, L0.f, L0.v); };
-      CKS(time_ms(ctx, launch, 5, &ms[form]));
+      float ms = 0.0f;
+      CKS(time_ms(ctx, launch, 5, &ms));
       ctx->launches += 6;
+      if (ms < best) { best = ms; pick = form; }
     }
-    ctx->tune.zpass = ms[1] <= ms[0] ? 1 : 0;
+    ctx->tune.zpass = pick;
   }
   return BAOREC_OK;
 }
@@ -199,7 +202,7 @@ extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
 extern "C" int baorec_tune_zpass(const baorec_ctx* ctx) { return ctx ? ctx->tune.zpass : -1; }
 
 extern "C" int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass) {
-  if (!ctx || zpass < 0 || zpass > 1) return BAOREC_ERR_ARG;
+  if (!ctx || zpass < 0 || zpass > 2) return BAOREC_ERR_ARG;
   ctx->tune.zpass = zpass;
   return BAOREC_OK;
 }

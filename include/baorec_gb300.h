@@ -488,8 +488,9 @@ int baorec_tune_pairs(const baorec_ctx* ctx);
 int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
 /* FFT preconditioner of the residual-driven solve where n[2] = 256: 1 batched
  * 2-D transforms of the xy planes around one kernel that transforms along z,
- * multiplies by S^-1(k) and transforms back (default), 0 3-D transforms with a
- * separate multiply.  The stencil autotune times both. */
+ * multiplies by S^-1(k) and transforms back (default), 2 the same with the
+ * z kernel's registers capped for three resident blocks per SM, 0 3-D
+ * transforms with a separate multiply.  The stencil autotune times all three. */
 int baorec_tune_zpass(const baorec_ctx* ctx);
 int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass);
 
