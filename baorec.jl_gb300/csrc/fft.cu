@@ -596,10 +596,18 @@ __global__ void __launch_bounds__(256, MINB) zpass_precond_kernel(cufftComplex* 
                                                             const float2* __restrict__ tw, int ncols) {
   __shared__ float2 s[kZCols][kZLen + 1];
   __shared__ float2 w[kZLen];
+  __shared__ float2 kzt[kZLen];   // per kz: (diag_z sin²(θz/2), sin θz)
   const int t = threadIdx.x, cl = t & (kZCols - 1), r = t >> 4;
   const int col = (int)blockIdx.x * kZCols + cl;
   const bool ok = col < ncols;
+  const float* hx2 = tab;
+  const float* sx = hx2 + g.n1h;
+  const float* hy2 = sx + g.n1h;
+  const float* sy = hy2 + g.n2;
+  const float* hz2 = sy + g.n2;
+  const float* sz = hz2 + g.n3;
   w[t] = __ldg(tw + t);
+  kzt[t] = make_float2(g.diag[2] * __ldg(hz2 + t), __ldg(sz + t));
   float2* base = reinterpret_cast<float2*>(a) + (ok ? col : 0);
   const size_t plane = (size_t)ncols;
   float2 v[16];
@@ -616,22 +624,19 @@ __global__ void __launch_bounds__(256, MINB) zpass_precond_kernel(cufftComplex* 
   for (int n2 = 0; n2 < 16; ++n2) v[n2] = s[cl][16 * r + n2];
   dft16<false>(v);
   {
-    const float* hx2 = tab;
-    const float* sx = hx2 + g.n1h;
-    const float* hy2 = sx + g.n1h;
-    const float* sy = hy2 + g.n2;
-    const float* hz2 = sy + g.n2;
-    const float* sz = hz2 + g.n3;
+    // S(k) = c0 + diag_z sin²(θz/2) + c1 sin θz with the column's x and y
+    // terms in c0, c1; one approximate reciprocal per mode (a preconditioner)
     const int cc = ok ? col : 0;
     const int j = cc / g.n1h, i = cc - j * g.n1h;
     const float hxi = __ldg(hx2 + i), sxi = __ldg(sx + i), hyj = __ldg(hy2 + j), syj = __ldg(sy + j);
+    const float c0 = g.diag[1] * hyj + g.diag[0] * hxi + g.cross[0] * syj * sxi;
+    const float c1 = g.cross[2] * syj + g.cross[1] * sxi;
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
       const int k = r + 16 * k2;
-      const float szk = __ldg(sz + k);
-      const float A = g.diag[1] * hyj + g.diag[2] * __ldg(hz2 + k) + g.cross[2] * syj * szk + g.diag[0] * hxi +
-                      (g.cross[0] * syj + g.cross[1] * szk) * sxi;
-      const float sc = (k == 0 && j == 0 && i == 0) ? 0.0f : g.invN * __frcp_rn(A);
+      const float2 z = kzt[k];
+      const float A = c0 + fmaf(z.y, c1, z.x);
+      const float sc = (k == 0 && cc == 0) ? 0.0f : __fdividef(g.invN, A);
       v[k2].x *= sc;
       v[k2].y *= sc;
     }

@@ -81,11 +81,66 @@ __global__ void add_kernel(float* __restrict__ a, const float* __restrict__ b, s
     a[e] += b[e];
 }
 
-// r = f - shift: the residual of a zero solution, as the accurate residual
-// kernel would compute it ((f - α) + a bracket of zero differences).
-__global__ void shift_kernel(const float* __restrict__ f, float* __restrict__ r, float shift, size_t N) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    r[e] = f[e] - shift;
+// Per-block (Σf, Σf²) in FP64 (four-cell FP32 partial sums) for the norm
+// |f - α| and the shift α = mean f of the residual-driven solve.
+__global__ void sum_sumsq_partial_kernel(const float* __restrict__ a, size_t N, double* __restrict__ part) {
+  double s1 = 0.0, s2 = 0.0;
+  const size_t N4 = ((uintptr_t)a % 16 == 0) ? N / 4 : 0;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
+    const float4 u = a4[e];
+    s1 += (double)((u.x + u.y) + (u.z + u.w));
+    s2 += (double)((u.x * u.x + u.y * u.y) + (u.z * u.z + u.w * u.w));
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    const double v = (double)a[e];
+    s1 += v;
+    s2 += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double red[2][32];
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = s1; red[1][threadIdx.x >> 5] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0.0, t2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { t1 += red[0][k]; t2 += red[1][k]; }
+    part[2 * blockIdx.x] = t1;
+    part[2 * blockIdx.x + 1] = t2;
+  }
+}
+
+// r = f - α with α = Σf / N from the nb partials of sum_sumsq_partial_kernel:
+// the residual of a zero solution, as the accurate residual kernel would
+// compute it ((f - α) + a bracket of zero differences), formed without the
+// host reading the sums first.
+__global__ void shift_mean_kernel(const float* __restrict__ f, float* __restrict__ r, size_t N,
+                                  const double* __restrict__ part, int nb) {
+  __shared__ double red[32];
+  __shared__ float alpha_s;
+  double t = 0.0;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) t += part[2 * k];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
+    alpha_s = (float)(sum / (double)N);
+  }
+  __syncthreads();
+  const float alpha = alpha_s;
+  const size_t N4 = ((uintptr_t)f % 16 == 0 && (uintptr_t)r % 16 == 0) ? N / 4 : 0;
+  const float4* f4 = reinterpret_cast<const float4*>(f);
+  float4* r4 = reinterpret_cast<float4*>(r);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
+    const float4 u = f4[e];
+    r4[e] = make_float4(u.x - alpha, u.y - alpha, u.z - alpha, u.w - alpha);
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    r[e] = f[e] - alpha;
 }
 
 // Full-weighting restriction (src/multigrid.jl:586-640): coarse c centred on fine 2c+1.
@@ -738,10 +793,6 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   CKS(mg_setup(ctx));
   baorec::Level& L0 = ctx->lev[0];
   const size_t N = L0.N;
-  // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²)
-  double sf = 0.0, sf2 = 0.0;
-  CKS(sum_mesh(ctx, f, N, &sf));
-  CKS(sumsq_mesh(ctx, f, N, &sf2));
   float* hiA = phi;
   float* hiB = ctx->phi_hi2;
   float* loA = ctx->phi_lo;
@@ -754,7 +805,24 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   // solution pair stays zero.
   const bool zero_start = !phi0 && ctx->cfg.mg_start != BAOREC_START_LEARNED;
   CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
-  double alpha = sf / (double)N;
+  // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²), in one pass; the host reads
+  // them when it first needs them (a zero start forms its first residual and
+  // queues its first FFT correction on the device before that)
+  constexpr int kSumBlocks = 8 * kNumSMs;
+  sum_sumsq_partial_kernel<<<kSumBlocks, 256, 0, ctx->stream>>>(f, N, ctx->dred);
+  CKLAUNCH();
+  CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kSumBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
+  CK(cudaEventRecord(ctx->ev_red, ctx->stream));
+  double sf = 0.0, sf2 = 0.0, alpha = 0.0, fn2 = 0.0;
+  auto read_sums = [&]() -> int {
+    CK(cudaEventSynchronize(ctx->ev_red));
+    for (int q = 0; q < kSumBlocks; ++q) { sf += ctx->hred[2 * q]; sf2 += ctx->hred[2 * q + 1]; }
+    alpha = sf / (double)N;
+    fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;   // |f - α|² at the initial α
+    return BAOREC_OK;
+  };
+  if (!zero_start) CKS(read_sums());
   LG G = level_geom(ctx, 0, 0.0f);
   bool have_e = false;
   int cycles = 0;
@@ -776,13 +844,18 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   bool spectral = ctx->cfg.mg_start != BAOREC_START_ZERO;
   int nspec = 0, m_last = 0;
   double rho_prev = 0.0, rate = 0.0;
-  const double fn2 = sf2 - 2.0 * alpha * sf + (double)N * alpha * alpha;   // |f - α|² at the initial α
   for (int it = 0;; ++it) {
     double s1 = 0.0, s2 = 0.0;
     bool speculative = false;
     if (it == 0 && zero_start) {
-      shift_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(f, L0.f, (float)alpha, N);
+      shift_mean_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(f, L0.f, N, ctx->dred, kSumBlocks);
       CKLAUNCH();
+      // the first FFT correction needs only r: queue it before waiting for the sums
+      if (spectral && ctx->cfg.max_cycles > 0) {
+        CKS(spectral_correction(ctx, L0.f, L0.v));
+        speculative = true;
+      }
+      CKS(read_sums());
       s2 = fn2;
     } else {
       if (stream0) {
