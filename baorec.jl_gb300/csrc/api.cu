@@ -221,6 +221,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
   cufftHandle plans[6] = {ctx->plan_r2c, ctx->plan_r2c2, ctx->plan_c2r, ctx->plan_c2r2, ctx->plan_c2r3, ctx->plan_c2r6};
   for (cufftHandle p : plans)
     if (cufftSetWorkArea(p, ctx->fft_work) != CUFFT_SUCCESS) return fail(set_error(ctx, BAOREC_ERR_CUFFT, "cufftSetWorkArea"));
+  if ((st = zpass_prepare(ctx))) return fail(st);
   if ((st = xvec_update(ctx))) return fail(st);
   if (cfg->method == BAOREC_MULTIGRID && (st = mg_setup(ctx))) return fail(st);
 #undef CKC

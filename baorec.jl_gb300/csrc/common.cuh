@@ -197,6 +197,7 @@ int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t n
 int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
+int zpass_prepare(baorec_ctx* ctx);   // batched xy plans of the z pass (n3 = 256)
 // Unit line of sight the FFT preconditioner uses (false: isotropic, l = 0).
 bool mean_los(const baorec_ctx* c, double l[3]);
 // r = f - A v with the finest level's exact operator (difference form, FP32).

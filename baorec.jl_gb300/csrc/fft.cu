@@ -309,7 +309,13 @@ int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
   return BAOREC_OK;
 }
 
+namespace {
+bool use_zpass(const baorec_ctx* ctx);
+int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch);
+}  // namespace
+
 int smooth(baorec_ctx* ctx, float* mesh) {
+  if (use_zpass(ctx)) return smooth_zpass(ctx, mesh, 1);
   KGeom g = kgeom_of(ctx);
   float R = ctx->cfg.smoothing_radius;
   CKFFT(cufftExecR2C(ctx->plan_r2c, mesh, ctx->ck));
@@ -325,6 +331,7 @@ int smooth_pair(baorec_ctx* ctx, float* a, float* b) {
     CKS(smooth(ctx, a));
     return smooth(ctx, b);
   }
+  if (use_zpass(ctx)) return smooth_zpass(ctx, a, 2);
   KGeom g = kgeom_of(ctx);
   float R = ctx->cfg.smoothing_radius;
   CKFFT(cufftExecR2C(ctx->plan_r2c2, a, ctx->ck));
@@ -590,26 +597,72 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
 // a: n3 = 256 planes of ncols = n1h * n2 modes (column i + n1h j), transformed
 // over x and y; tw: e^{-2πi m/256}.  In place: a <- IFFT_z(S⁻¹ FFT_z(a)), with
 // S⁻¹ and the 1/N of the unnormalised transforms as spectral_inverse_kernel.
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) zpass_precond_kernel(cufftComplex* __restrict__ a, SGeom g,
-                                                            const float* __restrict__ tab,
-                                                            const float2* __restrict__ tw, int ncols) {
+// Per-mode multipliers of the z pass.  setup(kzt, t) fills the block's
+// per-kz table (t = kz), column(col) the per-column terms, factor(kzt, k)
+// gives the multiplier of mode (column, kz = k).
+struct PrecondMul {   // S⁻¹(k)/N of the FFT preconditioner (spectral_inverse_kernel)
+  SGeom g;
+  const float* tab;
+  float c0, c1;
+  int cc;
+  __device__ __forceinline__ void setup(float2* kzt, int t) const {
+    const float* hz2 = tab + 2 * g.n1h + 2 * g.n2;
+    kzt[t] = make_float2(g.diag[2] * __ldg(hz2 + t), __ldg(hz2 + g.n3 + t));   // diag_z sin²(θz/2), sin θz
+  }
+  // S(k) = c0 + diag_z sin²(θz/2) + c1 sin θz with the column's x and y terms in c0, c1
+  __device__ __forceinline__ void column(int col) {
+    cc = col;
+    const int j = col / g.n1h, i = col - j * g.n1h;
+    const float* sx = tab + g.n1h;
+    const float* hy2 = sx + g.n1h;
+    const float* sy = hy2 + g.n2;
+    const float hxi = __ldg(tab + i), sxi = __ldg(sx + i), hyj = __ldg(hy2 + j), syj = __ldg(sy + j);
+    c0 = g.diag[1] * hyj + g.diag[0] * hxi + g.cross[0] * syj * sxi;
+    c1 = g.cross[2] * syj + g.cross[1] * sxi;
+  }
+  // one approximate reciprocal per mode (a preconditioner); the k = 0 mode is dropped
+  __device__ __forceinline__ float factor(const float2* kzt, int k) const {
+    const float2 z = kzt[k];
+    return (k == 0 && cc == 0) ? 0.0f : __fdividef(g.invN, c0 + fmaf(z.y, c1, z.x));
+  }
+};
+
+struct GaussMul {   // smooth!: exp(-0.5 R² k²)/N, k² and the factor as gauss_kernel evaluates them
+  KGeom g;
+  float R2;
+  float c0;
+  __device__ __forceinline__ void setup(float2* kzt, int t) const {
+    float kx, ky, kz;
+    kvals(g, 0, 0, t, kx, ky, kz);
+    kzt[t] = make_float2(__fmul_rn(kz, kz), 0.0f);
+  }
+  __device__ __forceinline__ void column(int col) {
+    const int j = col / g.n1h, i = col - j * g.n1h;
+    float kx, ky, kz;
+    kvals(g, i, j, 0, kx, ky, kz);
+    c0 = __fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky));
+  }
+  __device__ __forceinline__ float factor(const float2* kzt, int k) const {
+    return expf(-0.5f * R2 * __fadd_rn(c0, kzt[k].x)) * g.invN;
+  }
+};
+
+// a (+ blockIdx.y spectra of n3 = 256 planes each): planes of ncols = n1h n2
+// modes (column i + n1h j), transformed over x and y; tw: e^{-2πi m/256}.
+// In place: a <- IFFT_z(M(k) FFT_z(a)) for the multiplier M.
+template <int MINB, class M>
+__global__ void __launch_bounds__(256, MINB) zpass_kernel(cufftComplex* __restrict__ a, M m,
+                                                          const float2* __restrict__ tw, int ncols) {
   __shared__ float2 s[kZCols][kZLen + 1];
   __shared__ float2 w[kZLen];
-  __shared__ float2 kzt[kZLen];   // per kz: (diag_z sin²(θz/2), sin θz)
+  __shared__ float2 kzt[kZLen];
   const int t = threadIdx.x, cl = t & (kZCols - 1), r = t >> 4;
   const int col = (int)blockIdx.x * kZCols + cl;
   const bool ok = col < ncols;
-  const float* hx2 = tab;
-  const float* sx = hx2 + g.n1h;
-  const float* hy2 = sx + g.n1h;
-  const float* sy = hy2 + g.n2;
-  const float* hz2 = sy + g.n2;
-  const float* sz = hz2 + g.n3;
   w[t] = __ldg(tw + t);
-  kzt[t] = make_float2(g.diag[2] * __ldg(hz2 + t), __ldg(sz + t));
-  float2* base = reinterpret_cast<float2*>(a) + (ok ? col : 0);
+  m.setup(kzt, t);
   const size_t plane = (size_t)ncols;
+  float2* base = reinterpret_cast<float2*>(a) + (size_t)blockIdx.y * plane * kZLen + (ok ? col : 0);
   float2 v[16];
   // x[16 n1 + r], n1 = 0..15 -> Σ_n1 x[16 n1 + r] W16^{n1 k1}, times W256^{r k1}
 #pragma unroll
@@ -623,23 +676,12 @@ __global__ void __launch_bounds__(256, MINB) zpass_precond_kernel(cufftComplex* 
 #pragma unroll
   for (int n2 = 0; n2 < 16; ++n2) v[n2] = s[cl][16 * r + n2];
   dft16<false>(v);
-  {
-    // S(k) = c0 + diag_z sin²(θz/2) + c1 sin θz with the column's x and y
-    // terms in c0, c1; one approximate reciprocal per mode (a preconditioner)
-    const int cc = ok ? col : 0;
-    const int j = cc / g.n1h, i = cc - j * g.n1h;
-    const float hxi = __ldg(hx2 + i), sxi = __ldg(sx + i), hyj = __ldg(hy2 + j), syj = __ldg(sy + j);
-    const float c0 = g.diag[1] * hyj + g.diag[0] * hxi + g.cross[0] * syj * sxi;
-    const float c1 = g.cross[2] * syj + g.cross[1] * sxi;
+  m.column(ok ? col : 0);
 #pragma unroll
-    for (int k2 = 0; k2 < 16; ++k2) {
-      const int k = r + 16 * k2;
-      const float2 z = kzt[k];
-      const float A = c0 + fmaf(z.y, c1, z.x);
-      const float sc = (k == 0 && cc == 0) ? 0.0f : __fdividef(g.invN, A);
-      v[k2].x *= sc;
-      v[k2].y *= sc;
-    }
+  for (int k2 = 0; k2 < 16; ++k2) {
+    const float sc = m.factor(kzt, r + 16 * k2);
+    v[k2].x *= sc;
+    v[k2].y *= sc;
   }
   // inverse: Z[r][n2] = W256^{-n2 r} Σ_k2 X[r + 16 k2] W16^{-n2 k2}
   dft16<true>(v);
@@ -688,6 +730,39 @@ bool xy_plans(baorec_ctx* ctx) {
   ctx->plan_c2r_xy = p[1];
   ctx->xy_state = 1;
   return true;
+}
+
+int spectral_tables(baorec_ctx* ctx);
+
+// z pass over `batch` spectra of n3 = 256 planes at a, multiplier m; form 2
+// caps the registers for three resident blocks per SM instead of two.
+template <class M>
+int zpass_launch(baorec_ctx* ctx, cufftComplex* a, const M& m, int batch) {
+  CKS(spectral_tables(ctx));
+  const int ncols = ctx->n1h * ctx->n2;
+  const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
+  auto k = ctx->tune.zpass == 2 ? zpass_kernel<3, M> : zpass_kernel<1, M>;
+  k<<<dim3((ncols + kZCols - 1) / kZCols, batch), 256, 0, ctx->stream>>>(a, m, tw, ncols);
+  CKLAUNCH();
+  return BAOREC_OK;
+}
+
+// True when smoothing and the preconditioner go through xy transforms and the
+// z pass: 256 z planes, the form enabled, and the plans built (eagerly at
+// context creation, so a graph capture never builds them).
+bool use_zpass(const baorec_ctx* ctx) { return ctx->n3 == kZLen && ctx->tune.zpass != 0 && ctx->xy_state == 1; }
+
+// smooth! of `batch` adjacent meshes through the z pass.
+int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch) {
+  GaussMul m;
+  m.g = kgeom_of(ctx);
+  m.R2 = ctx->cfg.smoothing_radius * ctx->cfg.smoothing_radius;
+  for (int b = 0; b < batch; ++b)
+    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, mesh + (size_t)b * ctx->N, ctx->ck + (size_t)b * ctx->Nk));
+  CKS(zpass_launch(ctx, ctx->ck, m, batch));
+  for (int b = 0; b < batch; ++b)
+    CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck + (size_t)b * ctx->Nk, mesh + (size_t)b * ctx->N));
+  return BAOREC_OK;
 }
 
 int spectral_tables(baorec_ctx* ctx) {
@@ -814,20 +889,28 @@ void spectral_callback_plan(baorec_ctx* ctx) {
 
 }  // namespace
 
+// The z pass's batched xy plans and tables for meshes of 256 z planes, built
+// when the context is created (a plan failure leaves the 3-D transforms in use).
+int zpass_prepare(baorec_ctx* ctx) {
+  if (ctx->n3 != kZLen) return BAOREC_OK;
+  CKS(spectral_tables(ctx));   // the twiddles and sine tables, before any graph capture
+  xy_plans(ctx);
+  return BAOREC_OK;
+}
+
 // e = S⁻¹ r (zero mean), S the operator with the box's mean line of sight.
 // r is read only; e may not alias r.
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   SGeom g = sgeom_of(ctx);
   CKS(spectral_tables(ctx));
   if (ctx->spec_cb_state == 0) spectral_callback_plan(ctx);
-  if (ctx->spec_cb_state != 1 && ctx->tune.zpass && ctx->n3 == kZLen && xy_plans(ctx)) {
+  if (ctx->spec_cb_state != 1 && use_zpass(ctx)) {
     const int ncols = ctx->n1h * ctx->n2;
     CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)r, ctx->ck));
-    const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
-    // form 2 caps the registers for three resident blocks per SM instead of two
-    auto k = ctx->tune.zpass == 2 ? zpass_precond_kernel<3> : zpass_precond_kernel<1>;
-    k<<<(ncols + kZCols - 1) / kZCols, 256, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, tw, ncols);
-    CKLAUNCH();
+    PrecondMul m;
+    m.g = g;
+    m.tab = ctx->stab;
+    CKS(zpass_launch(ctx, ctx->ck, m, 1));
     CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck, e));
     return BAOREC_OK;
   }
