@@ -312,6 +312,7 @@ int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
 namespace {
 bool use_zpass(const baorec_ctx* ctx);
 int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch);
+int zgrad_launch(baorec_ctx* ctx, const cufftComplex* src, int inv_lap);
 }  // namespace
 
 int smooth(baorec_ctx* ctx, float* mesh) {
@@ -432,13 +433,22 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
     CKLAUNCH();
     return BAOREC_OK;
   }
+  float* planes = psi4 + 4 * ctx->N;
+  const int inv_lap = ctx->cfg.method == BAOREC_ITERATIVE ? 1 : 0;
+  if (use_zpass(ctx)) {
+    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
+    CKS(zgrad_launch(ctx, ctx->ck + 3 * ctx->Nk, inv_lap));
+    for (int c = 0; c < 3; ++c)
+      CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck + (size_t)c * ctx->Nk, planes + (size_t)c * ctx->N));
+    interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
+    CKLAUNCH();
+    return BAOREC_OK;
+  }
   KGeom g = kgeom_of(ctx);
   // cuFFT's R2C reads but does not modify its input
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
-  grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g,
-                                                               ctx->cfg.method == BAOREC_ITERATIVE ? 1 : 0);
+  grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g, inv_lap);
   CKLAUNCH();
-  float* planes = psi4 + 4 * ctx->N;
   CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, planes));
   interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
   CKLAUNCH();
@@ -698,6 +708,87 @@ __global__ void __launch_bounds__(256, MINB) zpass_kernel(cufftComplex* __restri
   }
 }
 
+// Displacement spectra through the z pass: one xy-transformed spectrum in
+// (a, 256 planes), three out (out + c Nk, c = 0..2): forward z transform,
+// then per component the multiply of grad_kernel (i k_c / N, over k² for the
+// iterative method) and the inverse z transform.  The forward spectrum stays
+// in shared memory (each thread reads back its own values) between components;
+// dynamic shared memory: exchange 16 x 257, spectrum 256 x 16, twiddles, kz.
+constexpr size_t kZGradSmem = sizeof(float2) * (kZCols * (kZLen + 1) + kZLen * kZCols + kZLen) + sizeof(float) * kZLen;
+
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) zgrad_kernel(const cufftComplex* __restrict__ a,
+                                                          cufftComplex* __restrict__ out, KGeom g, int inv_lap,
+                                                          const float2* __restrict__ tw, int ncols) {
+  extern __shared__ __align__(16) float2 zg_smem[];
+  float2 (*s)[kZLen + 1] = reinterpret_cast<float2 (*)[kZLen + 1]>(zg_smem);
+  float2 (*xs)[kZCols] = reinterpret_cast<float2 (*)[kZCols]>(zg_smem + kZCols * (kZLen + 1));   // [kz][column]
+  float2* w = zg_smem + kZCols * (kZLen + 1) + kZLen * kZCols;
+  float* kzt = reinterpret_cast<float*>(w + kZLen);
+  const int t = threadIdx.x, cl = t & (kZCols - 1), r = t >> 4;
+  const int col = (int)blockIdx.x * kZCols + cl;
+  const bool ok = col < ncols;
+  w[t] = __ldg(tw + t);
+  {
+    float kx, ky, kz;
+    kvals(g, 0, 0, t, kx, ky, kz);
+    kzt[t] = kz;
+  }
+  const size_t plane = (size_t)ncols, nk = plane * kZLen;
+  const float2* src = reinterpret_cast<const float2*>(a) + (ok ? col : 0);
+  float2 v[16];
+#pragma unroll
+  for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? src[(size_t)(16 * n1 + r) * plane] : make_float2(0.0f, 0.0f);
+  dft16<false>(v);
+  __syncthreads();
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) s[cl][16 * k1 + r] = cmulf(v[k1], w[r * k1]);
+  __syncthreads();
+#pragma unroll
+  for (int n2 = 0; n2 < 16; ++n2) v[n2] = s[cl][16 * r + n2];
+  dft16<false>(v);   // v[k2] = X[kz = r + 16 k2]
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) xs[16 * r + k2][cl] = v[k2];
+  float kxy[2];
+  {
+    const int cc = ok ? col : 0;
+    const int j = cc / g.n1h, i = cc - j * g.n1h;
+    float kz;
+    kvals(g, i, j, 0, kxy[0], kxy[1], kz);
+  }
+  const float c0 = __fadd_rn(__fmul_rn(kxy[0], kxy[0]), __fmul_rn(kxy[1], kxy[1]));
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+      const float kz = kzt[r + 16 * k2];
+      const float kc = c == 0 ? kxy[0] : (c == 1 ? kxy[1] : kz);
+      const float2 d = xs[16 * r + k2][cl];
+      // (i k) (re + i im) = (-k im, k re), as grad_kernel
+      float re = -__fmul_rn(kc, d.y), im = __fmul_rn(kc, d.x);
+      if (inv_lap) {
+        const float k2v = __fadd_rn(c0, __fmul_rn(kz, kz));
+        if (k2v > 0.0f) { re = __fdiv_rn(re, k2v); im = __fdiv_rn(im, k2v); }
+        else { re = 0.0f; im = 0.0f; }
+      }
+      v[k2] = make_float2(re * g.invN, im * g.invN);
+    }
+    dft16<true>(v);
+    __syncthreads();   // the previous component's reads of s are done
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) s[cl][16 * r + n2] = cmulf_conj(v[n2], w[n2 * r]);
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) v[k1] = s[cl][16 * k1 + r];
+    dft16<true>(v);
+    if (ok) {
+      float2* dst = reinterpret_cast<float2*>(out) + (size_t)c * nk + col;
+#pragma unroll
+      for (int n1 = 0; n1 < 16; ++n1) dst[(size_t)(16 * n1 + r) * plane] = v[n1];
+    }
+  }
+}
+
 // Batched 2-D transforms of the n3 xy planes (R2C and C2R) for the z pass,
 // built at the first correction; any failure leaves the 3-D transforms in use.
 bool xy_plans(baorec_ctx* ctx) {
@@ -762,6 +853,16 @@ int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch) {
   CKS(zpass_launch(ctx, ctx->ck, m, batch));
   for (int b = 0; b < batch; ++b)
     CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck + (size_t)b * ctx->Nk, mesh + (size_t)b * ctx->N));
+  return BAOREC_OK;
+}
+
+// Ψ spectra (three, at ctx->ck) of the xy-transformed field spectrum at src.
+int zgrad_launch(baorec_ctx* ctx, const cufftComplex* src, int inv_lap) {
+  const int ncols = ctx->n1h * ctx->n2;
+  const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
+  auto k = ctx->tune.zpass == 2 ? zgrad_kernel<3> : zgrad_kernel<1>;
+  k<<<(ncols + kZCols - 1) / kZCols, 256, kZGradSmem, ctx->stream>>>(src, ctx->ck, kgeom_of(ctx), inv_lap, tw, ncols);
+  CKLAUNCH();
   return BAOREC_OK;
 }
 
@@ -895,6 +996,8 @@ int zpass_prepare(baorec_ctx* ctx) {
   if (ctx->n3 != kZLen) return BAOREC_OK;
   CKS(spectral_tables(ctx));   // the twiddles and sine tables, before any graph capture
   xy_plans(ctx);
+  CK(cudaFuncSetAttribute(zgrad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZGradSmem));
+  CK(cudaFuncSetAttribute(zgrad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZGradSmem));
   return BAOREC_OK;
 }
 

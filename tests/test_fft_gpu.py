@@ -124,3 +124,21 @@ def test_displacement_meshes_match_oracle(method):
     ref = O.displacement_meshes_iterative(fld, [L] * 3) if method == "iterative" else O.gradient_meshes(fld, [L] * 3)
     for a in range(3):
         assert rel_l2(psi[a].cpu().numpy(), ref[a]) < FFT_TOL * 5
+
+
+@pytest.mark.parametrize("method,zpass", [("iterative", 1), ("multigrid", 1), ("multigrid", 2), ("multigrid", 0)])
+def test_displacement_through_z_pass_matches_oracle(method, zpass):
+    """Meshes with 256 z planes: the displacement spectra from one forward z
+    transform and three inverse ones (the gradient multiply between them, over
+    k² for the iterative method), against the oracle, for each transform form."""
+    import baorec
+    shape, bs = (32, 48, 256), [400.0, 600.0, 3200.0]
+    fld = O.smooth(np.random.default_rng(9).standard_normal(shape).astype(F32), 30.0, bs)
+    cls = baorec.IterativeRecon if method == "iterative" else baorec.MultigridRecon
+    rec = cls(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=[0.0] * 3)
+    ctx = baorec.setup_fft_(rec, shape)
+    ctx.call("baorec_set_tune_zpass", zpass)
+    psi = baorec.compute_displacements(np.asfortranarray(fld), rec)
+    ref = O.displacement_meshes_iterative(fld, bs) if method == "iterative" else O.gradient_meshes(fld, bs)
+    for a in range(3):
+        assert rel_l2(psi[a].cpu().numpy(), ref[a]) < FFT_TOL * 5
