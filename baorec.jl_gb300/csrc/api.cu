@@ -4,6 +4,7 @@
 #include <stdarg.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <new>
 
 #include "common.cuh"
@@ -56,8 +57,24 @@ int finish(baorec_ctx* ctx, uint32_t flags) {
   return BAOREC_OK;
 }
 
+// Page-locked host memory (cudaHostAlloc, cudaHostRegister) is mapped into
+// the device's address space: kernels read and write it over the host link
+// directly, so a host array in such memory is used in place instead of being
+// copied through a staging buffer (the bytes still cross the link once, but
+// the transfer overlaps the kernel that consumes it).  Returns the device
+// address of p, or null for pageable memory.
+static const float* host_alias(const float* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<const float*>(a.devicePointer) : nullptr;
+}
+
 int stage_in(baorec_ctx* ctx, int slot, const float* p, int64_t n, uint32_t flags, const float** out) {
   if (!(flags & BAOREC_HOST) || !p || n <= 0) { *out = p; return BAOREC_OK; }
+  if (const float* d = host_alias(p)) { *out = d; return BAOREC_OK; }
   CKS(ensure(ctx, ctx->stage[slot], (size_t)n * 4));
   CK(cudaMemcpyAsync(ctx->stage[slot].p, p, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
   *out = (const float*)ctx->stage[slot].p;
@@ -66,6 +83,8 @@ int stage_in(baorec_ctx* ctx, int slot, const float* p, int64_t n, uint32_t flag
 
 int stage_out_alloc(baorec_ctx* ctx, int slot, int64_t n, uint32_t flags, float* user, float** dev) {
   if (!(flags & BAOREC_HOST)) { *dev = user; return BAOREC_OK; }
+  if (user && n > 0)
+    if (const float* d = host_alias(user)) { *dev = const_cast<float*>(d); return BAOREC_OK; }
   CKS(ensure(ctx, ctx->stage[slot], (size_t)(n > 0 ? n : 1) * 4));
   *dev = (float*)ctx->stage[slot].p;
   return BAOREC_OK;
@@ -73,6 +92,7 @@ int stage_out_alloc(baorec_ctx* ctx, int slot, int64_t n, uint32_t flags, float*
 
 int stage_out_copy(baorec_ctx* ctx, float* user, const float* dev, int64_t n, uint32_t flags) {
   if (!(flags & BAOREC_HOST) || n <= 0) return BAOREC_OK;
+  if (dev == user || dev == host_alias(user)) return BAOREC_OK;   // written in place
   CK(cudaMemcpyAsync(user, dev, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   return BAOREC_OK;
 }
@@ -688,6 +708,14 @@ extern "C" int baorec_read_cic(baorec_ctx* ctx, const float* mesh, const float* 
 // are those of the unchunked call.
 static constexpr int64_t kPipeChunk = (int64_t)1 << 20;
 
+// Every array page-locked: the read-out kernel reads the positions and writes
+// the results in place over the host link, with no staging or chunking.
+static bool all_host_alias(std::initializer_list<const float*> ps) {
+  for (const float* p : ps)
+    if (!host_alias(p)) return false;
+  return true;
+}
+
 static int readout_pipelined(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n, int field,
                              int mode, float* const outs[6], int nout, int field2) {
   if (!ctx->s_in) {
@@ -744,7 +772,7 @@ static int shifts_common(baorec_ctx* ctx, const float* x, const float* y, const 
     return set_error(ctx, BAOREC_ERR_ARG, "read_shifts: bad arguments");
   if (field < BAOREC_FIELD_DISP || field > BAOREC_FIELD_SUM) return set_error(ctx, BAOREC_ERR_ARG, "unknown field %d", field);
   CKS(ensure_psi(ctx));
-  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk) {
+  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk && !all_host_alias({x, y, z, o0, o1, o2})) {
     float* const outs[6] = {o0, o1, o2, nullptr, nullptr, nullptr};
     CKS(readout_pipelined(ctx, x, y, z, n, field, mode, outs, 3, 0));
     return finish(ctx, flags & ~BAOREC_ASYNC);
@@ -773,7 +801,7 @@ extern "C" int baorec_reconstructed_positions2(baorec_ctx* ctx, const float* x, 
   for (int fl : {field_a, field_b})
     if (fl < BAOREC_FIELD_DISP || fl > BAOREC_FIELD_SUM) return set_error(ctx, BAOREC_ERR_ARG, "unknown field %d", fl);
   CKS(ensure_psi(ctx));
-  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk) {
+  if ((flags & BAOREC_HOST) && n > 2 * kPipeChunk && !all_host_alias({x, y, z, oxa, oya, oza, oxb, oyb, ozb})) {
     float* const po[6] = {oxa, oya, oza, oxb, oyb, ozb};
     CKS(readout_pipelined(ctx, x, y, z, n, field_a, 1, po, 6, field_b));
     return finish(ctx, flags & ~BAOREC_ASYNC);

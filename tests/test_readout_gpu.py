@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import baorec_oracle as O
-from _util import F32, uniform_box
+from _util import F32, small_lightcone, uniform_box
 
 pytestmark = pytest.mark.gpu
 
@@ -100,3 +100,46 @@ def test_chunked_host_readout_equals_device():
     sd = baorec.read_shifts(rec, xd, yd, zd, np.asfortranarray(fld), field="rsd")
     for u, v in zip(s, sd):
         np.testing.assert_array_equal(u, v.cpu().numpy())
+
+
+def test_page_locked_host_arrays_used_in_place():
+    """Page-locked (pinned) host arrays are read and written by the kernels in
+    place over the host link, with no staging: the reconstruction from pinned
+    catalogs (deterministic paint) and the read-out into pinned outputs, above
+    two pipeline chunks, equal the device-array calls bit for bit."""
+    import ctypes as C
+    import torch
+    import baorec
+    from baorec import _lib
+    m = small_lightcone(n_data=20000, rand_factor=5, n_grid=32, seed=4)
+    n = 32
+    bs, bm = O.setup_box(m.rx, m.ry, m.rz, 200.0)
+    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm,
+                                mg_mode="convergent", rtol=1e-6, start="spectral")
+    ctx = baorec.setup_fft_(rec, (n, n, n))
+    cats = [m.x, m.y, m.z, m.w, m.rx, m.ry, m.rz, m.rw]
+    pin = [torch.from_numpy(np.ascontiguousarray(a, dtype=F32)).pin_memory() for a in cats]
+    dev = [t.cuda() for t in pin]
+    npart = 2 * (1 << 20) + 777
+    rng = np.random.default_rng(8)
+    q = [(bm[a] + rng.random(npart) * bs[a]).astype(F32) for a in range(3)]
+    qpin = [torch.from_numpy(a).pin_memory() for a in q]
+    qdev = [t.cuda() for t in qpin]
+    res = []
+    for cat, pos, loc in ((dev, qdev, "cuda"), (pin, qpin, "pin")):
+        flags = _lib.HOST if loc == "pin" else 0
+        p = [t.data_ptr() for t in cat]
+        ctx.call("baorec_reconstructed_potential", *p[:4], len(m.x), *p[4:], len(m.rx), flags | _lib.DETERMINISTIC)
+        phi = torch.empty(n ** 3, device="cuda")
+        ctx.call("baorec_get_result", C.c_void_p(phi.data_ptr()), 0)
+        outs = [torch.empty(npart, device="cuda") if loc == "cuda" else torch.empty(npart).pin_memory()
+                for _ in range(6)]
+        o = [t.data_ptr() for t in outs]
+        ctx.call("baorec_reconstructed_positions2", *[t.data_ptr() for t in pos], npart,
+                 _lib.FIELD["sum"], *o[:3], _lib.FIELD["disp"], *o[3:], flags)
+        torch.cuda.synchronize()
+        res.append((phi.cpu().numpy(), [t.cpu().numpy() for t in outs]))
+    (p0, o0), (p1, o1) = res
+    np.testing.assert_array_equal(p0, p1)
+    for u, v in zip(o0, o1):
+        np.testing.assert_array_equal(u, v)
