@@ -844,6 +844,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   bool spectral = ctx->cfg.mg_start != BAOREC_START_ZERO;
   int nspec = 0, m_last = 0;
   double rho_prev = 0.0, rate = 0.0;
+  const float* pending_d = nullptr;   // last FFT correction of an outer step, not yet added to e
   for (int it = 0;; ++it) {
     double s1 = 0.0, s2 = 0.0;
     bool speculative = false;
@@ -864,7 +865,8 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
         ctx->launches++;
       } else if (tile0) {
         CK(launch_resid_acc(ctx->stream, hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f, G, (float)alpha,
-                            ctx->dred, &nparts));
+                            ctx->dred, &nparts, have_e ? pending_d : nullptr));
+        pending_d = nullptr;
         ctx->launches++;
       } else {
         resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
@@ -949,7 +951,9 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
         std::swap(rin, rout);
         CKS(spectral_correction(ctx, rin, d));
       }
-      if (m > 1) {
+      if (m > 1 && tile0 && !stream0) {
+        pending_d = d;   // the tiled accurate residual adds the last correction as it loads e
+      } else if (m > 1) {
         add_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L0.v, d, N);
         CKLAUNCH();
       }

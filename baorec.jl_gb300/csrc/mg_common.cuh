@@ -122,8 +122,10 @@ cudaError_t launch_resid_diff(cudaStream_t s, const float* e, const float* rhs, 
 cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float shift, bool clamp,
                          float* acc = nullptr);
 // Accurate residual with solution update; writes (Σr, Σr²) per block to part, returns the block count.
+// The correction is e (+ ed, added in FP32 first, when both are given).
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* e, const float* f,
-                             float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts);
+                             float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts,
+                             const float* ed = nullptr);
 int tile_blocks(const LG& G);
 // streaming (2.5-D, cp.async-pipelined) forms of the finest-level residuals (mg_stream.cu)
 bool stream_ok(const int n[3]);

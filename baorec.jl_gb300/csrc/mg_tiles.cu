@@ -526,10 +526,13 @@ __global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restr
 
 // r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
 // operator, whose coefficients are evaluated with IEEE round-to-nearest
-// operations in the reference's order.  Per-block (Σr, Σr²) to part.
-template <bool LOCAL, int TY, int TZ>
+// operations in the reference's order.  Per-block (Σr, Σr²) to part.  The
+// solution pair is (hi, lo) + ec first; with HASD the correction is ec + ed,
+// added in FP32 as a separate e += d pass would.
+template <bool LOCAL, int TY, int TZ, bool HASD>
 __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                        const float* __restrict__ ec, const float* __restrict__ f,
+                                                        const float* __restrict__ ec, const float* __restrict__ ed,
+                                                        const float* __restrict__ f,
                                                         float* __restrict__ ohi, float* __restrict__ olo,
                                                         float* __restrict__ r, LG G, float alpha,
                                                         double* __restrict__ part) {
@@ -549,10 +552,10 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
   __syncthreads();
   {
     float4* sw4 = reinterpret_cast<float4*>(smem);
-    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = 4;
+    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = HASD ? 3 : 4;
 #pragma unroll
     for (int k0 = 0; k0 < K; k0 += B) {
-      float4 h[B], l[B], e[B];
+      float4 h[B], l[B], e[B], d[B];
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int t = threadIdx.x + (k0 + b) * NT;
@@ -562,12 +565,19 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
           h[b] = __ldg(reinterpret_cast<const float4*>(hi + o));
           l[b] = __ldg(reinterpret_cast<const float4*>(lo + o));
           if (ec) e[b] = __ldg(reinterpret_cast<const float4*>(ec + o));
+          if (HASD) d[b] = __ldg(reinterpret_cast<const float4*>(ed + o));
         }
       }
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int t = threadIdx.x + (k0 + b) * NT;
         if (k0 + b < K && t < TOT) {
+          if (HASD) {
+            e[b].x = e[b].x + d[b].x;
+            e[b].y = e[b].y + d[b].y;
+            e[b].z = e[b].z + d[b].z;
+            e[b].w = e[b].w + d[b].w;
+          }
           if (ec) {
             df_add(h[b].x, l[b].x, e[b].x, h[b].x, l[b].x);
             df_add(h[b].y, l[b].y, e[b].y, h[b].y, l[b].y);
@@ -706,13 +716,13 @@ cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
 }
 
 template <bool LOCAL, int TY, int TZ>
-cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f, float* ohi,
-                  float* olo, float* r, const LG& G, float alpha, double* part) {
-  auto k = resid_acc2_kernel<LOCAL, TY, TZ>;
+cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* ed, const float* f,
+                  float* ohi, float* olo, float* r, const LG& G, float alpha, double* part) {
+  auto k = (ed && ec) ? resid_acc2_kernel<LOCAL, TY, TZ, true> : resid_acc2_kernel<LOCAL, TY, TZ, false>;
   constexpr size_t b = win_bytes<1, TY, TZ>(2);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(hi, lo, ec, f, ohi, olo, r, G, alpha, part);
+  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
   return cudaGetLastError();
 }
 
@@ -759,14 +769,15 @@ cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs,
 }
 
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f,
-                             float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts) {
+                             float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts,
+                             const float* ed) {
   *nparts = tile_blocks(G);
   const bool big = big_tiles(G);
   if (G.local)
-    return big ? acc_t<true, 16, 16>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part)
-               : acc_t<true, 8, 8>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part);
-  return big ? acc_t<false, 16, 16>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part)
-             : acc_t<false, 8, 8>(s, hi, lo, ec, f, ohi, olo, r, G, alpha, part);
+    return big ? acc_t<true, 16, 16>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part)
+               : acc_t<true, 8, 8>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
+  return big ? acc_t<false, 16, 16>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part)
+             : acc_t<false, 8, 8>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
 }
 
 }  // namespace baorec
