@@ -465,11 +465,16 @@ def run_gb300(args):
 
     # rooflines measured live (CUDA events on the context stream around a run
     # of launches on the finest level); the headline is the dominant kernel of
-    # the timed path: the accurate residual for the FFT / learned starts, the
-    # red-black sweep for the plain multigrid start
+    # the timed path (largest share of its launch list): the FP32 running
+    # residual of the FFT corrections for the FFT / learned starts (6 launches
+    # per reconstruction against the accurate residual's 2), in the form the
+    # solve uses; the red-black sweep for the plain multigrid start
     peak, peak_src = measured_peak()
     N = int(np.prod(n))
-    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: "resid_kernel (difference form)",
+    pairs = tune.get("pair_residual", 0) == 1
+    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel",
+             3: "resid_pairs_kernel (FP32 running residual, two cells per thread)" if pairs
+             else "resid_kernel (difference form)",
              4: "resid_acc_stream_kernel", 5: "resid_diff_stream_kernel"}
     meas = {}
     for which in (() if args.no_kernels else (0, 1, 3, 4, 5)):
@@ -480,8 +485,7 @@ def run_gb300(args):
                        "frac": ach / peak, "peak_source": peak_src,
                        "traffic": traffic_per_launch(names[which].split()[0], N),
                        "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
-    # the accurate residual in the form the solve uses (streaming unless the tuner chose the tiles)
-    head = 0 if args.start == "zero" else (4 if tune.get("stream_residuals", -1) != 0 else 1)
+    head = 0 if args.start == "zero" else (5 if tune.get("stream_residuals", -1) != 0 else 3)
     roofline, aux = None, {}
     if meas:
         roofline = dict(meas[head])
