@@ -138,6 +138,8 @@ _SIGS = {
     "baorec_set_tune_pairs": (C.c_int, [P, C.c_int]),
     "baorec_tune_zpass": (C.c_int, [P]),
     "baorec_set_tune_zpass": (C.c_int, [P, C.c_int]),
+    "baorec_tune_xy": (C.c_int, [P]),
+    "baorec_set_tune_xy": (C.c_int, [P, C.c_int]),
     "baorec_sky_to_cartesian": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
                                           P, P, P, U32]),
     "baorec_cartesian_to_sky": (C.c_int, [P, P, P, P, I64, P, C.c_int32, C.c_double, C.c_double, C.c_float,
@@ -272,7 +274,8 @@ class Context:
         return {"paint_tile": pt.value, "tile16_per_level": list(bt),
                 "stream_residuals": int(self.lib.baorec_tune_stream(self.h)),
                 "pair_residual": int(self.lib.baorec_tune_pairs(self.h)),
-                "fft_zpass": int(self.lib.baorec_tune_zpass(self.h))}
+                "fft_zpass": int(self.lib.baorec_tune_zpass(self.h)),
+                "fft_xy_fused": int(self.lib.baorec_tune_xy(self.h))}
 
     def fft_callbacks(self) -> dict:
         """State of the FFT start's cuFFT load callback (baorec_fft_callbacks)."""

@@ -102,6 +102,7 @@ struct baorec_ctx {
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming
     int pairs = 1;                     // running residual on 32x16x16 tiles: 1 packed z-pairs, 0 one cell per thread
     int zpass = 1;                     // FFT preconditioner: 1 (2: capped registers) xy transforms + fused z pass where n3 = 256, 0 3-D transforms
+    int xy = 0;                        // xy transforms of the z-pass paths: 0 cuFFT, 1 fused kernels (256 x 256 planes)
     int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1
     bool tuned = false;
   } tune;
@@ -198,6 +199,11 @@ int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
 int zpass_prepare(baorec_ctx* ctx);   // batched xy plans of the z pass (n3 = 256)
+// fused 2-D real transforms of 256 x 256 xy planes (xyfft.cu)
+bool xy_fused_ok(const baorec_ctx* ctx);
+int xy_fused_prepare(baorec_ctx* ctx);
+int xy_r2c(baorec_ctx* ctx, const float* in, cufftComplex* out, int planes);
+int xy_c2r(baorec_ctx* ctx, const cufftComplex* in, float* out, int planes);
 // Unit line of sight the FFT preconditioner uses (false: isotropic, l = 0).
 bool mean_los(const baorec_ctx* c, double l[3]);
 // r = f - A v with the finest level's exact operator (difference form, FP32).

@@ -313,6 +313,22 @@ namespace {
 bool use_zpass(const baorec_ctx* ctx);
 int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch);
 int zgrad_launch(baorec_ctx* ctx, const cufftComplex* src, int inv_lap);
+
+// Batched 2-D transforms of `meshes` adjacent meshes' xy planes: the fused
+// kernels of xyfft.cu for 256 x 256 planes (unless the autotuner chose
+// cuFFT), else the cuFFT plans (which overwrite a C2R input).
+int xy_forward(baorec_ctx* ctx, const float* in, cufftComplex* out, int meshes) {
+  if (ctx->tune.xy && xy_fused_ok(ctx)) return xy_r2c(ctx, in, out, meshes * ctx->n3);
+  for (int b = 0; b < meshes; ++b)
+    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)(in + (size_t)b * ctx->N), out + (size_t)b * ctx->Nk));
+  return BAOREC_OK;
+}
+int xy_inverse(baorec_ctx* ctx, cufftComplex* in, float* out, int meshes) {
+  if (ctx->tune.xy && xy_fused_ok(ctx)) return xy_c2r(ctx, in, out, meshes * ctx->n3);
+  for (int b = 0; b < meshes; ++b)
+    CKFFT(cufftExecC2R(ctx->plan_c2r_xy, in + (size_t)b * ctx->Nk, out + (size_t)b * ctx->N));
+  return BAOREC_OK;
+}
 }  // namespace
 
 int smooth(baorec_ctx* ctx, float* mesh) {
@@ -436,10 +452,9 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
   float* planes = psi4 + 4 * ctx->N;
   const int inv_lap = ctx->cfg.method == BAOREC_ITERATIVE ? 1 : 0;
   if (use_zpass(ctx)) {
-    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
+    CKS(xy_forward(ctx, field, ctx->ck + 3 * ctx->Nk, 1));
     CKS(zgrad_launch(ctx, ctx->ck + 3 * ctx->Nk, inv_lap));
-    for (int c = 0; c < 3; ++c)
-      CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck + (size_t)c * ctx->Nk, planes + (size_t)c * ctx->N));
+    CKS(xy_inverse(ctx, ctx->ck, planes, 3));
     interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
     CKLAUNCH();
     return BAOREC_OK;
@@ -848,11 +863,9 @@ int smooth_zpass(baorec_ctx* ctx, float* mesh, int batch) {
   GaussMul m;
   m.g = kgeom_of(ctx);
   m.R2 = ctx->cfg.smoothing_radius * ctx->cfg.smoothing_radius;
-  for (int b = 0; b < batch; ++b)
-    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, mesh + (size_t)b * ctx->N, ctx->ck + (size_t)b * ctx->Nk));
+  CKS(xy_forward(ctx, mesh, ctx->ck, batch));
   CKS(zpass_launch(ctx, ctx->ck, m, batch));
-  for (int b = 0; b < batch; ++b)
-    CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck + (size_t)b * ctx->Nk, mesh + (size_t)b * ctx->N));
+  CKS(xy_inverse(ctx, ctx->ck, mesh, batch));
   return BAOREC_OK;
 }
 
@@ -996,6 +1009,7 @@ int zpass_prepare(baorec_ctx* ctx) {
   if (ctx->n3 != kZLen) return BAOREC_OK;
   CKS(spectral_tables(ctx));   // the twiddles and sine tables, before any graph capture
   xy_plans(ctx);
+  CKS(xy_fused_prepare(ctx));
   CK(cudaFuncSetAttribute(zgrad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZGradSmem));
   CK(cudaFuncSetAttribute(zgrad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZGradSmem));
   return BAOREC_OK;
@@ -1009,12 +1023,12 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   if (ctx->spec_cb_state == 0) spectral_callback_plan(ctx);
   if (ctx->spec_cb_state != 1 && use_zpass(ctx)) {
     const int ncols = ctx->n1h * ctx->n2;
-    CKFFT(cufftExecR2C(ctx->plan_r2c_xy, (cufftReal*)r, ctx->ck));
+    CKS(xy_forward(ctx, r, ctx->ck, 1));
     PrecondMul m;
     m.g = g;
     m.tab = ctx->stab;
     CKS(zpass_launch(ctx, ctx->ck, m, 1));
-    CKFFT(cufftExecC2R(ctx->plan_c2r_xy, ctx->ck, e));
+    CKS(xy_inverse(ctx, ctx->ck, e, 1));
     return BAOREC_OK;
   }
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)r, ctx->ck));

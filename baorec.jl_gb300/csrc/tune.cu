@@ -6,7 +6,8 @@
 //            also the streaming against the tiled residual kernels and the
 //            running residual with two z-cells per thread against one, and
 //            (n3 = 256) the FFT preconditioner's xy transforms + z pass
-//            against its 3-D transforms;
+//            against its 3-D transforms, and (256 x 256 planes) the fused xy
+//            kernels against cuFFT's;
 //   paint:   the tile edge (4, 8 or 16 cells) of the deterministic paint,
 //            on 2^21 uniform particles in the box.
 // Choices live in ctx->tune and apply to every later launch of the context.
@@ -132,20 +133,25 @@ int tune_stencils(baorec_ctx* ctx) {
     }
     ctx->tune.pairs = ms[1] <= ms[0] ? 1 : 0;
   }
-  // FFT preconditioner: batched xy transforms around the fused z pass against
-  // 3-D transforms with a separate multiply (n3 = 256 only)
+  // FFT preconditioner: batched xy transforms around the fused z pass (two
+  // register forms; xy transforms by cuFFT or, for 256 x 256 planes, by the
+  // fused kernels) against 3-D transforms with a separate multiply (n3 = 256)
   if (nl > 0 && ctx->n3 == 256) {
+    const int cand[5][2] = {{0, 0}, {1, 0}, {2, 0}, {1, 1}, {2, 1}};
+    const int ncand = xy_fused_ok(ctx) ? 5 : 3;
     float best = 1e30f;
     int pick = 1;
-    for (int form = 0; form < 3; ++form) {
-      ctx->tune.zpass = form;
+    for (int c = 0; c < ncand; ++c) {
+      ctx->tune.zpass = cand[c][0];
+      ctx->tune.xy = cand[c][1];
       auto launch = [&]() -> int { return spectral_correction(ctx, L0.f, L0.v); };
       float ms = 0.0f;
       CKS(time_ms(ctx, launch, 5, &ms));
       ctx->launches += 6;
-      if (ms < best) { best = ms; pick = form; }
+      if (ms < best) { best = ms; pick = c; }
     }
-    ctx->tune.zpass = pick;
+    ctx->tune.zpass = cand[pick][0];
+    ctx->tune.xy = cand[pick][1];
   }
   return BAOREC_OK;
 }
@@ -204,6 +210,14 @@ extern "C" int baorec_tune_zpass(const baorec_ctx* ctx) { return ctx ? ctx->tune
 extern "C" int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass) {
   if (!ctx || zpass < 0 || zpass > 2) return BAOREC_ERR_ARG;
   ctx->tune.zpass = zpass;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_tune_xy(const baorec_ctx* ctx) { return ctx ? ctx->tune.xy : -1; }
+
+extern "C" int baorec_set_tune_xy(baorec_ctx* ctx, int xy) {
+  if (!ctx || xy < 0 || xy > 1) return BAOREC_ERR_ARG;
+  ctx->tune.xy = xy;
   return BAOREC_OK;
 }
 

@@ -493,6 +493,11 @@ int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
  * transforms with a separate multiply.  The stencil autotune times all three. */
 int baorec_tune_zpass(const baorec_ctx* ctx);
 int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass);
+/* The xy transforms of the z-pass paths (preconditioner, smoothing,
+ * displacement) for 256 x 256 planes: 0 cuFFT's batched 2-D transforms
+ * (default), 1 one fused kernel per direction.  The stencil autotune times both. */
+int baorec_tune_xy(const baorec_ctx* ctx);
+int baorec_set_tune_xy(baorec_ctx* ctx, int xy);
 
 /* ---- Catalog coordinates (examples/lightcone.jl:30-82) ------------------------
  * sky_to_cartesian (lightcone.jl:30-47): ra, dec in degrees and redshift z ->
