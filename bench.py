@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--only-start", action="store_true", help="time only the --start solve (no other starts)")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel roofline and paint timings")
     ap.add_argument("--batch-mocks", type=int, default=64)
+    ap.add_argument("--set-tune", default="",
+                    help="after the autotuner, force choices: comma-separated key=value of pair_residual, "
+                         "fft_zpass, fft_xy_fused, stream_residuals (a profiler distorts the tuner's timings, "
+                         "so a launch list under ncu pins the choices of the timed run)")
     ap.add_argument("--conv-only", action="store_true",
                     help="only time the learned guess's tensor-core convolutions, every shape on a --mesh grid "
                          "(a small case for profilers)")
@@ -400,6 +404,13 @@ def run_gb300(args):
     tune = ctx.autotune()
     for c_ in others.values():
         c_.autotune(paint=False)
+    setters = {"pair_residual": "baorec_set_tune_pairs", "fft_zpass": "baorec_set_tune_zpass",
+               "fft_xy_fused": "baorec_set_tune_xy", "stream_residuals": "baorec_set_tune_stream"}
+    for kv in filter(None, args.set_tune.split(",")):
+        k, v = kv.split("=")
+        for c_ in [ctx] + list(others.values()):
+            c_.call(setters[k], int(v))
+        tune[k] = int(v)
     nd, nr = len(m.x), len(m.rx)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
