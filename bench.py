@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--batch-mocks", type=int, default=64)
     ap.add_argument("--set-tune", default="",
                     help="after the autotuner, force choices: comma-separated key=value of pair_residual, "
-                         "fft_zpass, fft_xy_fused, stream_residuals (a profiler distorts the tuner's timings, "
+                         "fft_zpass, fft_xy_fused, stream_residuals, tiles (per level, 1:1:0:0) (a profiler "
+                         "distorts the tuner's timings, "
                          "so a launch list under ncu pins the choices of the timed run)")
     ap.add_argument("--conv-only", action="store_true",
                     help="only time the learned guess's tensor-core convolutions, every shape on a --mesh grid "
@@ -408,6 +409,12 @@ def run_gb300(args):
                "fft_xy_fused": "baorec_set_tune_xy", "stream_residuals": "baorec_set_tune_stream"}
     for kv in filter(None, args.set_tune.split(",")):
         k, v = kv.split("=")
+        if k == "tiles":   # per-level tile choices, e.g. tiles=1:1:0:0 (1 = 32x16x16, 0 = 32x8x8)
+            bt = [int(x) for x in v.split(":")] + [-1] * 16
+            for c_ in [ctx] + list(others.values()):
+                c_.call("baorec_set_tune", int(tune["paint_tile"]), (C.c_int32 * 16)(*bt[:16]))
+            tune["tile16_per_level"] = bt[:16]
+            continue
         for c_ in [ctx] + list(others.values()):
             c_.call(setters[k], int(v))
         tune[k] = int(v)
