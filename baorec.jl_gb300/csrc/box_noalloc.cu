@@ -13,6 +13,14 @@
 // particles, so a call accepts at most kMaxParticles = 16,777,216 particles
 // and rejects larger catalogs with BAOREC_ERR_TOO_LARGE.  Every GPU that
 // loads the library holds the 24.6 KB array until the process exits.
+//
+// The call is synchronous: it waits for its stream and copies six values into
+// host stack memory, neither of which is allowed while the stream is being
+// captured, so a call on a capturing stream is refused (BAOREC_ERR_ARG)
+// before anything is enqueued.  The array's device address is looked up once
+// per device and cached; cudaDeviceReset unloads the module that holds the
+// array, so a process that resets a device must not call this entry point on
+// that device again.
 #include <mutex>
 
 #include "common.cuh"
@@ -100,6 +108,18 @@ cudaError_t scratch_for_current_device(float** out) {
   return cudaSuccess;
 }
 
+// The particle arrays must be device (or managed) memory of the current
+// device: the kernels run there, next to the scratch array of that device.
+bool on_current_device(const void* p, int dev) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) return false;
+  return at.type == cudaMemoryTypeManaged || at.device == dev;
+}
+
 }  // namespace
 }  // namespace baorec
 
@@ -108,9 +128,18 @@ extern "C" int baorec_setup_box_noalloc(const float* x, const float* y, const fl
   using namespace baorec;
   if (!x || !y || !z || !box_size_out || !box_min_out || n < 1) return BAOREC_ERR_ARG;
   if (n > kMaxParticles) return BAOREC_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BAOREC_ERR_CUDA;
+  if (!on_current_device(x, dev) || !on_current_device(y, dev) || !on_current_device(z, dev)) return BAOREC_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return BAOREC_ERR_ARG;
+  }
+  if (cap != cudaStreamCaptureStatusNone) return BAOREC_ERR_ARG;
   float* part = nullptr;
   if (scratch_for_current_device(&part) != cudaSuccess) return BAOREC_ERR_CUDA;
-  cudaStream_t s = (cudaStream_t)stream;
   const int nblocks = (int)((n + (int64_t)kThreads * kItemsPerThread - 1) / ((int64_t)kThreads * kItemsPerThread));
   box_partial_noalloc_kernel<<<nblocks, kThreads, 0, s>>>(x, y, z, n, part);
   if (cudaGetLastError() != cudaSuccess) return BAOREC_ERR_CUDA;

@@ -4,7 +4,7 @@
  * Each entry point replaces one function of BAOrec.jl's reconstruction path;
  * the comment above it names the Julia method (file:line inside the BAOrec.jl
  * project) whose behaviour it reproduces.  A Julia package binds these with
- * `ccall`, Python with ctypes.
+ * `ccall`, Python with ctypes (baorec.jl_gb300/baorec/_lib.py).
  *
  * Conventions
  *  - Every function returns a baorec_status (0 = success).  On failure
@@ -142,10 +142,15 @@ int baorec_setup_box(baorec_ctx* ctx, const float* x, const float* y, const floa
  * partial results in a fixed 24.6 KB device array that every GPU loading the
  * library holds until exit.  x, y, z are device arrays of n particles; at most
  * 16,777,216 particles per call (larger n returns BAOREC_ERR_TOO_LARGE, n < 1
- * BAOREC_ERR_ARG).  The outputs are host arrays.  Work runs on `stream`
- * (cudaStream_t, NULL = legacy default stream) and the call waits for it.
- * The first call on each device looks up the array's device address (with
- * that device current); make that first call before any stream capture.
+ * BAOREC_ERR_ARG).  x, y, z must be device or managed memory of the current
+ * device (anything else is BAOREC_ERR_ARG).  The outputs are host arrays.
+ * Work runs on `stream` (cudaStream_t, NULL = legacy default stream) and the
+ * call is synchronous: it waits for that stream, so it cannot be recorded
+ * into a CUDA graph, and a call on a stream that is being captured returns
+ * BAOREC_ERR_ARG without touching the capture.  The first call on each device
+ * looks up the array's device address (with that device current) and caches
+ * it; after cudaDeviceReset of a device the cached address is stale, so do
+ * not call this entry point on that device again in the same process.
  * All calls share the one array: calls that overlap on the GPU race. */
 int baorec_setup_box_noalloc(const float* x, const float* y, const float* z, int64_t n, float pad,
                              void* stream, float box_size_out[3], float box_min_out[3]);

@@ -225,3 +225,34 @@ void prolong(float* v, const float* c, int n1, int n2, int n3, int add) {
         for (int q = 0; q < 8; ++q) v[o[q]] = add ? v[o[q]] + val[q] : val[q];
       }
 }
+
+/* A v in FP64 arithmetic with the FP32 coefficients of src/multigrid.jl:17-29,
+ * 55-62 (computed in FP32 by coef(), exactly as the FP32 restatement rounds
+ * them) and the operator of src/multigrid.jl:262-276: 2 Σ gp_i v - bracket.
+ * This is the accuracy judge's operator: the FP64 solution of the same
+ * discrete system the FP32 code solves. */
+void apply_op_f64(double* out, const double* v, int n1, int n2, int n3, const float* L, const float* P0,
+                  const float* P1, const float* P2, const float* los, float beta) {
+  geom_t G;
+  geom_init(&G, n1, n2, n3, L, P0, P1, P2, los, beta);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 0; k < n3; ++k)
+    for (int j = 0; j < n2; ++j)
+      for (int i = 0; i < n1; ++i) {
+        float gpf[3], gf, pf[3];
+        coef(&G, i, j, k, gpf, &gf, pf);
+        const double gp0 = gpf[0], gp1 = gpf[1], gp2 = gpf[2], g = gf, p0 = pf[0], p1 = pf[1], p2 = pf[2];
+        int ip = i + 1 == n1 ? 0 : i + 1, im = i == 0 ? n1 - 1 : i - 1;
+        int jp = j + 1 == n2 ? 0 : j + 1, jm = j == 0 ? n2 - 1 : j - 1;
+        int kp = k + 1 == n3 ? 0 : k + 1, km = k == 0 ? n3 - 1 : k - 1;
+        double s = gp0 * (v[IDX(ip, j, k)] + v[IDX(im, j, k)]) + gp1 * (v[IDX(i, jp, k)] + v[IDX(i, jm, k)]) +
+                   gp2 * (v[IDX(i, j, kp)] + v[IDX(i, j, km)]) +
+                   g / 2 * (p0 * p1 * (v[IDX(ip, jp, k)] + v[IDX(im, jm, k)] - v[IDX(im, jp, k)] - v[IDX(ip, jm, k)]) +
+                            p0 * p2 * (v[IDX(ip, j, kp)] + v[IDX(im, j, km)] - v[IDX(im, j, kp)] - v[IDX(ip, j, km)]) +
+                            p1 * p2 * (v[IDX(i, jp, kp)] + v[IDX(i, jm, km)] - v[IDX(i, jm, kp)] - v[IDX(i, jp, km)]));
+        if (G.local)
+          s += g * (p0 * (v[IDX(ip, j, k)] - v[IDX(im, j, k)]) + p1 * (v[IDX(i, jp, k)] - v[IDX(i, jm, k)]) +
+                    p2 * (v[IDX(i, j, kp)] - v[IDX(i, j, km)]));
+        out[IDX(i, j, k)] = 2 * (gp0 + gp1 + gp2) * v[IDX(i, j, k)] - s;
+      }
+}

@@ -53,3 +53,32 @@ def test_struct_layout_matches_header(lib):
     assert ctypes.sizeof(_lib.Config) == 4 * 31
     assert ctypes.sizeof(_lib.SolveStats) == 32
     assert ctypes.sizeof(_lib.GuessTrainConfig) == 4 * 20
+
+
+def test_field_offsets_match_header(tmp_path):
+    """Every field of every struct: offsetof from a C program compiled against
+    the header equals the ctypes mirror's offset (and the struct sizes)."""
+    import shutil
+    import subprocess
+    from baorec import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = tmp_path / "abi_layout"
+    subprocess.run([cc, "-std=c11", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_layout.c"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    mirror = {"baorec_config": _lib.Config, "baorec_solve_stats": _lib.SolveStats,
+              "baorec_batch_item": _lib.BatchItem, "baorec_guess_train_config": _lib.GuessTrainConfig,
+              "baorec_power_config": _lib.PowerConfig}
+    seen = {k: set() for k in mirror}
+    for line in out.splitlines():
+        st, field, val = line.split()
+        cls = mirror[st]
+        if field == "sizeof":
+            assert ctypes.sizeof(cls) == int(val), st
+        else:
+            assert getattr(cls, field).offset == int(val), (st, field)
+            seen[st].add(field)
+    for st, cls in mirror.items():
+        assert seen[st] == {name for name, _ in cls._fields_}, st

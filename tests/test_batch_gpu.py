@@ -1,9 +1,14 @@
 """Batched box reconstructions in one CUDA graph: every mock's shifted
 positions equal those of the same mock reconstructed alone through the
 per-mock API (mixed meshes, boxes, CIC/TSC and smoothing radii), and a
-replay reproduces them."""
+replay reproduces them.  One CIC and one TSC mock are also checked against
+the oracle pipeline (src/recon.jl:134-153 with src/iterative.jl,
+src/mas.jl:218-269, src/recon.jl:264-388), so an error shared by the batch
+and the per-mock path cannot hide."""
 import numpy as np
 import pytest
+
+import baorec_oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -50,4 +55,14 @@ def test_batch_matches_single_mock_reconstructions():
             # float atomics in the paint may add in another order: Mpc/h-level agreement far below 1e-3
             assert np.max(np.abs(got - np.asarray(ref[a]))) < 1e-3
             assert np.max(np.abs(got - f0[a])) < 1e-3
+    # the oracle pipeline for the first CIC and the first TSC mock
+    for i in (0, 1):
+        n, L, mas, R, np_, _ = SPECS[i]
+        m = cat[i]
+        d, _, _, pos = O.run_iterative((n,) * 3, 2.0, 0.8, R, m.x, m.y, m.z, m.w, box_size=[L] * 3,
+                                       box_min=[0.0] * 3, los=[0.0, 0.0, 1.0], n_iter=3, mas=mas)
+        disp = O.compute_displacements_iterative(d, *pos, [L] * 3, [0.0] * 3)
+        ref = O.reconstructed_positions(O.read_shifts(disp, *pos, 0.8, los=[0.0, 0.0, 1.0], field="sum"), *pos)
+        for a in range(3):
+            assert np.max(np.abs(outs[i][a].cpu().numpy() - ref[a])) < 1e-3, (i, a)
     b.close()

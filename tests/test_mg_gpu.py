@@ -258,3 +258,30 @@ def test_z_pass_preconditioner_matches_3d_transforms(los):
         assert abs(rels[0] - rel) <= 1e-4 * rels[0] + 2e-6
         assert [k for _, k in h0] == [k for _, k in h1]
         assert rel_l2(p1 - p1.mean(), p0 - p0.mean()) < 1e-5
+
+
+def test_cycle_cap_returns_not_converged_with_the_last_iterate():
+    """At the V-cycle cap the solve returns BAOREC_ERR_NOT_CONVERGED, φ holds
+    the last iterate (its FP64 residual is the reported one), and the plain
+    method continued from that iterate reaches the tolerance."""
+    import baorec
+    from baorec import _lib
+    f, bs, bm = _problem(n=32, seed=3)
+    ff = np.asfortranarray(f)
+    rec = _recon(bs, bm, None, mg_mode="convergent", rtol=1e-6, max_cycles=1, start="zero")
+    phi = baorec.zeros_mesh(f.shape, device=False)
+    with pytest.raises(_lib.NotConverged):
+        baorec.solve_(phi, ff, rec)
+    st = rec.solve_stats
+    assert st["status"] == _lib.ERR_NOT_CONVERGED
+    assert st["cycles"] == 1 and st["rel_residual"] > 1e-6
+    coef = O.coefs_f64(O.stencil_coefficients(f.shape, bs, bm, rec.beta, None, F32))
+    r = (f.astype(np.float64) - st["alpha"]) - O.apply_operator(np.asarray(phi, np.float64), coef, True)
+    rel = np.linalg.norm(r - r.mean()) / np.linalg.norm(f.astype(np.float64) - st["alpha"])
+    assert abs(rel - st["rel_residual"]) <= 0.05 * st["rel_residual"], (rel, st)
+    # the fallback: more V-cycles from the capped iterate
+    rec2 = _recon(bs, bm, None, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="zero")
+    phi2 = baorec.zeros_mesh(f.shape, device=False)
+    st2 = baorec.solve_(phi2, ff, rec2, phi0=np.asfortranarray(phi))
+    assert st2["rel_residual"] <= 1e-6
+    assert st2["rel_residual_initial"] <= 1.05 * st["rel_residual"]

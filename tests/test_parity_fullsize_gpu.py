@@ -1,0 +1,163 @@
+"""End-to-end parity of the benchmarked workloads at their full sizes.
+
+Lightcone (the benchmark's workload): 5e5 data + 5e6 randoms on the shell
+r = 1000-1500 Mpc/h, RA 0-90, Dec 0-45, 256^3 mesh over setup_box(randoms,
+25), CIC, R = 15, b = 2, f = 0.8, radial line of sight, residual-driven solve
+to a 1e-6 relative residual, launch shapes from the autotuner as the
+benchmark picks them.  The reference's path for it is
+src/recon.jl:184-212 -> src/multigrid.jl:755-773 -> src/mas.jl:218-269 ->
+src/recon.jl:264-306.
+
+* The right-hand side (setup_overdensity! with randoms, src/recon.jl:60-91)
+  matches the FP32 oracle; cells where the randoms' threshold test flips
+  between the two paints (their rounding differs) are counted, not compared.
+* For every start (plain V-cycles, FFT start, learned start) the gradient of
+  the potential is within 1e-5 (relative L2) of the FP64 solution of the same
+  system (oracle/fp64_oracle.py), which is the displacement bar.
+* The shifted positions of the composed call (reconstructed_potential! then
+  reconstructed_positions :sum for the data, :sum and :disp for the
+  randoms) are within 1e-3 Mpc/h of the oracle pipeline: FP32 paint, smoothing
+  and normalisation, FP64 solve, FP32 read-out and shift.
+
+Box (the periodic-box workload): 2e5 particles from the lognormal field,
+128^3 mesh, L = 1000, CIC, R = 15, b = 2, f = 0.8, LOS +z, 3 iterations
+(run!, src/recon.jl:134-153): shifted positions within 1e-3 Mpc/h of the FP32
+oracle and the displacement field within 1e-5 of the FP64 oracle run.
+"""
+import numpy as np
+import pytest
+
+import baorec_oracle as O
+import fp64_oracle as P
+from _util import F32
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+BIAS, GROWTH, R = 2.0, 0.8, 15.0
+BETA = F32(F32(GROWTH) / F32(BIAS))
+WEIGHTS = "baorec.jl_gb300/weights/guess_lightcone.npy"
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _mesh_np(t):
+    """x-fastest CUDA mesh -> NumPy [ix, iy, iz]."""
+    return t.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def headline():
+    import os
+    import torch
+    import baorec
+    from baorec import mocks
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    torch.cuda.set_device(0)
+    m = mocks.lightcone_mock(n_data=500_000, rand_factor=10, n_grid=N, seed=2024)
+    bs, bm = O.setup_box(m.rx, m.ry, m.rz, 25.0)
+    X = [_dev(a) for a in (m.x, m.y, m.z, m.w)]
+    Rr = [_dev(a) for a in (m.rx, m.ry, m.rz, m.rw)]
+    recs = {}
+    for start in ("zero", "spectral", "learned"):
+        gp = baorec.guess.load_params(os.path.join(root, WEIGHTS)) if start == "learned" else None
+        rec = baorec.MultigridRecon(bias=BIAS, f=GROWTH, smoothing_radius=R, box_size=bs, box_min=bm, los=None,
+                                    mg_mode="convergent", rtol=1e-6, nu1=2, nu2=2, max_cycles=50, start=start,
+                                    guess_params=gp)
+        ctx = baorec.setup_fft_(rec, (N,) * 3)
+        ctx.autotune(paint=start == "spectral")
+        recs[start] = rec
+    # the GPU right-hand side, and the FP64 solution of exactly that system
+    f_gpu = baorec.zeros_mesh((N,) * 3)
+    baorec.setup_overdensity_(f_gpu, recs["spectral"], *X, *Rr)
+    f_gpu_np = _mesh_np(f_gpu)
+    phi64, alpha64, hist = P.solve(f_gpu_np, bs, bm, BETA, None, rtol=1e-11)
+    grad64 = P.gradient_meshes(phi64, bs.astype(np.float64))
+    # the oracle pipeline from the particles
+    f_or = O.setup_overdensity_randoms(np.zeros((N,) * 3, F32), BIAS, R, bs, bm, m.x, m.y, m.z, m.w,
+                                       m.rx, m.ry, m.rz, m.rw)
+    return dict(m=m, bs=bs, bm=bm, X=X, R=Rr, recs=recs, f_gpu=f_gpu, f_gpu_np=f_gpu_np, grad64=grad64,
+                f_or=f_or, fp64_hist=hist)
+
+
+def test_headline_rhs_matches_fp32_oracle(headline):
+    f, fo = headline["f_gpu_np"], headline["f_or"]
+    flips = (f == 0) != (fo == 0)
+    nflip = int(flips.sum())
+    print("threshold flips", nflip, "of", f.size)
+    assert nflip <= 8
+    keep = ~flips
+    err = float(np.linalg.norm((f - fo)[keep].astype(np.float64)) / np.linalg.norm(fo[keep].astype(np.float64)))
+    print("rhs rel-L2 (flips excluded)", err)
+    assert err < 1e-5
+
+
+@pytest.mark.parametrize("start", ["zero", "spectral", "learned"])
+def test_headline_gradient_within_1e5_of_fp64(headline, start):
+    import baorec
+    rec = headline["recs"][start]
+    phi = baorec.zeros_mesh((N,) * 3)
+    st = baorec.solve_(phi, headline["f_gpu"], rec)
+    assert st["rel_residual"] <= 1e-6, st
+    g = baorec.compute_displacements(phi, rec)
+    err = P.rel_l2_vector([_mesh_np(t) for t in g], headline["grad64"])
+    print(start, "grad rel-L2 vs FP64", err, st)
+    assert err < 1e-5
+
+
+def test_headline_shifted_positions_match_oracle_pipeline(headline):
+    import baorec
+    h = headline
+    rec = h["recs"]["spectral"]
+    phi = baorec.zeros_mesh((N,) * 3)
+    baorec.reconstructed_potential_(phi, rec, *h["X"], *h["R"])
+    assert rec.solve_stats["rel_residual"] <= 1e-6
+    got_d = baorec.reconstructed_positions(rec, *h["X"][:3], field="sum")
+    got_rs, got_ri = baorec.reconstructed_positions2(rec, *h["R"][:3], fields=("sum", "disp"))
+    # oracle: FP64 solve of the oracle's own right-hand side, FP32 read-out and shift
+    bs, bm, m = h["bs"], h["bm"], h["m"]
+    phi64, _, _ = P.solve(h["f_or"], bs, bm, BETA, None, rtol=1e-11)
+    grads = tuple(g.astype(F32) for g in P.gradient_meshes(phi64, bs.astype(np.float64)))
+    worst = 0.0
+    for (x, y, z), field, got in (((m.x, m.y, m.z), "sum", got_d), ((m.rx, m.ry, m.rz), "sum", got_rs),
+                                  ((m.rx, m.ry, m.rz), "disp", got_ri)):
+        disp = tuple(O.read_cic(g, x, y, z, bs, bm) for g in grads)
+        ref = O.reconstructed_positions(O.read_shifts(disp, x, y, z, GROWTH, los=None, field=field), x, y, z)
+        for a in range(3):
+            worst = max(worst, float(np.max(np.abs(got[a].cpu().numpy() - ref[a]))))
+    print("max |dpos| vs oracle pipeline", worst, "Mpc/h")
+    assert worst < 1e-3
+
+
+def test_box_config_matches_oracle_and_fp64():
+    import torch
+    import baorec
+    from baorec import mocks
+    torch.cuda.set_device(0)
+    n, L = 128, 1000.0
+    m = mocks.box_mock(n_part=200_000, L=L, n_grid=n, seed=1234)
+    los = [0.0, 0.0, 1.0]
+    rec = baorec.IterativeRecon(bias=BIAS, f=GROWTH, smoothing_radius=R, box_size=[L] * 3, box_min=[0.0] * 3,
+                                los=los, n_iter=3)
+    x, y, z = m.x.copy(), m.y.copy(), m.z.copy()
+    delta = baorec.run_(rec, (n,) * 3, x, y, z, m.w)
+    got = baorec.reconstructed_positions(rec, x, y, z, field="sum")
+    # FP32 oracle pipeline (the reference CPU's arithmetic)
+    d32, _, _, pos = O.run_iterative((n,) * 3, BIAS, GROWTH, R, m.x, m.y, m.z, m.w, box_size=[L] * 3,
+                                     box_min=[0.0] * 3, los=los, n_iter=3)
+    disp = O.compute_displacements_iterative(d32, *pos, [L] * 3, [0.0] * 3)
+    ref = O.reconstructed_positions(O.read_shifts(disp, *pos, GROWTH, los=los, field="sum"), *pos)
+    worst = max(float(np.max(np.abs(got[a] - ref[a]))) for a in range(3))
+    print("box max |dpos| vs FP32 oracle", worst)
+    assert worst < 1e-3
+    # displacement field against the FP64 oracle run
+    d64, _, _, _ = O.run_iterative((n,) * 3, BIAS, GROWTH, R, m.x, m.y, m.z, m.w, box_size=[L] * 3,
+                                   box_min=[0.0] * 3, los=los, n_iter=3, dtype=np.float64)
+    psi64 = O.displacement_meshes_iterative(d64, np.array([L] * 3))
+    psi = baorec.compute_displacements(delta, rec)
+    err = P.rel_l2_vector([_mesh_np(t) for t in psi], psi64)
+    print("box displacement rel-L2 vs FP64", err)
+    assert err < 1e-5

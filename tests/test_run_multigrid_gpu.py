@@ -1,0 +1,88 @@
+"""run! for a MultigridRecon with randoms (src/recon.jl:215-261), end to end
+against the oracle: the box is replaced by setup_box(randoms, 500)
+(src/recon.jl:253) exactly, and the shifted positions of the composed call
+match the oracle pipeline (FP32 paint, smoothing and normalisation on the
+same box, then the FP64 solution for the residual-driven solve, or the FP32
+FMG schedule of src/multigrid.jl:722-752 for the reference mode), read out and
+shifted in FP32 (src/mas.jl:218-269, src/recon.jl:264-306, 366-388)."""
+import numpy as np
+import pytest
+
+import baorec_oracle as O
+import fp64_oracle as P
+from _util import F32, small_lightcone
+
+pytestmark = pytest.mark.gpu
+
+BIAS, GROWTH, R = 2.0, 0.8, 15.0
+BETA = F32(F32(GROWTH) / F32(BIAS))
+
+
+def _oracle_positions(grads, m, bs, bm):
+    out = []
+    for (x, y, z), field in (((m.x, m.y, m.z), "sum"), ((m.rx, m.ry, m.rz), "sum"), ((m.rx, m.ry, m.rz), "disp")):
+        disp = tuple(O.read_cic(g, x, y, z, bs, bm) for g in grads)
+        out.append(O.reconstructed_positions(O.read_shifts(disp, x, y, z, GROWTH, los=None, field=field), x, y, z))
+    return out
+
+
+def _gpu_positions(rec, m, device):
+    import baorec
+    import torch
+    if device:
+        d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        xs, rs = [d(a) for a in (m.x, m.y, m.z)], [d(a) for a in (m.rx, m.ry, m.rz)]
+    else:
+        xs, rs = [m.x, m.y, m.z], [m.rx, m.ry, m.rz]
+    g = lambda t: np.asarray(t.cpu().numpy() if hasattr(t, "cpu") else t)
+    out = [tuple(g(a) for a in baorec.reconstructed_positions(rec, *xs, field="sum"))]
+    out += [tuple(g(a) for a in baorec.reconstructed_positions(rec, *rs, field=f)) for f in ("sum", "disp")]
+    return out
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_run_convergent_matches_oracle(device):
+    import baorec
+    import torch
+    n = 64
+    m = small_lightcone(n_data=40000, rand_factor=5, n_grid=n, seed=21)
+    rec = baorec.MultigridRecon(bias=BIAS, f=GROWTH, smoothing_radius=R, mg_mode="convergent", rtol=1e-6,
+                                start="spectral")
+    args = [m.x, m.y, m.z, m.w, m.rx, m.ry, m.rz, m.rw]
+    if device:
+        args = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in args]
+    baorec.run_(rec, (n,) * 3, *args)
+    obs, obm = O.setup_box(m.rx, m.ry, m.rz, 500.0)
+    np.testing.assert_array_equal(np.asarray(rec.box_size, F32), obs)
+    np.testing.assert_array_equal(np.asarray(rec.box_min, F32), obm)
+    assert rec.solve_stats["rel_residual"] <= 1e-6
+    got = _gpu_positions(rec, m, device)
+    f = O.setup_overdensity_randoms(np.zeros((n,) * 3, F32), BIAS, R, obs, obm, m.x, m.y, m.z, m.w,
+                                    m.rx, m.ry, m.rz, m.rw)
+    phi64, _, _ = P.solve(f, obs, obm, BETA, None, rtol=1e-11)
+    grads = tuple(a.astype(F32) for a in P.gradient_meshes(phi64, obs.astype(np.float64)))
+    ref = _oracle_positions(grads, m, obs, obm)
+    worst = max(float(np.max(np.abs(g[a] - r[a]))) for g, r in zip(got, ref) for a in range(3))
+    print("convergent run! max |dpos|", worst)
+    assert worst < 1e-3
+
+
+def test_run_reference_schedule_matches_fp32_oracle():
+    """The reference FMG schedule (damped Jacobi, 6 cycles per level, no
+    residual test) is a fixed FP32 iteration: its positions follow the FP32
+    oracle's FMG to the rounding the iteration accumulates (the reference's
+    own CPU and GPU runs agree to 9.3e-4 Mpc/h, test/bchmk_*_mgrid.csv)."""
+    import baorec
+    n = 64
+    m = small_lightcone(n_data=40000, rand_factor=5, n_grid=n, seed=22)
+    rec = baorec.MultigridRecon(bias=BIAS, f=GROWTH, smoothing_radius=R)
+    baorec.run_(rec, (n,) * 3, m.x, m.y, m.z, m.w, m.rx, m.ry, m.rz, m.rw)
+    phi_o, obs, obm = O.run_multigrid((n,) * 3, BIAS, GROWTH, R, m.x, m.y, m.z, m.w,
+                                      randoms=(m.rx, m.ry, m.rz, m.rw))
+    np.testing.assert_array_equal(np.asarray(rec.box_size, F32), obs)
+    np.testing.assert_array_equal(np.asarray(rec.box_min, F32), obm)
+    got = _gpu_positions(rec, m, False)
+    ref = _oracle_positions(O.gradient_meshes(phi_o, obs), m, obs, obm)
+    worst = max(float(np.max(np.abs(g[a] - r[a]))) for g, r in zip(got, ref) for a in range(3))
+    print("reference-schedule run! max |dpos|", worst)
+    assert worst < 1e-3
