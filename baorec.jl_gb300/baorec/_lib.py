@@ -151,6 +151,8 @@ _SIGS = {
     "baorec_guess_get_params": (C.c_int, [P, P, I64]),
     "baorec_guess_eval": (C.c_int, [P, P, P, P, P, C.POINTER(C.c_double), C.c_int]),
     "baorec_guess_apply": (C.c_int, [P, P, P]),
+    "baorec_guess_set_level": (C.c_int, [P, C.c_int32]),
+    "baorec_guess_level": (C.c_int32, [P]),
     "baorec_guess_sample": (C.c_int, [P, C.POINTER(GuessTrainConfig), I64, P, P]),
     "baorec_guess_train": (C.c_int, [P, C.POINTER(GuessTrainConfig), P]),
     "baorec_set_gradient": (C.c_int, [P, C.c_int32]),

@@ -92,6 +92,7 @@ class MultigridRecon:
     start: str = "zero"                  # convergent mode: "zero" | "spectral" | "learned"
     start_rate: float = 0.5
     guess_params: object = None          # learned start: network parameters (baorec.guess)
+    guess_level: int = 0                 # learned start: 0 network on this mesh, 1 on its first restriction
     gradient: str = "fft"                # displacement from φ: "fft" (reference) | "fd" (central differences)
     solve_stats: dict = dc_field(default_factory=dict)
 
@@ -289,6 +290,7 @@ def _ctx(recon, shape, ran_min=0.01) -> _lib.Context:
         ctx = _lib.Context(cfg)
         recon.fft_plan = ctx
         if getattr(recon, "guess_params", None) is not None:
+            ctx.call("baorec_guess_set_level", int(getattr(recon, "guess_level", 0)))
             p = np.ascontiguousarray(recon.guess_params, dtype=np.float32)
             ctx.call("baorec_guess_set_params", p.ctypes.data, p.size)
     elif recon.box_size is not None and recon.box_min is not None:

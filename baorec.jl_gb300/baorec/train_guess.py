@@ -1,13 +1,19 @@
 """Train the learned initial guess on the device and write its parameters.
 
-    python -m baorec.train_guess --steps 2000 --out baorec.jl_gb300/weights/guess_lightcone.npy
+    python -m baorec.train_guess --steps 20000 --n 128 --mesh 128 \
+        --out baorec.jl_gb300/weights/guess_lightcone.npy
 
-(run with baorec.jl_gb300 on sys.path).  Training pairs are 128^3 sub-boxes,
-at the cell size of the 256^3 lightcone workload, of synthetic lognormal
-fields in that workload's survey window (shell 1000-1500 Mpc/h, RA 0-90 deg,
-Dec 0-45 deg), solved to 5e-7 by the residual-driven solver; the loss is the
-mean squared Laplacian of the potential error.  Prints the loss history in
-tenths and the held-out start residuals (FFT start vs learned start).
+(run with baorec.jl_gb300 on sys.path).  Training pairs are n^3 boxes at the
+cell size of a mesh^3 grid over the lightcone workload's box (with n = mesh =
+128 every pair covers the whole box at 11.9 Mpc/h: the first restriction of
+the 256^3 workload, where guess_level 1 runs the network), filled with
+synthetic lognormal fields in the survey window (shell 1000-1500 Mpc/h,
+RA 0-90 deg, Dec 0-45 deg) and solved to 5e-7 by the residual-driven solver;
+the loss is the mean squared Laplacian of the potential error, Adam at lr
+1e-3, batch 4.  Training runs in chunks of --chunk steps (fresh fields in
+every chunk, the Adam state carried over); after each chunk the parameters
+are written to --checkpoints (if given) and the held-out start residuals
+(FFT start vs learned start) are printed as one JSON line.
 """
 from __future__ import annotations
 
@@ -56,21 +62,36 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--mesh", type=int, default=256, help="cell size of a mesh^3 grid over the workload box")
+    ap.add_argument("--chunk", type=int, default=0, help="steps per chunk (0: one chunk)")
+    ap.add_argument("--checkpoints", default=None, help="directory for the parameters after each chunk")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
-    ctx, cfg = training_context(a.n)
-    cfg.steps, cfg.batch, cfg.lr, cfg.seed = a.steps, a.batch, a.lr, a.seed + 1000
+    ctx, cfg = training_context(a.n, a.mesh)
+    cfg.batch, cfg.lr = a.batch, a.lr
     guess.init(ctx, a.seed)
     before = held_out(ctx, cfg)
-    t0 = time.time()
-    hist = guess.train(ctx, cfg)
+    chunk = a.chunk if a.chunk > 0 else a.steps
+    hist_all, done, t0 = [], 0, time.time()
+    while done < a.steps:
+        k = min(chunk, a.steps - done)
+        cfg.steps, cfg.seed = k, a.seed + 1000 + done   # fresh fields in every chunk
+        hist_all.append(guess.train(ctx, cfg))
+        done += k
+        after = held_out(ctx, cfg)
+        if a.checkpoints:
+            import os
+            os.makedirs(a.checkpoints, exist_ok=True)
+            guess.save(os.path.join(a.checkpoints, f"guess_step{done}.npy"), guess.get_params(ctx))
+        print(json.dumps({"steps_done": done, "seconds": time.time() - t0, "loss": float(np.mean(hist_all[-1])),
+                          "mean_ratio_learned_over_fft": float(np.mean([b / a_ for a_, b in after]))}), flush=True)
     dt = time.time() - t0
-    after = held_out(ctx, cfg)
+    hist = np.concatenate(hist_all)
     p = guess.get_params(ctx)
     if a.out:
         guess.save(a.out, p)
     print(json.dumps({
-        "steps": a.steps, "batch": a.batch, "lr": a.lr, "train_seconds": dt,
+        "steps": a.steps, "batch": a.batch, "lr": a.lr, "n": a.n, "mesh": a.mesh, "train_seconds": dt,
         "loss_tenths": [float(np.mean(h)) for h in np.array_split(hist, 10)] if len(hist) >= 10 else hist.tolist(),
         "held_out_untrained": before, "held_out_trained": after,
         "mean_ratio_learned_over_fft": float(np.mean([b / a_ for a_, b in after])),

@@ -270,6 +270,9 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   cudaFree(ctx->coarse_M);
   cudaFree(ctx->stab);
   guess_free(ctx);
+  if (ctx->guess_child) baorec_destroy(ctx->guess_child);
+  for (cudaEvent_t e : ctx->ev_guess)
+    if (e) cudaEventDestroy(e);
   for (int l = 0; l < ctx->nlev; ++l) {
     cudaFree(ctx->lev[l].f);
     for (int a = 0; a < 3; ++a) cudaFree(ctx->lev[l].ax[a]);

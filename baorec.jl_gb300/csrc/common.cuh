@@ -94,6 +94,12 @@ struct baorec_ctx {
   int dense_level = -1;                // first level with at most 512 cells
   bool coarse_dirty = true;            // coarse_M / dense_level need rebuilding
   baorec::GuessNet* net = nullptr;     // learned initial guess (weights, workspace)
+  // learned guess on the first restriction (guess_level 1): a context at n/2
+  // per axis over the same box owns the network; events order its stream
+  // after this context's and back
+  baorec_ctx* guess_child = nullptr;
+  int guess_level = 0;
+  cudaEvent_t ev_guess[2] = {nullptr, nullptr};
   // deterministic paint scratch: tile keys, permutation, tile counts/offsets, fixed-point mesh
   baorec::DevBuf sort_keys, sort_perm, sort_tiles, fix_mesh;
   baorec::DevBuf pw_mesh, pw_spec, pw_part, pw_nz;   // power-spectrum scratch (power.cu)
@@ -215,6 +221,8 @@ int positions_device(baorec_ctx* ctx, const float* x, const float* y, const floa
                      float* ox, float* oy, float* oz);
 // learned initial guess (guess_net.cu)
 int guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
+// guess_apply on this mesh, or on its first restriction when guess_level is 1
+int guess_dispatch_apply(baorec_ctx* ctx, const float* f, float* phi0);
 void guess_free(baorec_ctx* ctx);
 int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);
 int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out);

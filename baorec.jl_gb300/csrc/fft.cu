@@ -24,6 +24,7 @@ namespace {
 
 struct KGeom {
   int n1h, n2, n3;
+  int nyq[3];      // index of the Nyquist mode per axis (n/2), -1 for odd n
   float mult[3];   // T(fs/n), fs = T(2π n / L) — the k-axis step of k_vec (src/utils.jl:3-10)
   float invN;
 };
@@ -35,9 +36,40 @@ KGeom kgeom_of(const baorec_ctx* c) {
   for (int a = 0; a < 3; ++a) {
     float fs = (float)(2.0 * 3.14159265358979323846 * (double)n[a] / (double)c->cfg.box_size[a]);
     g.mult[a] = fs / (float)n[a];
+    g.nyq[a] = n[a] % 2 == 0 ? n[a] / 2 : -1;
   }
   g.invN = (float)(1.0 / (double)c->N);
   return g;
+}
+
+// Hermitian part of a spectral product in the planes a C2R reads as Hermitian.
+//
+// A real field's half-complex spectrum F satisfies F(partner) = conj F, where
+// inside the kx = 0 and kx = n1/2 planes the partner of (ky, kz) is
+// (-ky, -kz) and the Nyquist indices n/2 are their own partners (their k value
+// is the same -k_nyq on both sides; the kx = n1/2 plane is its own partner in
+// x).  A factor odd in k_a flips sign between partners except where the
+// a-index is its own partner, so on those entries i k_a F (a derivative) or
+// k_a k_b F with exactly one self-partnered index (a mixed Hessian term) is
+// anti-Hermitian.  FFTW's c2r (the reference's plan_rfft inverse) and
+// pocketfft read only the Hermitian part of these two planes; cuFFT resolves
+// the rest differently.  The kernels below therefore write the Hermitian part,
+// zero on those entries, so every correct C2R gives the reference's field.
+__device__ __forceinline__ bool in_real_plane(const KGeom& g, int i) { return i == 0 || i == g.nyq[0]; }
+
+// index along axis a is its own partner (x: always, inside the two planes)
+__device__ __forceinline__ bool self_partner(const KGeom& g, int a, int j, int k) {
+  return a == 0 ? true : (a == 1 ? j == g.nyq[1] : k == g.nyq[2]);
+}
+
+// entry (i, j, k) of (odd factor in a) x F is anti-Hermitian: drop it
+__device__ __forceinline__ bool drop_odd(const KGeom& g, int a, int i, int j, int k) {
+  return in_real_plane(g, i) && self_partner(g, a, j, k);
+}
+
+// entry of (odd in a) x (odd in b) x F, a != b, is anti-Hermitian: drop it
+__device__ __forceinline__ bool drop_odd2(const KGeom& g, int a, int b, int i, int j, int k) {
+  return in_real_plane(g, i) && (self_partner(g, a, j, k) != self_partner(g, b, j, k));
 }
 
 // k axes of k_vec: rfftfreq for x, fftfreq (negative half from -n/2) for y, z.
@@ -96,6 +128,7 @@ __global__ void hessian_kernel(const cufftComplex* __restrict__ dk, cufftComplex
 #pragma unroll
         for (int b = a; b < 3; ++b) {
           float s = __fmul_rn(kv[a], kv[b]);
+          if (a != b && drop_odd2(g, a, b, i, j, k)) s = 0.0f;
           out[e + (size_t)m * nk] = make_float2(__fmul_rn(s, d.x), __fmul_rn(s, d.y));
           ++m;
         }
@@ -158,7 +191,8 @@ __global__ void grad_kernel(const cufftComplex* __restrict__ src, cufftComplex* 
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       // (i k) * (re + i im) = (-k im, k re)
-      float re = -__fmul_rn(kv[a], d.y), im = __fmul_rn(kv[a], d.x);
+      const float ka = drop_odd(g, a, i, j, k) ? 0.0f : kv[a];
+      float re = -__fmul_rn(ka, d.y), im = __fmul_rn(ka, d.x);
       if (inv_lap) {
         if (k2 > 0.0f) { re = __fdiv_rn(re, k2); im = __fdiv_rn(im, k2); }
         else { re = 0.0f; im = 0.0f; }
@@ -765,11 +799,14 @@ __global__ void __launch_bounds__(256, MINB) zgrad_kernel(const cufftComplex* __
 #pragma unroll
   for (int k2 = 0; k2 < 16; ++k2) xs[16 * r + k2][cl] = v[k2];
   float kxy[2];
+  bool real_plane, jnyq;   // column in the kx = 0 / n1/2 planes; ky index Nyquist
   {
     const int cc = ok ? col : 0;
     const int j = cc / g.n1h, i = cc - j * g.n1h;
     float kz;
     kvals(g, i, j, 0, kxy[0], kxy[1], kz);
+    real_plane = in_real_plane(g, i);
+    jnyq = j == g.nyq[1];
   }
   const float c0 = __fadd_rn(__fmul_rn(kxy[0], kxy[0]), __fmul_rn(kxy[1], kxy[1]));
 #pragma unroll 1
@@ -777,7 +814,9 @@ __global__ void __launch_bounds__(256, MINB) zgrad_kernel(const cufftComplex* __
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
       const float kz = kzt[r + 16 * k2];
-      const float kc = c == 0 ? kxy[0] : (c == 1 ? kxy[1] : kz);
+      float kc = c == 0 ? kxy[0] : (c == 1 ? kxy[1] : kz);
+      // the Hermitian part in the kx = 0 / n1/2 planes (see drop_odd)
+      if (real_plane && (c == 0 || (c == 1 && jnyq) || (c == 2 && r + 16 * k2 == g.nyq[2]))) kc = 0.0f;
       const float2 d = xs[16 * r + k2][cl];
       // (i k) (re + i im) = (-k im, k re), as grad_kernel
       float re = -__fmul_rn(kc, d.y), im = __fmul_rn(kc, d.x);

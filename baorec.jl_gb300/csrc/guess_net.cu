@@ -767,8 +767,7 @@ static_assert(sizeof(baorec_guess_train_config) == 4 * 20, "baorec_guess_train_c
 
 extern "C" int64_t baorec_guess_num_params(void) { return (int64_t)kP.total; }
 
-extern "C" int baorec_guess_init(baorec_ctx* ctx, uint32_t seed) {
-  if (!ctx) return BAOREC_ERR_ARG;
+static int guess_init_impl(baorec_ctx* ctx, uint32_t seed) {
   CKS(net_alloc(ctx));
   std::mt19937_64 rng(seed);
   std::vector<float> p(kP.total, 0.0f);
@@ -794,8 +793,7 @@ extern "C" int baorec_guess_init(baorec_ctx* ctx, uint32_t seed) {
   return BAOREC_OK;
 }
 
-extern "C" int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int64_t n) {
-  if (!ctx || !params) return BAOREC_ERR_ARG;
+static int guess_set_params_impl(baorec_ctx* ctx, const float* params, int64_t n) {
   if (n != (int64_t)kP.total)
     return set_error(ctx, BAOREC_ERR_ARG, "guess_set_params: %lld values, the network has %zu", (long long)n, kP.total);
   CKS(net_alloc(ctx));
@@ -806,8 +804,7 @@ extern "C" int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int
   return BAOREC_OK;
 }
 
-extern "C" int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n) {
-  if (!ctx || !params) return BAOREC_ERR_ARG;
+static int guess_get_params_impl(baorec_ctx* ctx, float* params, int64_t n) {
   CKS(need_params(ctx));
   if (n != (int64_t)kP.total)
     return set_error(ctx, BAOREC_ERR_ARG, "guess_get_params: room for %lld values, the network has %zu", (long long)n,
@@ -817,9 +814,8 @@ extern "C" int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n
   return BAOREC_OK;
 }
 
-extern "C" int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* target, float* out,
-                                 float* grads, double* loss, int loss_kind) {
-  if (!ctx || !features || !out || loss_kind < 0 || loss_kind > 1) return BAOREC_ERR_ARG;
+static int guess_eval_impl(baorec_ctx* ctx, const float* features, const float* target, float* out, float* grads,
+                           double* loss, int loss_kind) {
   CKS(need_params(ctx));
   CKS(mg_setup(ctx));
   GuessNet* g = ctx->net;
@@ -843,23 +839,14 @@ extern "C" int baorec_guess_eval(baorec_ctx* ctx, const float* features, const f
   return finish(ctx, 0);
 }
 
-extern "C" int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0) {
-  if (!ctx || !f || !phi0) return BAOREC_ERR_ARG;
-  CKS(guess_apply(ctx, f, phi0));
-  return finish(ctx, 0);
-}
-
-extern "C" int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index, float* f,
-                                   float* phi) {
-  if (!ctx || !tc || !f || !phi) return BAOREC_ERR_ARG;
+static int guess_sample_impl(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index, float* f,
+                             float* phi) {
   CKS(mg_setup(ctx));
   CKS(make_sample(ctx, tc, (uint64_t)index, f, phi));
   return finish(ctx, 0);
 }
 
-extern "C" int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history) {
-  if (!ctx || !tc || tc->steps < 0 || tc->batch < 1 || tc->loss < 0 || tc->loss > 1)
-    return set_error(ctx, BAOREC_ERR_ARG, "guess_train: bad config");
+static int guess_train_impl(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history) {
   CKS(need_params(ctx));
   CKS(net_train_alloc(ctx));
   CKS(mg_setup(ctx));
@@ -895,14 +882,193 @@ extern "C" int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_conf
   return finish(ctx, 0);
 }
 
-extern "C" int baorec_guess_set_conv_path(baorec_ctx* ctx, int32_t tensor_core) {
-  if (!ctx || tensor_core < 0 || tensor_core > 1) return BAOREC_ERR_ARG;
+static int guess_set_conv_path_impl(baorec_ctx* ctx, int32_t tensor_core) {
   CKS(net_alloc(ctx));
   ctx->net->use_tc = tensor_core != 0;
   return BAOREC_OK;
 }
 
-extern "C" int32_t baorec_guess_tc_layers(baorec_ctx* ctx) { return ctx && ctx->net ? ctx->net->tc_layers : -1; }
+
+// ---- the network on this mesh or on its first restriction -----------------
+//
+// guess_level 0: the network runs on the context's own mesh.  guess_level 1:
+// it runs on a child context at n/2 per axis over the same box (the first
+// restriction of the multigrid), which owns the network; every
+// baorec_guess_* call is routed to the context that owns it, and its error
+// message is copied back.
+
+namespace baorec {
+namespace {
+
+baorec_ctx* net_ctx(baorec_ctx* ctx) { return ctx->guess_level == 1 && ctx->guess_child ? ctx->guess_child : ctx; }
+
+int routed(baorec_ctx* ctx, baorec_ctx* c, int st) {
+  if (st != BAOREC_OK && c != ctx) {
+    snprintf(ctx->msg, sizeof(ctx->msg), "%s", c->msg);
+    ctx->launches += 0;
+  }
+  return st;
+}
+
+int sync_child_box(baorec_ctx* ctx) {
+  baorec_ctx* c = ctx->guess_child;
+  bool same = true;
+  for (int a = 0; a < 3; ++a)
+    same = same && c->cfg.box_size[a] == ctx->cfg.box_size[a] && c->cfg.box_min[a] == ctx->cfg.box_min[a];
+  if (same) return BAOREC_OK;
+  return routed(ctx, c, baorec_set_box(c, ctx->cfg.box_size, ctx->cfg.box_min));
+}
+
+__global__ void scale_kernel(float* __restrict__ a, float s, size_t n) {
+  for (size_t i = gtid(); i < n; i += gstride()) a[i] *= s;
+}
+
+// φ0 = S⁻¹ f + P (s_c net_c(features of R f)): the FFT start on this mesh plus
+// the network's correction computed on the child from the full-weighting
+// restriction R f (src/multigrid.jl:520-584) and brought back by the
+// trilinear prolongation P (src/multigrid.jl:398-453), added in place.
+int guess_apply_coarse(baorec_ctx* ctx, const float* f, float* phi0) {
+  baorec_ctx* c = ctx->guess_child;
+  if (!c->net || !c->net->has_params)
+    return set_error(ctx, BAOREC_ERR_ARG, "learned guess: no network parameters (init, set or train them first)");
+  CKS(sync_child_box(ctx));
+  CKS(mg_setup(ctx));
+  CKS(routed(ctx, c, mg_setup(c)));
+  for (cudaEvent_t* e : {&ctx->ev_guess[0], &ctx->ev_guess[1]})
+    if (!*e) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  const int nl[3] = {ctx->n1, ctx->n2, ctx->n3};
+  float* fc = c->mesh3;            // R f
+  float* phs = c->mesh3 + c->N;    // the child's FFT start of R f (a feature)
+  const int64_t l0 = c->launches;
+  CKS(spectral_correction(ctx, f, phi0));
+  CKS(mg_reduce(ctx, fc, f, nl));
+  CK(cudaEventRecord(ctx->ev_guess[0], ctx->stream));
+  CK(cudaStreamWaitEvent(c->stream, ctx->ev_guess[0], 0));
+  float s = 1.0f;
+  CKS(routed(ctx, c, net_features(c, fc, phs, c->lev[0].r, &s)));
+  CKS(routed(ctx, c, net_forward(c)));
+  scale_kernel<<<eblocks(c->N), 256, 0, c->stream>>>(c->net->out, s, c->N);
+  CK(cudaGetLastError());
+  c->launches++;
+  CK(cudaEventRecord(ctx->ev_guess[1], c->stream));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_guess[1], 0));
+  ctx->launches += c->launches - l0;
+  return mg_prolong(ctx, phi0, c->net->out, nl, 1);
+}
+
+// move the parameters of the network owned by `from` into `to` (allocating its network)
+int move_params(baorec_ctx* ctx, baorec_ctx* from, baorec_ctx* to) {
+  if (!from->net || !from->net->has_params) return BAOREC_OK;
+  CKS(routed(ctx, to, net_alloc(to)));
+  CK(cudaStreamSynchronize(from->stream));
+  CK(cudaMemcpyAsync(to->net->params, from->net->params, kP.total * 4, cudaMemcpyDeviceToDevice, to->stream));
+  CK(cudaStreamSynchronize(to->stream));
+  to->net->has_params = true;
+  to->net->frags_ok = false;
+  to->net->use_tc = from->net->use_tc;
+  return BAOREC_OK;
+}
+
+}  // namespace
+
+int guess_dispatch_apply(baorec_ctx* ctx, const float* f, float* phi0) {
+  return ctx->guess_level == 1 && ctx->guess_child ? guess_apply_coarse(ctx, f, phi0) : guess_apply(ctx, f, phi0);
+}
+
+}  // namespace baorec
+
+extern "C" int baorec_guess_set_level(baorec_ctx* ctx, int32_t level) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (level != 0 && level != 1) return set_error(ctx, BAOREC_ERR_ARG, "guess_set_level: level must be 0 or 1");
+  if (level == ctx->guess_level) return BAOREC_OK;
+  if (level == 1) {
+    const int n = ctx->n1;
+    if (!(ctx->n1 == ctx->n2 && ctx->n2 == ctx->n3) || n % 8 != 0)
+      return set_error(ctx, BAOREC_ERR_ARG, "guess_set_level: the restriction needs a cubic mesh with n divisible by 8");
+    if (!ctx->guess_child) {
+      baorec_config cc = ctx->cfg;
+      for (int a = 0; a < 3; ++a) cc.n[a] = n / 2;
+      cc.method = BAOREC_MULTIGRID;
+      cc.mg_mode = BAOREC_MG_CONVERGENT;
+      cc.mg_start = BAOREC_START_SPECTRAL;
+      baorec_ctx* c = nullptr;
+      const int st = baorec_create(&cc, &c);
+      if (st != BAOREC_OK) {
+        set_error(ctx, st, "guess_set_level: %s", baorec_last_error(c));
+        if (c) baorec_destroy(c);
+        return st;
+      }
+      ctx->guess_child = c;
+    }
+    CKS(move_params(ctx, ctx, ctx->guess_child));
+    guess_free(ctx);
+  } else {
+    CKS(move_params(ctx, ctx->guess_child, ctx));
+    baorec_destroy(ctx->guess_child);
+    ctx->guess_child = nullptr;
+  }
+  ctx->guess_level = level;
+  return BAOREC_OK;
+}
+
+extern "C" int32_t baorec_guess_level(const baorec_ctx* ctx) { return ctx ? ctx->guess_level : -1; }
+
+extern "C" int baorec_guess_init(baorec_ctx* ctx, uint32_t seed) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_init_impl(c, seed));
+}
+
+extern "C" int baorec_guess_set_params(baorec_ctx* ctx, const float* params, int64_t n) {
+  if (!ctx || !params) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_set_params_impl(c, params, n));
+}
+
+extern "C" int baorec_guess_get_params(baorec_ctx* ctx, float* params, int64_t n) {
+  if (!ctx || !params) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_get_params_impl(c, params, n));
+}
+
+extern "C" int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* target, float* out,
+                                 float* grads, double* loss, int loss_kind) {
+  if (!ctx || !features || !out || loss_kind < 0 || loss_kind > 1) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_eval_impl(c, features, target, out, grads, loss, loss_kind));
+}
+
+extern "C" int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0) {
+  if (!ctx || !f || !phi0) return BAOREC_ERR_ARG;
+  CKS(guess_dispatch_apply(ctx, f, phi0));
+  return finish(ctx, 0);
+}
+
+extern "C" int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index, float* f,
+                                   float* phi) {
+  if (!ctx || !tc || !f || !phi) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_sample_impl(c, tc, index, f, phi));
+}
+
+extern "C" int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, float* loss_history) {
+  if (!ctx || !tc || tc->steps < 0 || tc->batch < 1 || tc->loss < 0 || tc->loss > 1)
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_train: bad config");
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_train_impl(c, tc, loss_history));
+}
+
+extern "C" int baorec_guess_set_conv_path(baorec_ctx* ctx, int32_t tensor_core) {
+  if (!ctx || tensor_core < 0 || tensor_core > 1) return BAOREC_ERR_ARG;
+  baorec_ctx* c = net_ctx(ctx);
+  return routed(ctx, c, guess_set_conv_path_impl(c, tensor_core));
+}
+
+extern "C" int32_t baorec_guess_tc_layers(baorec_ctx* ctx) {
+  if (!ctx) return -1;
+  baorec_ctx* c = net_ctx(ctx);
+  return c->net ? c->net->tc_layers : -1;
+}
 
 extern "C" int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, const void* x,
                                   const float* w, const float* bias, const void* add, void* y, int32_t relu,

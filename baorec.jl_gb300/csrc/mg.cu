@@ -226,16 +226,27 @@ __global__ void resid_acc_kernel(const float* __restrict__ hi, const float* __re
     };
     float h0, l0;
     V(i, j, k, h0, l0);
-    auto D = [&](int a, int bb, int cc) {
+    // (h_u - h_0, l_u - l_0) of every neighbour, combined by dd_sum2 / dd_cross / dd_diff2
+    auto Dh = [&](int a, int bb, int cc) {
       float h, l; V(a, bb, cc, h, l);
-      return __fadd_rn(__fsub_rn(h, h0), __fsub_rn(l, l0));
+      return __fsub_rn(h, h0);
     };
-    Nb b = gather(D, G.n, i, j, k);
+    auto Dl = [&](int a, int bb, int cc) {
+      float h, l; V(a, bb, cc, h, l);
+      return __fsub_rn(l, l0);
+    };
+    const Nb bh = gather(Dh, G.n, i, j, k), bl = gather(Dl, G.n, i, j, k);
+    auto P = [](float h, float l) { return make_float2(h, l); };
     // −A v expressed with differences (the constant terms cancel)
-    float br = c.gpx * (b.xp + b.xm) + c.gpy * (b.yp + b.ym) + c.gpz * (b.zp + b.zm) +
-               c.g / 2.0f * (c.pxy * ((b.pp0 + b.mm0) - (b.mp0 + b.pm0)) + c.pxz * ((b.p0p + b.m0m) - (b.m0p + b.p0m)) +
-                             c.pyz * ((b._pp + b._mm) - (b._mp + b._pm)));
-    if (G.local) br += c.dx * (b.xp - b.xm) + c.dy * (b.yp - b.ym) + c.dz * (b.zp - b.zm);
+    float br = c.gpx * dd_sum2(P(bh.xp, bl.xp), P(bh.xm, bl.xm)) + c.gpy * dd_sum2(P(bh.yp, bl.yp), P(bh.ym, bl.ym)) +
+               c.gpz * dd_sum2(P(bh.zp, bl.zp), P(bh.zm, bl.zm)) +
+               c.g / 2.0f *
+                   (c.pxy * dd_cross(P(bh.pp0, bl.pp0), P(bh.mm0, bl.mm0), P(bh.mp0, bl.mp0), P(bh.pm0, bl.pm0)) +
+                    c.pxz * dd_cross(P(bh.p0p, bl.p0p), P(bh.m0m, bl.m0m), P(bh.m0p, bl.m0p), P(bh.p0m, bl.p0m)) +
+                    c.pyz * dd_cross(P(bh._pp, bl._pp), P(bh._mm, bl._mm), P(bh._mp, bl._mp), P(bh._pm, bl._pm)));
+    if (G.local)
+      br += c.dx * dd_diff2(P(bh.xp, bl.xp), P(bh.xm, bl.xm)) + c.dy * dd_diff2(P(bh.yp, bl.yp), P(bh.ym, bl.ym)) +
+            c.dz * dd_diff2(P(bh.zp, bl.zp), P(bh.zm, bl.zm));
     float rv = (f[e] - alpha) + br;
     ohi[e] = h0;
     olo[e] = l0;
@@ -777,7 +788,7 @@ int start_residual(baorec_ctx* ctx, const float* f, int start, double* rel) {
   float* r = L0.r + N;
   if (start == BAOREC_START_ZERO) CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
   else if (start == BAOREC_START_SPECTRAL) CKS(spectral_correction(ctx, f, v));
-  else CKS(guess_apply(ctx, f, v));
+  else CKS(guess_dispatch_apply(ctx, f, v));
   CKS(operator_residual(ctx, v, f, r));
   double sf = 0.0, sf2 = 0.0, sr = 0.0, sr2 = 0.0;
   CKS(sum_mesh(ctx, f, N, &sf));
@@ -798,7 +809,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   float* loA = ctx->phi_lo;
   float* loB = ctx->phi_lo2;
   if (phi0 && phi0 != phi) CK(cudaMemcpyAsync(hiA, phi0, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-  if (!phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED) CKS(guess_apply(ctx, f, hiA));
+  if (!phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED) CKS(guess_dispatch_apply(ctx, f, hiA));
   else if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
   // The first residual of a zero solution needs no stencil: r = f - α with
   // α = mean f, so Σr = 0 and |r| = |f - α| (relative residual 1), and the

@@ -126,16 +126,18 @@ __global__ void __launch_bounds__(NTS) resid_acc_stream_kernel(const float* __re
       const float gpz = __fadd_rn(G.icell2[2], __fmul_rn(g, pz2));
       const int q = (ly + 1) * WXS + lane + 4;
       const float h0 = H[s0][q], l0 = Lo[s0][q];
-      auto D = [&](int s, int u) { return __fadd_rn(__fsub_rn(H[s][u], h0), __fsub_rn(Lo[s][u], l0)); };
-      const float dxp = D(s0, q + 1), dxm = D(s0, q - 1), dyp = D(s0, q + WXS), dym = D(s0, q - WXS);
-      const float dzp = D(sp, q), dzm = D(sm, q);
-      float br = gpx * (dxp + dxm) + gpy * (dyp + dym) + gpz * (dzp + dzm) +
+      auto D = [&](int s, int u) { return make_float2(__fsub_rn(H[s][u], h0), __fsub_rn(Lo[s][u], l0)); };
+      const float2 xp = D(s0, q + 1), xm = D(s0, q - 1), yp = D(s0, q + WXS), ym = D(s0, q - WXS);
+      const float2 zp = D(sp, q), zm = D(sm, q);
+      float br = gpx * dd_sum2(xp, xm) + gpy * dd_sum2(yp, ym) + gpz * dd_sum2(zp, zm) +
                  g / 2.0f *
-                     (__fmul_rn(px, py) * ((D(s0, q + 1 + WXS) + D(s0, q - 1 - WXS)) -
-                                           (D(s0, q - 1 + WXS) + D(s0, q + 1 - WXS))) +
-                      __fmul_rn(px, pz) * ((D(sp, q + 1) + D(sm, q - 1)) - (D(sp, q - 1) + D(sm, q + 1))) +
-                      __fmul_rn(py, pz) * ((D(sp, q + WXS) + D(sm, q - WXS)) - (D(sp, q - WXS) + D(sm, q + WXS))));
-      if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
+                     (__fmul_rn(px, py) * dd_cross(D(s0, q + 1 + WXS), D(s0, q - 1 - WXS), D(s0, q - 1 + WXS),
+                                                   D(s0, q + 1 - WXS)) +
+                      __fmul_rn(px, pz) * dd_cross(D(sp, q + 1), D(sm, q - 1), D(sp, q - 1), D(sm, q + 1)) +
+                      __fmul_rn(py, pz) * dd_cross(D(sp, q + WXS), D(sm, q - WXS), D(sp, q - WXS), D(sm, q + WXS)));
+      if (LOCAL)
+        br += __fmul_rn(g, px) * dd_diff2(xp, xm) + __fmul_rn(g, py) * dd_diff2(yp, ym) +
+              __fmul_rn(g, pz) * dd_diff2(zp, zm);
       const size_t o = (size_t)x + (size_t)G.n[0] * ((size_t)y + (size_t)G.n[1] * (size_t)z);
       const float rv = (__ldg(f + o) - alpha) + br;
       ohi[o] = h0;

@@ -612,16 +612,18 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
     const f2 c0 = sw[q];
     auto D = [&](int u) {
       float a, b;
-      U2(sub2(sw[u], c0), a, b);   // (h_u - h_0, l_u - l_0), each rounded once
-      return __fadd_rn(a, b);
+      U2(sub2(sw[u], c0), a, b);   // (h_u - h_0, l_u - l_0), each exact for neighbouring values
+      return make_float2(a, b);
     };
-    const float dxp = D(q + 1), dxm = D(q - 1), dyp = D(q + SX), dym = D(q - SX), dzp = D(q + SXY), dzm = D(q - SXY);
-    float br = gpx * (dxp + dxm) + gpy * (dyp + dym) + gpz * (dzp + dzm) +
+    const float2 xp = D(q + 1), xm = D(q - 1), yp = D(q + SX), ym = D(q - SX), zp = D(q + SXY), zm = D(q - SXY);
+    float br = gpx * dd_sum2(xp, xm) + gpy * dd_sum2(yp, ym) + gpz * dd_sum2(zp, zm) +
                g / 2.0f *
-                   (__fmul_rn(px, py) * ((D(q + 1 + SX) + D(q - 1 - SX)) - (D(q - 1 + SX) + D(q + 1 - SX))) +
-                    __fmul_rn(px, pz) * ((D(q + 1 + SXY) + D(q - 1 - SXY)) - (D(q - 1 + SXY) + D(q + 1 - SXY))) +
-                    __fmul_rn(py, pz) * ((D(q + SX + SXY) + D(q - SX - SXY)) - (D(q - SX + SXY) + D(q + SX - SXY))));
-    if (LOCAL) br += __fmul_rn(g, px) * (dxp - dxm) + __fmul_rn(g, py) * (dyp - dym) + __fmul_rn(g, pz) * (dzp - dzm);
+                   (__fmul_rn(px, py) * dd_cross(D(q + 1 + SX), D(q - 1 - SX), D(q - 1 + SX), D(q + 1 - SX)) +
+                    __fmul_rn(px, pz) * dd_cross(D(q + 1 + SXY), D(q - 1 - SXY), D(q - 1 + SXY), D(q + 1 - SXY)) +
+                    __fmul_rn(py, pz) * dd_cross(D(q + SX + SXY), D(q - SX - SXY), D(q - SX + SXY), D(q + SX - SXY)));
+    if (LOCAL)
+      br += __fmul_rn(g, px) * dd_diff2(xp, xm) + __fmul_rn(g, py) * dd_diff2(yp, ym) +
+            __fmul_rn(g, pz) * dd_diff2(zp, zm);
     const int o = ro[ly + SY * lz] + x0 + lane;
     const float rv = (fv - alpha) + br;
     float h0, l0;

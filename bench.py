@@ -203,7 +203,9 @@ def power_timing(args, baorec, torch, np, X, R, bs, bm):
 def workload(args, seed):
     from baorec import mocks
     import numpy as np
-    m = mocks.lightcone_mock(n_data=args.n_data, rand_factor=args.rand_factor, n_grid=args.mesh, seed=seed)
+    # the lognormal field is sampled on at most a 256^3 grid (above that, R = 15 Mpc/h smoothing leaves
+    # less than 1e-3 of the power at its Nyquist wave number)
+    m = mocks.lightcone_mock(n_data=args.n_data, rand_factor=args.rand_factor, n_grid=min(args.mesh, 256), seed=seed)
     # padded mesh: box from the randoms with a 25 Mpc/h pad (cell 5.96 Mpc/h at 256^3)
     pad = 25.0 * 256 / args.mesh
     f32 = np.float32
@@ -309,6 +311,110 @@ def traffic_per_launch(name, N):
         return None
 
 
+def run_box(args, torch, np):
+    """The periodic-box workload: 2e5 particles Poisson-sampled from the
+    lognormal field, 128^3 mesh, L = 1000 Mpc/h, CIC, R = 15, b = 2, f = 0.8,
+    LOS +z, 3 iterative-FFT steps, shifted positions (:sum); device arrays,
+    CUDA events on the context stream.  Returns the timing and the context
+    (its result is the last reconstruction)."""
+    import baorec
+    from baorec import _lib, mocks
+    n, L = 128, 1000.0
+    m = mocks.box_mock(n_part=200_000, L=L, n_grid=n, seed=1234)
+    rec = baorec.IterativeRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=[L] * 3, box_min=[0.0] * 3,
+                                los=[0.0, 0.0, 1.0], n_iter=3)
+    ctx = baorec.setup_fft_(rec, (n,) * 3)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
+    out = [torch.empty(len(m.x), device="cuda") for _ in range(3)]
+    ptrs = [t.data_ptr() for t in X]
+    optr = [t.data_ptr() for t in out]
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.call("baorec_reconstructed_overdensity", *ptrs, len(m.x), None, None, None, None, 0, _lib.ASYNC)
+        ctx.call("baorec_reconstructed_positions", *ptrs[:3], len(m.x), _lib.FIELD["sum"], *optr, _lib.ASYNC)
+
+    for _ in range(args.warmup):
+        step()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    return {"workload": "periodic box 128^3, L=1000, 2e5 particles, CIC, R=15, b=2, f=0.8, LOS +z, 3 iterations, "
+                        ":sum shifted positions", "value": 1000.0 / ms, "unit": "recons/s", "ms_per_step": ms}, \
+        (m, rec, ctx)
+
+
+def oracle_checks(args, torch, np, ctxs, m, bs, bm, X, R, box):
+    """Relative L2 error of the displacement field against the FP64 oracle
+    (oracle/fp64_oracle.py, oracle/baorec_oracle.py) for both workloads,
+    computed after the timed region on the host cores.
+
+    Lightcone: the right-hand side the GPU painted and normalised is solved
+    by every start's GPU solve and, in FP64, by the oracle; "solve" is the
+    error of the GPU gradient against that FP64 gradient (the arithmetic of
+    the solve and the gradient).  "pipeline" compares the same GPU gradient
+    with the FP64 oracle run from the particles (paint, smoothing,
+    normalisation and solve all in FP64); cells where the randoms' threshold
+    test of src/recon.jl:86-88 comes out differently in FP32 and FP64 are
+    counted in "threshold_flips".  Box: the GPU displacement meshes against
+    the FP64 oracle run of the same catalog."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import baorec
+    import baorec_oracle as O
+    import fp64_oracle as P
+    n = (args.mesh,) * 3
+    beta = np.float32(np.float32(0.8) / np.float32(2.0))
+    t0 = time.perf_counter()
+    c0 = next(iter(ctxs.values()))
+    fd = baorec.zeros_mesh(n)
+    c0.call("baorec_setup_overdensity_randoms", fd.data_ptr(), *[t.data_ptr() for t in X], X[0].numel(),
+            *[t.data_ptr() for t in R], R[0].numel(), 0)
+    torch.cuda.synchronize()
+    f_np = fd.cpu().numpy()
+    grads = {}
+    for start, c in ctxs.items():
+        phi = baorec.zeros_mesh(n)
+        st = c.status("baorec_mg_solve", fd.data_ptr(), phi.data_ptr(), None, None)
+        g = [baorec.zeros_mesh(n) for _ in range(3)]
+        c.call("baorec_set_result", phi.data_ptr(), 0)
+        c.call("baorec_displacement_meshes", *[t.data_ptr() for t in g])
+        torch.cuda.synchronize()
+        grads[start] = ([t.cpu().numpy() for t in g], st, c.solve_stats()["rel_residual"])
+    phi64, _, hist = P.solve(f_np, bs, bm, beta, None, rtol=1e-11)
+    g64 = P.gradient_meshes(phi64, np.asarray(bs, np.float64))
+    solve = {s: {"l2": P.rel_l2_vector(g, g64), "status": st, "rel_residual": rr} for s, (g, st, rr) in grads.items()}
+    f64 = O.setup_overdensity_randoms(np.zeros(n, np.float64), 2.0, 15.0, np.asarray(bs, np.float64),
+                                      np.asarray(bm, np.float64), m.x, m.y, m.z, m.w, m.rx, m.ry, m.rz, m.rw)
+    flips = int(((f64 == 0) != (f_np == 0)).sum())
+    phip, _, _ = P.solve(f64, bs, bm, beta, None, rtol=1e-11)
+    gp = P.gradient_meshes(phip, np.asarray(bs, np.float64))
+    pipeline = {s: P.rel_l2_vector(g, gp) for s, (g, _, _) in grads.items()}
+    lc = {"solve": solve, "pipeline": pipeline, "threshold_flips": flips, "fp64_solve_rel_residual": hist[-1],
+          "note": "GPU gradient of the potential vs the FP64 oracle; solve = same right-hand side, pipeline = "
+                  "FP64 from the particles"}
+    # box: displacement meshes of the last timed reconstruction vs the FP64 oracle run
+    bm_, brec, bctx = box
+    L = float(brec.box_size[0])
+    nb = (bctx.cfg.n[0],) * 3
+    # the timed steps painted the same catalog (positions inside the box, nothing wraps)
+    psi = [baorec.zeros_mesh(nb) for _ in range(3)]
+    bctx.call("baorec_displacement_meshes", *[t.data_ptr() for t in psi])
+    torch.cuda.synchronize()
+    d64, _, _, _ = O.run_iterative(nb, 2.0, 0.8, 15.0, bm_.x, bm_.y, bm_.z, bm_.w, box_size=[L] * 3,
+                                   box_min=[0.0] * 3, los=[0.0, 0.0, 1.0], n_iter=3, dtype=np.float64)
+    psi64 = O.displacement_meshes_iterative(d64, np.array([L] * 3))
+    bx = {"l2": P.rel_l2_vector([t.cpu().numpy() for t in psi], psi64),
+          "note": "GPU displacement meshes of the box reconstruction vs the FP64 oracle run"}
+    return {"lightcone_%d" % args.mesh: lc, "box_128": bx, "seconds": time.perf_counter() - t0}
+
+
 def cpu_baseline(args, m, bs, bm, reps=1):
     """The reference's CPU algorithm on this host: one full reconstruction per sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -390,9 +496,10 @@ def run_gb300(args):
 
     def make(start, gradient="fft"):
         gp = baorec.guess.load_params(weights) if start == "learned" else None
+        # the learned start's network runs on the 128^3 restriction of the 256^3 mesh, where it was trained
         rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=None,
                                     mg_mode="convergent", rtol=1e-6, nu1=2, nu2=2, max_cycles=50, start=start,
-                                    guess_params=gp, gradient=gradient)
+                                    guess_params=gp, gradient=gradient, guess_level=1 if args.mesh == 256 else 0)
         return baorec.setup_fft_(rec, n)
 
     ctx = make(args.start)
@@ -559,14 +666,24 @@ def run_gb300(args):
         aux["power multipoles (survey, l = 0, 2, 4)"] = power_timing(args, baorec, torch, np, X, R, bs, bm)
 
     batch = None if args.no_batch else run_batch(args, torch, np)
+    box, box_state = run_box(args, torch, np)
 
-    cpu = None
+    # the metric's own comparison: learned-start recons/s over plain-multigrid recons/s
+    rates = {args.start: value}
+    rates.update({k: v["value"] for k, v in arms.items()})
+    learned_vs_plain = rates["learned"] / rates["zero"] if "learned" in rates and "zero" in rates else None
+    spectral_vs_plain = rates["spectral"] / rates["zero"] if "spectral" in rates and "zero" in rates else None
+
+    cpu, checks = None, None
     if rank == 0 and ws == 1 and not args.no_cpu:
         port, tc = cpu_baseline(args, m, bs, bm)
         cpu = {"value": 1.0 / tc, "unit": UNIT, "cores": port.threads, "kind": "port",
                "sample": "one full reconstruction of this workload by the reference's CPU algorithm "
                          "(serial CIC paint, FMG damped Jacobi w=0.4 nu=5, 6 cycles/level, C/OpenMP + "
                          "scipy.fft); the reference schedule has no residual test"}
+        solvers = {args.start: ctx}
+        solvers.update({k: v for k, v in others.items() if "+" not in k})
+        checks = oracle_checks(args, torch, np, solvers, m, bs, bm, X, R, box_state)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -582,6 +699,13 @@ def run_gb300(args):
                        "rel_residual": stats["rel_residual"], "cycles_per_step": cycles,
                        "spectral_steps_per_step": [h[0] for h in hist]},
             "starts": arms,
+            "learned_vs_plain": learned_vs_plain,
+            "spectral_vs_plain": spectral_vs_plain,
+            "l2_vs_fp64": None if checks is None else {
+                "lightcone_%d" % args.mesh: checks["lightcone_%d" % args.mesh]["solve"][args.start]["l2"],
+                "box_128": checks["box_128"]["l2"]},
+            "accuracy": checks,
+            "box": box,
             "gpu_launches": launches,
             "clocks": clk,
             "roofline": roofline,

@@ -408,6 +408,19 @@ int baorec_guess_eval(baorec_ctx* ctx, const float* features, const float* targe
                       float* grads, double* loss, int loss_kind);
 /* phi0 = FFT start + learned correction for the right-hand side f (device meshes). */
 int baorec_guess_apply(baorec_ctx* ctx, const float* f, float* phi0);
+/* Where the network runs: level 0 (default) on this context's mesh; level 1
+ * on the first restriction of the mesh (n/2 per axis, same box), the way a
+ * multigrid coarse level sees it: the right-hand side is restricted with the
+ * full-weighting operator of reduce! (src/multigrid.jl:520-584), the
+ * network's correction is computed there against the FFT start of that
+ * coarse problem and brought back with the trilinear prolongation of
+ * prolong! (src/multigrid.jl:398-453) onto this mesh's FFT start.  Level 1
+ * needs a cubic mesh with n % 8 == 0; it creates a child context at n/2 that
+ * owns the network from then on (every baorec_guess_* call on this context
+ * acts on the child's network; parameters set before the switch move with
+ * it).  Returns BAOREC_ERR_ARG for other levels. */
+int baorec_guess_set_level(baorec_ctx* ctx, int32_t level);
+int32_t baorec_guess_level(const baorec_ctx* ctx);
 /* One training pair (device meshes f and its solution phi); moves the box. */
 int baorec_guess_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, int64_t index,
                         float* f, float* phi);

@@ -71,7 +71,8 @@ def test_trained_network_improves_the_fft_start_and_keeps_the_solution():
     import torch
     import baorec
     from baorec import guess, train_guess
-    ctx, cfg = train_guess.training_context(128)
+    # the committed parameters were trained on the 128^3 restriction of the 256^3 lightcone box
+    ctx, cfg = train_guess.training_context(128, 128)
     guess.init(ctx, 3)
     untrained = train_guess.held_out(ctx, cfg, count=4)
     guess.set_params(ctx, guess.load_params(f"{guess.WEIGHTS_DIR}/guess_lightcone.npy"))
@@ -100,3 +101,48 @@ def test_trained_network_improves_the_fft_start_and_keeps_the_solution():
     print("spectral", grads["spectral"][0], "learned", grads["learned"][0])
     g0, g1 = grads["spectral"][1], grads["learned"][1]
     assert max(rel_l2(g1[a], g0[a]) for a in range(3)) < 2e-5
+
+
+def test_learned_start_on_the_restriction_of_the_lightcone_mesh():
+    """guess_level 1 on the 256^3 lightcone mesh: the network runs on the
+    128^3 restriction (full weighting in, trilinear prolongation out, the
+    operators of src/multigrid.jl:398-453, 520-584), which is where the
+    committed parameters were trained.  The parameters move to the child
+    context and back, the learned start's residual is below the FFT start's,
+    and the solve from it converges to the FFT start's solution."""
+    import torch
+    import baorec
+    from baorec import _lib, guess, mocks
+    W = guess.load_params(f"{guess.WEIGHTS_DIR}/guess_lightcone.npy")
+    n = 256
+    m = mocks.lightcone_mock(n_data=200_000, rand_factor=10, n_grid=n, seed=77)
+    bs, bm = O.setup_box(m.rx, m.ry, m.rz, 25.0)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    X = [dev(a) for a in (m.x, m.y, m.z, m.w)]
+    Rr = [dev(a) for a in (m.rx, m.ry, m.rz, m.rw)]
+    recs = {}
+    for start in ("spectral", "learned"):
+        recs[start] = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm,
+                                            mg_mode="convergent", rtol=1e-6, start=start,
+                                            guess_params=W if start == "learned" else None, guess_level=1)
+    ctx = baorec.setup_fft_(recs["learned"], (n,) * 3)
+    assert ctx.lib.baorec_guess_level(ctx.h) == 1
+    np.testing.assert_array_equal(guess.get_params(ctx), W)
+    f = baorec.zeros_mesh((n,) * 3)
+    baorec.setup_overdensity_(f, recs["spectral"], *X, *Rr)
+    r_fft = guess.start_residual(ctx, f.data_ptr(), "spectral")
+    r_l = guess.start_residual(ctx, f.data_ptr(), "learned")
+    print("256^3 start residual: FFT %.4f, learned on the restriction %.4f (ratio %.3f)" % (r_fft, r_l, r_l / r_fft))
+    assert r_l < r_fft
+    grads = {}
+    for start, rec in recs.items():
+        phi = baorec.zeros_mesh((n,) * 3)
+        st = baorec.solve_(phi, f, rec)
+        assert st["rel_residual"] <= 1e-6, st
+        grads[start] = O.gradient_meshes(phi.cpu().numpy().astype(np.float64), bs.astype(np.float64))
+    assert max(rel_l2(grads["learned"][a], grads["spectral"][a]) for a in range(3)) < 2e-5
+    # back to level 0: the parameters move with the network
+    ctx.call("baorec_guess_set_level", 0)
+    assert ctx.lib.baorec_guess_level(ctx.h) == 0
+    np.testing.assert_array_equal(guess.get_params(ctx), W)
+    assert ctx.status("baorec_guess_set_level", 2) == _lib.ERR_ARG
