@@ -165,6 +165,7 @@ _SIGS = {
     "baorec_guess_set_conv_path": (C.c_int, [P, C.c_int32]),
     "baorec_guess_tc_layers": (C.c_int32, [P]),
     "baorec_guess_conv3": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, C.c_int32, C.c_int32]),
+    "baorec_guess_conv3_held_back": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int64]),
     "baorec_guess_profile_conv": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                             C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "baorec_read_cic": (C.c_int, [P, P, P, P, P, I64, P, U32]),

@@ -76,6 +76,38 @@ def _sample_cells(prob, n_part, n, L, origin, rng):
     return x[perm], y[perm], z[perm]
 
 
+def field_cdf(delta):
+    """Cumulative cell distribution ∝ 1 + δ of a field, for :func:`sample_field`."""
+    w = np.clip(1.0 + delta, 0.0, None).ravel()
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    return cdf
+
+
+def sample_field(delta, n_part, L, rng, shift=(0, 0, 0), cdf=None):
+    """``n_part`` FP32 positions in the periodic box [0, L)^3 drawn from the
+    cells of ``delta`` (indexed [ix, iy, iz]) with probability ∝ 1 + δ and
+    uniform inside the cell, the field moved periodically by ``shift`` cells.
+    The cells come from the inverse of the cumulative distribution, which is
+    the same multinomial draw as :func:`_sample_cells` for many catalogs of
+    one field without redoing its O(cells) work per catalog."""
+    n = delta.shape[0]
+    if cdf is None:
+        cdf = field_cdf(delta)
+    cells = np.searchsorted(cdf, rng.random(n_part), side="right")
+    cells = np.minimum(cells, cdf.size - 1)
+    ix, iy, iz = np.unravel_index(cells, delta.shape)
+    cell = L / n
+    u = rng.random((3, n_part))
+    f32 = np.float32
+    out = []
+    for idx, sh, uu in ((ix, shift[0], u[0]), (iy, shift[1], u[1]), (iz, shift[2], u[2])):
+        a = np.mod((idx + sh + uu) * cell, L).astype(f32)
+        a[a >= f32(L)] = f32(0)
+        out.append(a)
+    return out
+
+
 @dataclass
 class BoxMock:
     x: np.ndarray

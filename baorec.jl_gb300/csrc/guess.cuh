@@ -39,6 +39,10 @@ struct ConvArgs {
   const __nv_bfloat16* wimg = nullptr;   // weight image (weight_image), null = mma.sync path
   unsigned* err = nullptr;               // device error word (kErrTimeout)
   int tc_loader = 0;                     // slab loader: 0 TMA boxes, 1 cp.async warps
+  // limit of every pipeline wait of the tcgen05 kernel (ns); the drains at
+  // the end of a block always allow 2 s
+  unsigned long long wait_ns = 2000000000ull;
+  int hold_back = 0;                     // test hook: the TMA slab loader issues no slab (waits expire)
 };
 
 struct WgradArgs {

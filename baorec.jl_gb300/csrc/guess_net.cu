@@ -940,10 +940,12 @@ int guess_apply_coarse(baorec_ctx* ctx, const float* f, float* phi0) {
   float* fc = c->mesh3;            // R f
   float* phs = c->mesh3 + c->N;    // the child's FFT start of R f (a feature)
   const int64_t l0 = c->launches;
-  CKS(spectral_correction(ctx, f, phi0));
+  // the child starts as soon as R f exists; this mesh's FFT start, which
+  // does not depend on the network, runs on this context's stream meanwhile
   CKS(mg_reduce(ctx, fc, f, nl));
   CK(cudaEventRecord(ctx->ev_guess[0], ctx->stream));
   CK(cudaStreamWaitEvent(c->stream, ctx->ev_guess[0], 0));
+  CKS(spectral_correction(ctx, f, phi0));
   float s = 1.0f;
   CKS(routed(ctx, c, net_features(c, fc, phs, c->lev[0].r, &s)));
   CKS(routed(ctx, c, net_forward(c)));
@@ -1112,6 +1114,56 @@ extern "C" int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, in
   if (e != cudaSuccess) rc = set_error(ctx, BAOREC_ERR_CUDA, "guess_conv3: %s", cudaGetErrorString(e));
   else rc = finish(ctx, 0);
   cudaStreamSynchronize(ctx->stream);
+  cudaFree(frag);
+  cudaFree(img);
+  return rc;
+}
+
+extern "C" int baorec_guess_conv3_held_back(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n,
+                                            int64_t wait_ns) {
+  if (!ctx) return BAOREC_ERR_ARG;
+  if (wait_ns < 1 || !guess::tc_supported(C3, cin, cout, n))
+    return set_error(ctx, BAOREC_ERR_ARG, "guess_conv3_held_back: no tcgen05 kernel for %d -> %d at n = %d", cin, cout,
+                     n);
+  const size_t nv = (size_t)n * n * n;
+  bf16 *x = nullptr, *y = nullptr, *img = nullptr;
+  float* w = nullptr;
+  uint2* frag = nullptr;
+  cudaError_t e = cudaMalloc(&x, nv * cin * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&y, nv * cout * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&w, (size_t)27 * cin * cout * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&frag, guess::frag_count(C3, cin, cout) * sizeof(uint2));
+  if (e == cudaSuccess) e = cudaMalloc(&img, guess::image_count(cin, cout) * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMemsetAsync(x, 0, nv * cin * sizeof(bf16), ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w, 0, (size_t)27 * cin * cout * sizeof(float), ctx->stream);
+  if (e == cudaSuccess) e = guess::weight_frags(ctx->stream, C3, cin, cout, w, frag, false);
+  if (e == cudaSuccess) e = guess::weight_image(ctx->stream, cin, cout, w, img, false);
+  if (e == cudaSuccess) {
+    guess::ConvArgs a;
+    a.in = x;
+    a.in_cs = cin;
+    a.out = y;
+    a.out_cs = cout;
+    a.add = nullptr;
+    a.add_cs = 0;
+    a.w = frag;
+    a.bias = nullptr;
+    a.relu = 0;
+    a.n_in = a.n_out = n;
+    a.wimg = img;
+    a.err = ctx->derr;
+    a.tc_loader = 0;            // TMA boxes
+    a.wait_ns = (unsigned long long)wait_ns;
+    a.hold_back = 1;            // no slab is ever loaded: the MMA issuer's first wait expires
+    e = guess::conv_forward(ctx->stream, C3, cin, cout, a);
+    ctx->launches++;
+  }
+  int rc = e != cudaSuccess ? set_error(ctx, BAOREC_ERR_CUDA, "guess_conv3_held_back: %s", cudaGetErrorString(e))
+                            : finish(ctx, 0);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(w);
   cudaFree(frag);
   cudaFree(img);
   return rc;

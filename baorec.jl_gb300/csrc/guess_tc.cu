@@ -53,7 +53,9 @@
 // accumulator behind them.  mbarriers hand slabs, weights and accumulators
 // between the roles; every wait is bounded in time and on expiry sets
 // kErrTimeout and stops its role, and the block drains its copies and MMAs
-// before freeing TMEM.
+// before freeing TMEM (drain waits are not cut short by another role giving
+// up; they are bounded by kWaitNs).  The pipeline waits' limit is a launch
+// argument; a test hook holds the slab loader back so that they expire.
 #include <algorithm>
 
 #include <cuda.h>
@@ -132,6 +134,8 @@ struct TcArgs {
   int n;              // grid edge (input = output)
   int zc;             // output rows per column
   unsigned* err;
+  unsigned long long wait_ns;   // limit of every pipeline wait
+  int hold_back;      // test hook: the TMA slab loader issues no slab
 };
 
 // ---- PTX wrappers -----------------------------------------------------------
@@ -178,14 +182,27 @@ __device__ __forceinline__ bool mbar_try_suspend(uint32_t bar, uint32_t parity) 
   return ok != 0;
 }
 
-// Wait for the phase of the given parity; false after kWaitNs or when another
-// role has given up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+// Wait for the phase of the given parity; false after limit_ns or when
+// another role has given up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = gtimer();
   for (;;) {
     if (mbar_try_suspend(bar, parity)) return true;
-    if (*abort_flag || gtimer() - t0 > kWaitNs) return false;
+    if (*abort_flag || gtimer() - t0 > limit_ns) return false;
+  }
+}
+
+// Wait for copies or MMAs this block has issued before it frees their
+// shared memory or TMEM: not cut short when another role gives up, bounded
+// by kWaitNs whatever the pipeline's own limit.
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (;;) {
+    if (mbar_try_suspend(bar, parity)) return true;
+    if (gtimer() - t0 > kWaitNs) return false;
   }
 }
 
@@ -422,12 +439,12 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
         bool ok = true;
         long long j = 0;   // slab loads issued
-        for (long long u = blockIdx.x; ok && u < nunits; u += gridDim.x) {
+        for (long long u = blockIdx.x; ok && !a.hold_back && u < nunits; u += gridDim.x) {
           const Unit t = unit_of(u, n, zc, YR);
           for (int p = 0; p < zc + 2; ++p, ++j) {
             const int slot = (int)(j % S);
             const long long use = j / S;
-            if (use > 0 && !mbar_wait(smem_u32(&bar_empty[slot]), (uint32_t)((use - 1) & 1), &abort_flag)) {
+            if (use > 0 && !mbar_wait(smem_u32(&bar_empty[slot]), (uint32_t)((use - 1) & 1), &abort_flag, a.wait_ns)) {
               ok = false;
               break;
             }
@@ -444,7 +461,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         for (int s = 0; s < S; ++s) {
           if (j <= s) break;
           const long long last = j - 1 - ((j - 1 - s) % S);
-          mbar_wait(smem_u32(&bar_full[s]), (uint32_t)((last / S) & 1), &abort_flag);
+          mbar_drain(smem_u32(&bar_full[s]), (uint32_t)((last / S) & 1));
         }
       }
     } else {
@@ -465,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           }
           const int slot = (int)(j % S);
           const long long use = j / S;
-          if (use > 0 && !mbar_wait(smem_u32(&bar_empty[slot]), (uint32_t)((use - 1) & 1), &abort_flag)) {
+          if (use > 0 && !mbar_wait(smem_u32(&bar_empty[slot]), (uint32_t)((use - 1) & 1), &abort_flag, a.wait_ns)) {
             ok = false;
             break;
           }
@@ -478,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       fence_proxy_async();
       for (; signalled < j; ++signalled) mbar_arrive(smem_u32(&bar_full[(int)(signalled % S)]));
     }
-    if (pt == 0) mbar_wait(smem_u32(&bar_w), 0, &abort_flag);
+    if (pt == 0) mbar_drain(smem_u32(&bar_w), 0);   // the weight copy has landed
   } else if (warp == kMmaWarp) {
     // ---- MMA issuer: slab p of a column feeds output rows p, p-1, p-2
     //      (dz = 0, 1, 2) in one MMA per tap (dx, dy) and k step ----
@@ -486,20 +503,21 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       constexpr uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTM >> 4) << 24);
       constexpr uint32_t kBlk = COUT * 16;          // bytes of one dz block of B
       constexpr uint32_t kLboB = 3 * COUT * 16;     // chunk stride of B
-      bool ok = mbar_wait(smem_u32(&bar_w), 0, &abort_flag);
+      bool ok = mbar_wait(smem_u32(&bar_w), 0, &abort_flag, a.wait_ns);
       long long j = 0, i0 = 0;   // slab loads and output rows before this column
       for (long long u = blockIdx.x; ok && u < nunits; u += gridDim.x) {
         for (int p = 0; p < zc + 2; ++p) {
           if (p < zc) {   // row p is first written now: its accumulator must be drained
             const long long i = i0 + p, use = i / kRing;
-            if (use > 0 && !mbar_wait(smem_u32(&bar_acce[acc_slot(i)]), (uint32_t)((use - 1) & 1), &abort_flag)) {
+            if (use > 0 && !mbar_wait(smem_u32(&bar_acce[acc_slot(i)]), (uint32_t)((use - 1) & 1), &abort_flag,
+                                      a.wait_ns)) {
               ok = false;
               break;
             }
           }
           const long long jj = j + p;
           const int slot = (int)(jj % S);
-          if (!mbar_wait(smem_u32(&bar_full[slot]), (uint32_t)((jj / S) & 1), &abort_flag)) {
+          if (!mbar_wait(smem_u32(&bar_full[slot]), (uint32_t)((jj / S) & 1), &abort_flag, a.wait_ns)) {
             ok = false;
             break;
           }
@@ -538,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       if (!ok) give_up(&abort_flag, a.err);
       // every MMA issued has completed before TMEM is freed
       mma_commit(smem_u32(&bar_fin));
-      mbar_wait(smem_u32(&bar_fin), 0, &abort_flag);
+      mbar_drain(smem_u32(&bar_fin), 0);
     }
   } else {
     // ---- epilogue: two teams of 4 warps take alternate output rows (a ring
@@ -554,7 +572,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       for (int zl = 0; zl < zc; ++zl, ++i) {
         if ((int)(i & 1) != team) continue;
         const int s = acc_slot(i);
-        const bool w = mbar_wait(smem_u32(&bar_accf[s]), (uint32_t)((i / kRing) & 1), &abort_flag);
+        const bool w = mbar_wait(smem_u32(&bar_accf[s]), (uint32_t)((i / kRing) & 1), &abort_flag, a.wait_ns);
         if (!__all_sync(0xffffffffu, w)) {
           ok = false;
           break;
@@ -737,6 +755,8 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
   a.relu = c.relu;
   a.n = n;
   a.err = c.err;
+  a.wait_ns = c.wait_ns;
+  a.hold_back = LOADER == kLoadTma ? c.hold_back : 0;
   // rows per column: the choice that balances the persistent CTAs best
   const long long ctas = (long long)kNumSMs * blocks_per_sm[dev];
   int best = 0;

@@ -524,6 +524,149 @@ __global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restr
   }
 }
 
+// The running residual of resid_pairs_kernel with the window streamed in z:
+// a block owns a 32 x 16 x TZ tile and keeps only three plane pairs of its
+// window in shared memory, a ring of slots.  Output pair k reads pairs k and
+// k + 1; the loads of pair k + 2 are issued into registers before pair k is
+// computed and stored into the slot pair k - 1 held after it, so they land
+// while the stencil runs instead of in a separate load phase (one barrier per
+// pair).  Per-cell arithmetic, thread mapping and window layout within a
+// pair are those of resid_pairs_kernel, so the results are the same bits.
+template <bool LOCAL, int TZ>
+__global__ void __launch_bounds__(NT, 2) resid_pairz_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
+                                                          float* __restrict__ r, LG G, float shift,
+                                                          float* __restrict__ acc) {
+  constexpr int TY = 16, SY = TY + 2;
+  constexpr int PR = 2 * WX;         // floats per row of a plane pair
+  constexpr int PP = SY * PR;        // floats per plane pair (one ring slot)
+  constexpr int NK = TZ / 2;         // output pairs per thread
+  constexpr int NS = 3;              // ring slots
+  constexpr int LT = SY * CH;        // 16-byte chunks of one plane of a pair: one per loading thread
+  static_assert(NWARP == TY, "one warp per output row");
+  static_assert(LT <= NT, "one chunk per thread and plane");
+  extern __shared__ __align__(16) float smem[];
+  float* sw = smem;                                   // NS slots
+  int* roy = reinterpret_cast<int*>(sw + NS * PP);    // SY row offsets (y part)
+  float* sp = reinterpret_cast<float*>(roy + SY);     // px (WX) | py (SY) | pz (TZ + 2)
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ly = 1 + warp, lx = XH + lane;
+  const size_t plane = (size_t)G.n[0] * G.n[1];
+  const size_t col = (size_t)(y0 + warp) * G.n[0] + x0 + lane;
+  float r0[2] = {0.0f, 0.0f}, r1[2] = {0.0f, 0.0f}, a0[2] = {0.0f, 0.0f}, a1[2] = {0.0f, 0.0f};
+  auto issue = [&](int k, float* rr, float* aa) {
+    if (k < NK) {
+      const size_t o = col + (size_t)(z0 + 2 * k) * plane;
+      rr[0] = __ldg(rhs + o);
+      rr[1] = __ldg(rhs + o + plane);
+      if (acc) { aa[0] = acc[o]; aa[1] = acc[o + plane]; }
+    }
+  };
+  issue(0, r0, a0);
+  issue(1, r1, a1);
+  // this thread's chunk of a plane pair: window row yy, x chunk c
+  const int lrow = threadIdx.x / CH, lc = threadIdx.x - CH * lrow;
+  const bool loader = threadIdx.x < LT;
+  const int xo = wrapi(x0 - XH + 4 * lc, G.n[0]);
+  const int yoff = loader ? G.n[0] * wrapi(y0 - 1 + lrow, G.n[1]) : 0;
+  // window plane w (0 = z0 - 1) of the mesh: periodic plane offset
+  auto zoff = [&](int w) { return (size_t)wrapi(z0 - 1 + w, G.n[2]) * plane; };
+  float4 pa, pb;   // chunk of plane pair j in flight
+  auto fetch = [&](int j) {
+    if (loader) {
+      pa = __ldg(reinterpret_cast<const float4*>(e + zoff(2 * j) + yoff + xo));
+      pb = __ldg(reinterpret_cast<const float4*>(e + zoff(2 * j + 1) + yoff + xo));
+    }
+  };
+  auto put = [&](int slot) {
+    if (loader) {
+      float4* d = reinterpret_cast<float4*>(sw + slot * PP + lrow * PR + 8 * lc);
+      d[0] = make_float4(pa.x, pb.x, pa.y, pb.y);
+      d[1] = make_float4(pa.z, pb.z, pa.w, pb.w);
+    }
+  };
+  fetch(0);
+  {
+    const float4 qa = pa, qb = pb;
+    fetch(1);
+    if (loader) {
+      float4* d = reinterpret_cast<float4*>(sw + lrow * PR + 8 * lc);
+      d[0] = make_float4(qa.x, qb.x, qa.y, qb.y);
+      d[1] = make_float4(qa.z, qb.z, qa.w, qb.w);
+    }
+  }
+  put(1);
+  if (LOCAL) {
+    for (int q = threadIdx.x; q < WX; q += NT) sp[q] = G.P[0][wrapi(x0 - XH + q, G.n[0])];
+    for (int q = threadIdx.x; q < SY; q += NT) sp[WX + q] = G.P[1][wrapi(y0 - 1 + q, G.n[1])];
+    for (int q = threadIdx.x; q < TZ + 2; q += NT) sp[WX + SY + q] = G.P[2][wrapi(z0 - 1 + q, G.n[2])];
+  }
+  __syncthreads();
+  const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1];
+  const float px2 = px * px, py2 = py * py;
+  const float dxy = G.cell2[0] * px2 + G.cell2[1] * py2;
+  auto L = [&](int q) { return *reinterpret_cast<const f2*>(sw + q); };
+  auto C = [](f2 a, f2 b) {
+    float a0, a1, b0, b1;
+    U2(a, a0, a1);
+    U2(b, b0, b1);
+    return P2(a1, b0);
+  };
+  constexpr int OX = 2, OY = PR;
+#pragma unroll 1
+  for (int k = 0; k < NK; ++k) {
+    const float rA = r0[0], rB = r0[1], aA = a0[0], aB = a0[1];
+    r0[0] = r1[0]; r0[1] = r1[1]; a0[0] = a1[0]; a0[1] = a1[1];
+    issue(k + 2, r1, a1);
+    if (k + 2 <= NK) fetch(k + 2);   // pairs 0 .. NK of the window
+    const f2 Pz = LOCAL ? P2(sp[WX + SY + 2 * k + 1], sp[WX + SY + 2 * k + 2]) : B2(G.pg[2]);
+    const f2 pz2 = mul2(Pz, Pz);
+    float dA, dB;
+    U2(fma2(B2(G.cell2[2]), pz2, B2(dxy)), dA, dB);
+    const f2 g = P2(__fdividef(G.beta, dA), __fdividef(G.beta, dB));
+    const f2 gpz = fma2(g, pz2, B2(G.icell2[2]));
+    const f2 hg = mul2(B2(0.5f), g);
+    const int q0 = ((k % NS) * SY + ly) * PR + 2 * lx, q1 = (((k + 1) % NS) * SY + ly) * PR + 2 * lx;
+    const f2 zm = L(q0), zp = L(q1);
+    const f2 s0 = C(zm, zp);
+    f2 o = mul2(gpz, add2(sub2(zp, s0), sub2(zm, s0)));
+    if (LOCAL) o = fma2(mul2(g, Pz), sub2(zp, zm), o);
+    {   // x neighbours and the x-z diagonals
+      const f2 kp = L(q0 + OX), km = L(q0 - OX), lp = L(q1 + OX), lm = L(q1 - OX);
+      const f2 xp = C(kp, lp), xm = C(km, lm);
+      o = fma2(fma2(g, B2(px2), B2(G.icell2[0])), add2(sub2(xp, s0), sub2(xm, s0)), o);
+      o = fma2(mul2(hg, mul2(B2(px), Pz)), sub2(add2(sub2(lp, s0), sub2(km, s0)), add2(sub2(lm, s0), sub2(kp, s0))), o);
+      if (LOCAL) o = fma2(mul2(g, B2(px)), sub2(xp, xm), o);
+    }
+    {   // y neighbours and the y-z diagonals
+      const f2 kp = L(q0 + OY), km = L(q0 - OY), lp = L(q1 + OY), lm = L(q1 - OY);
+      const f2 yp = C(kp, lp), ym = C(km, lm);
+      o = fma2(fma2(g, B2(py2), B2(G.icell2[1])), add2(sub2(yp, s0), sub2(ym, s0)), o);
+      o = fma2(mul2(hg, mul2(B2(py), Pz)), sub2(add2(sub2(lp, s0), sub2(km, s0)), add2(sub2(lm, s0), sub2(kp, s0))), o);
+      if (LOCAL) o = fma2(mul2(g, B2(py)), sub2(yp, ym), o);
+    }
+    {   // x-y diagonals (in-plane)
+      const f2 pp = C(L(q0 + OX + OY), L(q1 + OX + OY)), mm = C(L(q0 - OX - OY), L(q1 - OX - OY));
+      const f2 mp = C(L(q0 - OX + OY), L(q1 - OX + OY)), pm = C(L(q0 + OX - OY), L(q1 + OX - OY));
+      o = fma2(mul2(hg, B2(px * py)), sub2(add2(sub2(pp, s0), sub2(mm, s0)), add2(sub2(mp, s0), sub2(pm, s0))), o);
+    }
+    float oA, oB, sA, sB;
+    U2(o, oA, oB);
+    U2(s0, sA, sB);
+    const size_t ga = col + (size_t)(z0 + 2 * k) * plane;
+    r[ga] = (rA - shift) + oA;
+    r[ga + plane] = (rB - shift) + oB;
+    if (acc) {
+      acc[ga] = aA + sA;
+      acc[ga + plane] = aB + sB;
+    }
+    // pair k + 2 goes where pair k - 1 was: every thread finished with that
+    // slot before the barrier that ended iteration k - 1
+    if (k + 2 <= NK) put((k + 2) % NS);
+    __syncthreads();
+  }
+}
+
 // r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
 // operator, whose coefficients are evaluated with IEEE round-to-nearest
 // operations in the reference's order.  Per-block (Σr, Σr²) to part.  The
@@ -707,6 +850,16 @@ cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   return cudaGetLastError();
 }
 
+template <bool LOCAL, int TZ>
+cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+  auto k = resid_pairz_kernel<LOCAL, TZ>;
+  constexpr size_t b = sizeof(float) * (3 * (16 + 2) * 2 * WX + WX + (16 + 2) + TZ + 2) + sizeof(int) * (16 + 2);
+  cudaError_t e = allow_smem(k, b);
+  if (e != cudaSuccess) return e;
+  k<<<dim3(G.n[0] / TX, G.n[1] / 16, G.n[2] / TZ), NT, b, s>>>(ec, rhs, r, G, 0.0f, acc);
+  return cudaGetLastError();
+}
+
 template <bool LOCAL>
 cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
   auto k = resid_pairs_kernel<LOCAL>;
@@ -762,6 +915,10 @@ cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, floa
 
 cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
   const bool big = big_tiles(G);
+  if (big && G.pairs == 3 && G.n[2] % 32 == 0)
+    return G.local ? pairz_t<true, 32>(s, ec, rhs, r, G, acc) : pairz_t<false, 32>(s, ec, rhs, r, G, acc);
+  if (big && G.pairs >= 2)
+    return G.local ? pairz_t<true, 16>(s, ec, rhs, r, G, acc) : pairz_t<false, 16>(s, ec, rhs, r, G, acc);
   if (big && G.pairs) return G.local ? pairs_t<true>(s, ec, rhs, r, G, acc) : pairs_t<false>(s, ec, rhs, r, G, acc);
   if (!G.local)
     return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)

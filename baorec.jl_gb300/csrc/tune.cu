@@ -117,11 +117,13 @@ int tune_stencils(baorec_ctx* ctx) {
     ctx->tune.stream0 = ms[1] <= ms[0] ? 1 : 0;
   }
   // finest level: the tiled running residual with two z-adjacent cells per
-  // thread (packed FP32x2) against one cell per thread
+  // thread (packed FP32x2) against one cell per thread, and the packed form
+  // with its window streamed in z (blocks of 16 and 32 planes)
   if (nl > 0 && tile_ok(L0.n)) {
     float* t = L0.r + L0.N;
-    float ms[2] = {0.0f, 0.0f};
-    for (int form = 0; form < 2; ++form) {
+    float ms[4] = {0.0f, 0.0f, 1e30f, 1e30f};
+    const int nforms = (L0.n[1] % 16 == 0 && L0.n[2] % 16 == 0) ? 4 : 2;
+    for (int form = 0; form < nforms; ++form) {
       ctx->tune.pairs = form;
       const LG G0 = level_geom_public(ctx, 0, 0.0f);
       auto launch = [&]() -> int {
@@ -131,7 +133,10 @@ int tune_stencils(baorec_ctx* ctx) {
       CKS(time_ms(ctx, launch, 10, &ms[form]));
       ctx->launches += 11;
     }
-    ctx->tune.pairs = ms[1] <= ms[0] ? 1 : 0;
+    int best = 0;
+    for (int form = 1; form < 4; ++form)
+      if (ms[form] < ms[best]) best = form;
+    ctx->tune.pairs = best;
   }
   // FFT preconditioner: batched xy transforms around the fused z pass (two
   // register forms; xy transforms by cuFFT or, for 256 x 256 planes, by the
@@ -200,7 +205,7 @@ extern "C" int baorec_set_tune_stream(baorec_ctx* ctx, int stream) {
 extern "C" int baorec_tune_pairs(const baorec_ctx* ctx) { return ctx ? ctx->tune.pairs : -1; }
 
 extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
-  if (!ctx || pairs < 0 || pairs > 1) return BAOREC_ERR_ARG;
+  if (!ctx || pairs < 0 || pairs > 3) return BAOREC_ERR_ARG;
   ctx->tune.pairs = pairs;
   return BAOREC_OK;
 }

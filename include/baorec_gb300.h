@@ -443,6 +443,15 @@ int32_t baorec_guess_tc_layers(baorec_ctx* ctx);
  * (BAOREC_ERR_ARG for 1 and 2 if the shape or n has none). */
 int baorec_guess_conv3(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, const void* x, const float* w,
                        const float* bias, const void* add, void* y, int32_t relu, int32_t path);
+/* Test hook of the bounded device waits (no reference counterpart): one
+ * tcgen05 convolution (zero input and weights, cin -> cout on an n^3 grid)
+ * whose slab loader is held back, so that no slab ever arrives and the
+ * pipeline's waits, limited to wait_ns each, expire.  The kernel records the
+ * timeout in the context's device error word, every role stops, the block
+ * waits for its weight copy and frees its TMEM, and the call returns
+ * BAOREC_ERR_CUDA with a "timed out" message; the context stays usable.
+ * BAOREC_ERR_ARG for shapes without a tcgen05 kernel. */
+int baorec_guess_conv3_held_back(baorec_ctx* ctx, int32_t cin, int32_t cout, int32_t n, int64_t wait_ns);
 /* Average device time (CUDA events on the context's stream) of `reps`
  * launches of one network convolution cin -> cout on an n^3 grid (path as in
  * baorec_guess_conv3) and its algorithmic FLOPs, 2 * 27 * cin * cout * n^3. */
@@ -501,7 +510,9 @@ int baorec_tune_stream(const baorec_ctx* ctx);
 int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
 /* FP32 running residual of the FFT corrections on 32x16x16 tiles: 1 two
  * z-adjacent cells per thread in packed FP32x2 arithmetic (default), 0 one cell
- * per thread.  The stencil autotune times both. */
+ * per thread, 2 and 3 the packed form with the window streamed through a ring
+ * of plane pairs in blocks of 16 and 32 z planes (the same results as 1).
+ * The stencil autotune times all four. */
 int baorec_tune_pairs(const baorec_ctx* ctx);
 int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
 /* FFT preconditioner of the residual-driven solve where n[2] = 256: 1 batched

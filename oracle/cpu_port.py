@@ -1,5 +1,8 @@
 """The reference's CPU reconstruction path, restated in C (cpu_ref.c, OpenMP)
 plus scipy.fft — the timed CPU baseline (test infrastructure, never the product).
+A second solver, the GPU's FFT-preconditioned defect correction to a 1e-6
+relative residual, can replace the reference's FMG schedule for a CPU timing
+of the same work the GPU does.
 
 One call of :meth:`CpuPort.lightcone_reconstruction` does what BAOrec.jl's
 CPU path does for a lightcone with multigrid (``examples/lightcone_mg.jl``):
@@ -132,8 +135,21 @@ class CpuPort:
 
         return fmg(f, tuple(n))
 
-    def lightcone_reconstruction(self, m, n, bs, bm, bias=2.0, growth=0.8, R=15.0, ran_min=0.01):
-        """One reconstruction; returns (data :sum, randoms :sum, randoms :disp) positions."""
+    def solve_convergent(self, f, n, bs, bm, beta, rtol=1e-6):
+        """The GPU's solver on the host: defect correction with the FFT
+        preconditioner of the box's mean line of sight (oracle/fp64_oracle.py,
+        FP64, C operator with OpenMP, scipy.fft with every core) until the
+        relative residual is below rtol."""
+        import fp64_oracle as P
+        phi, _, hist = P.solve(self._mesh3(f, n), bs, bm, beta, None, rtol=rtol)
+        self.last_history = hist
+        return np.asarray(phi, dtype=np.float64).ravel(order="F").astype(F32)
+
+    def lightcone_reconstruction(self, m, n, bs, bm, bias=2.0, growth=0.8, R=15.0, ran_min=0.01, solver="fmg"):
+        """One reconstruction; returns (data :sum, randoms :sum, randoms :disp)
+        positions.  solver "fmg" is the reference's schedule
+        (src/multigrid.jl:722-752); "convergent" solves to a 1e-6 relative
+        residual like the GPU's residual-driven solve."""
         N = int(np.prod(n))
         d = np.zeros(N, F32)
         r = np.zeros(N, F32)
@@ -147,7 +163,7 @@ class CpuPort:
         d = d - al * r
         d = np.where(r > thr, d / np.where(r > thr, F32(bias) * al * r, F32(1)), F32(0)).astype(F32)
         beta = F32(F32(growth) / F32(bias))
-        phi = self.fmg(d, n, bs, bm, beta)
+        phi = self.fmg(d, n, bs, bm, beta) if solver == "fmg" else self.solve_convergent(d, n, bs, bm, beta)
         grads = self.gradient(phi, n, bs)
         out = []
         for (x, y, z), field in (((m.x, m.y, m.z), "sum"), ((m.rx, m.ry, m.rz), "sum"), ((m.rx, m.ry, m.rz), "disp")):

@@ -80,7 +80,8 @@ def test_trained_network_improves_the_fft_start_and_keeps_the_solution():
     r_un = np.mean([b / a for a, b in untrained])
     r_tr = np.mean([b / a for a, b in trained])
     print("learned / FFT start residual: untrained %.3f, trained %.3f" % (r_un, r_tr))
-    assert r_tr < 0.99 and r_tr < r_un
+    # trained for 20k Adam steps (batch 4) at this geometry: about 0.37 of the FFT start's residual
+    assert r_tr < 0.5 and r_tr < r_un
     # the learned start changes the path, not the answer
     n = 128
     f = torch.empty(n ** 3, device="cuda")
@@ -133,7 +134,9 @@ def test_learned_start_on_the_restriction_of_the_lightcone_mesh():
     r_fft = guess.start_residual(ctx, f.data_ptr(), "spectral")
     r_l = guess.start_residual(ctx, f.data_ptr(), "learned")
     print("256^3 start residual: FFT %.4f, learned on the restriction %.4f (ratio %.3f)" % (r_fft, r_l, r_l / r_fft))
-    assert r_l < r_fft
+    # a perfect correction on the restriction would give about 0.77 (the prolonged correction leaves the
+    # error's fine-scale part); the trained network gives about 0.83
+    assert r_l < 0.9 * r_fft
     grads = {}
     for start, rec in recs.items():
         phi = baorec.zeros_mesh((n,) * 3)

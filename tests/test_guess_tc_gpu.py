@@ -169,3 +169,29 @@ def test_network_tcgen05_matches_mma_forward_and_gradients():
     assert rel(o1, o0) < 1e-2, rel(o1, o0)
     assert abs(l1 - l0) / l0 < 1e-3
     assert rel(g1, g0) < 2e-2, rel(g1, g0)
+
+
+def test_expired_waits_return_a_status_and_leave_the_context_usable():
+    """The bounded waits of the tcgen05 convolution: with the slab loader held
+    back and every pipeline wait limited to 20 µs, the waits expire, the
+    kernel records the timeout (no trap, no fault), every role stops, the
+    block waits for its weight copy and frees its TMEM, and the call returns a
+    status.  The context then runs a normal convolution that equals the
+    mma.sync kernel's, and a second expiry behaves the same."""
+    import torch
+    from baorec import _lib, guess
+    n = 128
+    ctx = _ctx(n)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        st = ctx.status("baorec_guess_conv3_held_back", 16, 16, n, 20_000)
+        assert st == _lib.ERR_CUDA
+        assert "timed out" in ctx.lib.baorec_last_error(ctx.h).decode()
+        x = _bf16(rng.normal(size=(n, n, n, 16))).cuda()
+        w = torch.from_numpy(rng.normal(scale=0.1, size=(27, 16, 16)).astype(np.float32)).cuda()
+        y_tc = guess.conv3(ctx, x, w, relu=False, path="tcgen05")
+        y_ms = guess.conv3(ctx, x, w, relu=False, path="mma")
+        a, b = y_tc.float().cpu().numpy(), y_ms.float().cpu().numpy()
+        assert np.max(np.abs(a - b)) <= 2e-2 * np.max(np.abs(b)), np.max(np.abs(a - b))
+    # shapes without a tcgen05 kernel are refused before any launch
+    assert ctx.status("baorec_guess_conv3_held_back", 16, 16, 96, 20_000) == _lib.ERR_ARG

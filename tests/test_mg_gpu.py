@@ -285,3 +285,40 @@ def test_cycle_cap_returns_not_converged_with_the_last_iterate():
     st2 = baorec.solve_(phi2, ff, rec2, phi0=np.asfortranarray(phi))
     assert st2["rel_residual"] <= 1e-6
     assert st2["rel_residual_initial"] <= 1.05 * st["rel_residual"]
+
+
+@pytest.mark.parametrize("shape,los", [((64, 64, 64), None), ((32, 48, 96), [0.0, 0.6, 0.8]), ((64, 32, 48), None)])
+def test_streamed_pair_running_residual_is_bit_identical(shape, los):
+    """The running residual with its window streamed through a ring of plane
+    pairs (16- and 32-plane blocks; the 32-plane form falls back to 16 where
+    n3 is not a multiple of 32) does the packed pair kernel's arithmetic cell
+    for cell: the FFT start's residual, the solve history and the solution
+    are the same bits."""
+    import ctypes as C
+    import torch
+    import baorec
+    from baorec import guess
+    bs = np.array([10.0 * s for s in shape], F32) * F32(9.0)
+    bm = np.array([300.0, -200.0, 150.0], F32)
+    rng = np.random.default_rng(31)
+    f = O.smooth(rng.standard_normal(shape).astype(F32), 40.0, bs)
+    f = (f - f.mean(dtype=np.float64)).astype(F32)
+    ff = np.asfortranarray(f)
+    fd = torch.from_numpy(np.ascontiguousarray(f.ravel(order="F"))).cuda()
+    out = []
+    for pairs in (1, 2, 3):
+        rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="spectral")
+        ctx = baorec.setup_fft_(rec, shape)
+        ctx.call("baorec_set_tune", 8, (C.c_int32 * 16)(*([1] * 16)))
+        ctx.call("baorec_set_tune_stream", 0)
+        ctx.call("baorec_set_tune_pairs", pairs)
+        assert ctx.lib.baorec_tune_pairs(ctx.h) == pairs
+        rel = guess.start_residual(ctx, fd.data_ptr(), "spectral")
+        phi = baorec.zeros_mesh(shape, device=False)
+        st = baorec.solve_(phi, ff, rec)
+        assert st["rel_residual"] <= 1e-6
+        out.append((rel, ctx.solve_history(), np.asarray(phi).copy()))
+    for rel, hist, phi in out[1:]:
+        assert rel == out[0][0]
+        assert hist == out[0][1]
+        np.testing.assert_array_equal(phi, out[0][2])

@@ -144,15 +144,26 @@ def test_headline_shifted_positions_match_oracle_pipeline(headline):
     assert int(((f_np == 0) != (h["f_or"] == 0)).sum()) <= 8
     phi64, _, _ = P.solve(f_np, bs, bm, BETA, None, rtol=1e-11)
     grads = tuple(g.astype(F32) for g in P.gradient_meshes(phi64, bs.astype(np.float64)))
-    worst = 0.0
+    # the FP32 floor of the reference's formula: the oracle's FP32 transform of the solution rounded to FP32
+    grads32 = O.gradient_meshes(np.ascontiguousarray(phi64.astype(F32)), bs)
+    worst, floor, sq, sq_floor, cnt = 0.0, 0.0, 0.0, 0.0, 0
     for (x, y, z), field, got in (((m.x, m.y, m.z), "sum", got_d), ((m.rx, m.ry, m.rz), "sum", got_rs),
                                   ((m.rx, m.ry, m.rz), "disp", got_ri)):
-        disp = tuple(O.read_cic(g, x, y, z, bs, bm) for g in grads)
-        ref = O.reconstructed_positions(O.read_shifts(disp, x, y, z, GROWTH, los=None, field=field), x, y, z)
+        ref = O.reconstructed_positions(O.read_shifts(tuple(O.read_cic(g, x, y, z, bs, bm) for g in grads),
+                                                      x, y, z, GROWTH, los=None, field=field), x, y, z)
+        r32 = O.reconstructed_positions(O.read_shifts(tuple(O.read_cic(g, x, y, z, bs, bm) for g in grads32),
+                                                      x, y, z, GROWTH, los=None, field=field), x, y, z)
         for a in range(3):
-            worst = max(worst, float(np.max(np.abs(got[a].cpu().numpy() - ref[a]))))
-    print("max |dpos| vs oracle FP64 solve + FP32 read-out", worst, "Mpc/h")
-    assert worst < 1e-3
+            d = got[a].cpu().numpy().astype(np.float64) - ref[a]
+            d32 = r32[a].astype(np.float64) - ref[a]
+            worst, floor = max(worst, float(np.max(np.abs(d)))), max(floor, float(np.max(np.abs(d32))))
+            sq, sq_floor, cnt = sq + float(np.sum(d * d)), sq_floor + float(np.sum(d32 * d32)), cnt + d.size
+    rms, rms_floor = np.sqrt(sq / cnt), np.sqrt(sq_floor / cnt)
+    print("|dpos| vs oracle FP64 solve + FP32 read-out: max", worst, "rms", rms, "Mpc/h; the FP32 formula's own: max",
+          floor, "rms", rms_floor)
+    # 1e-3 Mpc/h, or the reference formula's FP32 floor where that is larger (displacements reach 180 Mpc/h here)
+    assert worst <= max(1e-3, 3.0 * floor)
+    assert rms <= 2.0 * rms_floor + 1e-5
 
 
 def test_box_config_matches_oracle_and_fp64():
