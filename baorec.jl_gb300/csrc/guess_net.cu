@@ -974,6 +974,11 @@ int move_params(baorec_ctx* ctx, baorec_ctx* from, baorec_ctx* to) {
 }  // namespace
 
 int guess_dispatch_apply(baorec_ctx* ctx, const float* f, float* phi0) {
+  // With one line of sight for the whole box the operator is a convolution
+  // and the FFT start S⁻¹f is its exact inverse: the error the network
+  // predicts is zero (and the network only ever saw the radial line of
+  // sight), so the learned start is the FFT start.
+  if (ctx->cfg.los_mode == BAOREC_LOS_GLOBAL) return spectral_correction(ctx, f, phi0);
   return ctx->guess_level == 1 && ctx->guess_child ? guess_apply_coarse(ctx, f, phi0) : guess_apply(ctx, f, phi0);
 }
 

@@ -809,12 +809,15 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   float* loA = ctx->phi_lo;
   float* loB = ctx->phi_lo2;
   if (phi0 && phi0 != phi) CK(cudaMemcpyAsync(hiA, phi0, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-  if (!phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED) CKS(guess_dispatch_apply(ctx, f, hiA));
   else if (!phi0) CK(cudaMemsetAsync(hiA, 0, N * 4, ctx->stream));
   // The first residual of a zero solution needs no stencil: r = f - α with
   // α = mean f, so Σr = 0 and |r| = |f - α| (relative residual 1), and the
-  // solution pair stays zero.
-  const bool zero_start = !phi0 && ctx->cfg.mg_start != BAOREC_START_LEARNED;
+  // solution pair stays zero.  The FFT start and the learned start are that
+  // zero start's first correction: d_0 = S⁻¹ r (FFT start) or d_0 = S⁻¹ r +
+  // the network's correction (learned start; S⁻¹ r = S⁻¹ f, the mean being
+  // outside S⁻¹'s range), so neither needs an accurate residual of its own.
+  const bool zero_start = !phi0;
+  const bool learned = !phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED;
   CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
   // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²), in one pass; the host reads
   // them when it first needs them (a zero start forms its first residual and
@@ -864,7 +867,8 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       CKLAUNCH();
       // the first FFT correction needs only r: queue it before waiting for the sums
       if (spectral && ctx->cfg.max_cycles > 0) {
-        CKS(spectral_correction(ctx, L0.f, L0.v));
+        if (learned) CKS(guess_dispatch_apply(ctx, f, L0.v));
+        else CKS(spectral_correction(ctx, L0.f, L0.v));
         speculative = true;
       }
       CKS(read_sums());

@@ -529,12 +529,13 @@ def _fp64_solve_check(torch, np, ctx, X, R, bs, bm, n):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import baorec
     import fp64_oracle as P
-    fd = baorec.zeros_mesh(n)
+    # torch fills these on its own stream: finish that before the context's stream uses them
+    fd, phi = baorec.zeros_mesh(n), baorec.zeros_mesh(n)
+    g = [baorec.zeros_mesh(n) for _ in range(3)]
+    torch.cuda.synchronize()
     ctx.call("baorec_setup_overdensity_randoms", fd.data_ptr(), *[t.data_ptr() for t in X], X[0].numel(),
              *[t.data_ptr() for t in R], R[0].numel(), 0)
-    phi = baorec.zeros_mesh(n)
     ctx.call("baorec_mg_solve", fd.data_ptr(), phi.data_ptr(), None, None)
-    g = [baorec.zeros_mesh(n) for _ in range(3)]
     ctx.call("baorec_set_result", phi.data_ptr(), 0)
     ctx.call("baorec_displacement_meshes", *[t.data_ptr() for t in g])
     torch.cuda.synchronize()
@@ -560,10 +561,13 @@ def _fp64_large_box_check(torch, np, cit, cmg, B, n):
     import fp64_oracle as P
     L = np.array([3000.0] * 3)
     d = baorec.zeros_mesh(n)
-    xs = [torch.empty_like(t) for t in B[:3]]
-    for a, b in zip(xs, B[:3]):
-        a.copy_(b)
-    cit.call("baorec_setup_overdensity", d.data_ptr(), *[t.data_ptr() for t in xs], B[3].data_ptr(), B[0].numel(), 1, 0)
+    g = [baorec.zeros_mesh(n) for _ in range(3)]
+    phi = baorec.zeros_mesh(n)
+    # torch fills these on its own stream: finish that before the contexts' streams use them; the paint
+    # without BAOREC_WRITEBACK leaves the positions as they are
+    torch.cuda.synchronize()
+    cit.call("baorec_setup_overdensity", d.data_ptr(), *[t.data_ptr() for t in B[:3]], B[3].data_ptr(), B[0].numel(),
+             1, 0)
     torch.cuda.synchronize()
     d64 = d.cpu().numpy().astype(np.float64)
     O.set_fft_workers(os.cpu_count())
@@ -573,14 +577,12 @@ def _fp64_large_box_check(torch, np, cit, cmg, B, n):
     for it in range(1, 6):
         dr = O.iterate(dr, d64, k, it, beta, los=[0.0, 0.0, 1.0])
     psi64 = O.displacement_meshes_iterative(dr, L)
-    g = [baorec.zeros_mesh(n) for _ in range(3)]
     cit.call("baorec_displacement_meshes", *[t.data_ptr() for t in g])
     torch.cuda.synchronize()
     it_err = P.rel_l2_vector([t.cpu().numpy() for t in g], psi64)
     del psi64, dr
     phi64, _, hist = P.solve(d64, L, np.zeros(3), np.float32(beta), [0.0, 0.0, 1.0], rtol=1e-10)
     g64 = P.gradient_meshes(phi64, L)
-    phi = baorec.zeros_mesh(n)
     cmg.call("baorec_mg_solve", d.data_ptr(), phi.data_ptr(), None, None)
     cmg.call("baorec_set_result", phi.data_ptr(), 0)
     cmg.call("baorec_displacement_meshes", *[t.data_ptr() for t in g])
@@ -615,6 +617,7 @@ def oracle_checks(args, torch, np, ctxs, m, bs, bm, X, R, box):
     t0 = time.perf_counter()
     c0 = next(iter(ctxs.values()))
     fd = baorec.zeros_mesh(n)
+    torch.cuda.synchronize()   # torch zero-fills on its own stream
     c0.call("baorec_setup_overdensity_randoms", fd.data_ptr(), *[t.data_ptr() for t in X], X[0].numel(),
             *[t.data_ptr() for t in R], R[0].numel(), 0)
     torch.cuda.synchronize()
@@ -622,8 +625,9 @@ def oracle_checks(args, torch, np, ctxs, m, bs, bm, X, R, box):
     grads = {}
     for start, c in ctxs.items():
         phi = baorec.zeros_mesh(n)
-        st = c.status("baorec_mg_solve", fd.data_ptr(), phi.data_ptr(), None, None)
         g = [baorec.zeros_mesh(n) for _ in range(3)]
+        torch.cuda.synchronize()
+        st = c.status("baorec_mg_solve", fd.data_ptr(), phi.data_ptr(), None, None)
         c.call("baorec_set_result", phi.data_ptr(), 0)
         c.call("baorec_displacement_meshes", *[t.data_ptr() for t in g])
         torch.cuda.synchronize()
@@ -646,6 +650,7 @@ def oracle_checks(args, torch, np, ctxs, m, bs, bm, X, R, box):
     nb = (bctx.cfg.n[0],) * 3
     # the timed steps painted the same catalog (positions inside the box, nothing wraps)
     psi = [baorec.zeros_mesh(nb) for _ in range(3)]
+    torch.cuda.synchronize()
     bctx.call("baorec_displacement_meshes", *[t.data_ptr() for t in psi])
     torch.cuda.synchronize()
     d64, _, _, _ = O.run_iterative(nb, 2.0, 0.8, 15.0, bm_.x, bm_.y, bm_.z, bm_.w, box_size=[L] * 3,

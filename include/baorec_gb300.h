@@ -61,7 +61,8 @@ typedef enum {
 #define BAOREC_MG_CONVERGENT 1  /* residual-driven V-cycles to rtol (no reference counterpart) */
 #define BAOREC_START_ZERO     0 /* convergent mode: V-cycles from a zero potential (plain multigrid) */
 #define BAOREC_START_SPECTRAL 1 /* convergent mode: FFT-preconditioned corrections first (no reference counterpart) */
-#define BAOREC_START_LEARNED  2 /* convergent mode: CNN initial guess, then as SPECTRAL (no reference counterpart) */
+#define BAOREC_START_LEARNED  2 /* convergent mode: CNN initial guess, then as SPECTRAL; with a fixed line of
+                                   sight the FFT start is exact and is the learned start (no reference counterpart) */
 #define BAOREC_FIELD_DISP 0     /* :disp */
 #define BAOREC_FIELD_RSD  1     /* :rsd  */
 #define BAOREC_FIELD_SUM  2     /* :sum  */

@@ -149,3 +149,27 @@ def test_learned_start_on_the_restriction_of_the_lightcone_mesh():
     assert ctx.lib.baorec_guess_level(ctx.h) == 0
     np.testing.assert_array_equal(guess.get_params(ctx), W)
     assert ctx.status("baorec_guess_set_level", 2) == _lib.ERR_ARG
+
+
+def test_learned_start_is_the_fft_start_for_a_fixed_line_of_sight():
+    """With one line of sight the FFT start is the exact inverse of the
+    operator: the learned start equals it (no network correction) and both
+    start at the residual the FFT's rounding leaves."""
+    import torch
+    import baorec
+    from baorec import guess
+    W = guess.load_params(f"{guess.WEIGHTS_DIR}/guess_lightcone.npy")
+    n = 128
+    rng = np.random.default_rng(4)
+    bs = np.array([1500.0] * 3, np.float32)
+    f = O.smooth(rng.standard_normal((n, n, n)).astype(np.float32), 30.0, bs)
+    fd = torch.from_numpy(np.ascontiguousarray(f.ravel(order="F"))).cuda()
+    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=[0.0] * 3,
+                                los=[0.0, 0.0, 1.0], mg_mode="convergent", rtol=1e-6, start="learned",
+                                guess_params=W, guess_level=1)
+    ctx = baorec.setup_fft_(rec, (n,) * 3)
+    torch.cuda.synchronize()
+    r_fft = guess.start_residual(ctx, fd.data_ptr(), "spectral")
+    r_l = guess.start_residual(ctx, fd.data_ptr(), "learned")
+    print("fixed line of sight: FFT start", r_fft, "learned", r_l)
+    assert r_l == r_fft and r_fft < 1e-5
