@@ -4,6 +4,7 @@
 // the 8-channel input layer).
 #include <cuda_runtime.h>
 
+#include "common.cuh"
 #include "guess.cuh"
 
 namespace baorec {
@@ -36,6 +37,21 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
 
 __device__ __forceinline__ size_t vox(int n, int x, int y, int z) { return ((size_t)z * n + y) * n + x; }
 
+// K order of the m16n8k16 operands.  A lane (q = lane & 3) holds the K
+// indices 2q, 2q+1, 8+2q, 9+2q of a k-step; the sum over K does not care
+// which input channel each index stands for, as long as the A loads and the
+// weight fragments agree.  The channels are assigned so that a lane's A
+// values are contiguous in the voxel's channel vector: with 16 input channels
+// lane q holds channels 4q .. 4q+3 (one 8-byte load), with 32 or more the
+// k-steps go in pairs and lane q holds channels 32p + 8q .. 8q+7 of pair p
+// (one 16-byte load feeding two k-steps).  K index j of k-step ks is channel
+// kchan(ks, j, KS).
+__host__ __device__ __forceinline__ int kchan(int ks, int j, int KS) {
+  const int q = (j & 7) >> 1, hi = j >= 8 ? 2 : 0, e = j & 1;
+  if (KS == 1) return 4 * q + hi + e;
+  return 32 * (ks >> 1) + 8 * q + 4 * (ks & 1) + hi + e;
+}
+
 // Source voxel of output voxel (x, y, z) through tap t; false when it falls
 // in the zero padding.  For UP the tap is the output's parity (checked by the
 // caller) and (x, y, z) are the coarse coordinates.
@@ -53,8 +69,8 @@ __device__ __forceinline__ bool src_of(int t, int x, int y, int z, int n_in, int
 
 // One warp = one task: kMT*16 consecutive x of one output row (for UP: of
 // one coarse row and one output parity), all output channels.
-template <int KIND, int CIN, int COUT>
-__global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
+template <int KIND, int CIN, int COUT, int WB = kWarps>
+__global__ void __launch_bounds__(WB * 32) conv_fwd_kernel(ConvArgs a) {
   constexpr int NB = COUT / 8;
   constexpr bool K8 = CIN == 8;
   constexpr int KS = K8 ? 1 : CIN / 16;
@@ -62,7 +78,7 @@ __global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
   const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
   const int nx = KIND == UP ? a.n_in : a.n_out;   // grid the tasks walk
   const int chunks = (nx + 16 * kMT - 1) / (16 * kMT);
-  const long long task = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const long long task = (long long)blockIdx.x * WB + (threadIdx.x >> 5);
   const long long ntask = (long long)chunks * nx * nx * (KIND == UP ? 8 : 1);
   if (task >= ntask) return;
   const int cx = (int)(task % chunks);
@@ -93,26 +109,49 @@ __global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
         const bool ok = x < nx && src_of<KIND>(t, x, y, z, a.n_in, xs, ys, zs);
         rows[m][h] = ok ? reinterpret_cast<const uint32_t*>(a.in + vox(a.n_in, xs, ys, zs) * a.in_cs) : nullptr;
       }
-#pragma unroll
-    for (int ks = 0; ks < KS; ++ks) {
+    if (K8) {
       uint2 b[NB];
 #pragma unroll
-      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)(t * KS + ks) * NB + nb) * 32 + lane);
+      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
 #pragma unroll
       for (int m = 0; m < kMT; ++m) {
-        const uint32_t* p0 = rows[m][0];
-        const uint32_t* p1 = rows[m][1];
-        const int o = 8 * ks;   // 16 channels = 8 words per K step
-        const uint32_t a0 = p0 ? __ldg(p0 + o + q) : 0u;
-        const uint32_t a1 = p1 ? __ldg(p1 + o + q) : 0u;
-        if (K8) {
+        const uint32_t a0 = rows[m][0] ? __ldg(rows[m][0] + q) : 0u;
+        const uint32_t a1 = rows[m][1] ? __ldg(rows[m][1] + q) : 0u;
 #pragma unroll
-          for (int nb = 0; nb < NB; ++nb) mma8(acc[m][nb], a0, a1, b[nb].x);
-        } else {
-          const uint32_t a2 = p0 ? __ldg(p0 + o + 4 + q) : 0u;
-          const uint32_t a3 = p1 ? __ldg(p1 + o + 4 + q) : 0u;
+        for (int nb = 0; nb < NB; ++nb) mma8(acc[m][nb], a0, a1, b[nb].x);
+      }
+    } else if (KS == 1) {
+      // channels 4q .. 4q+3 of the row: (a0, a2) for row g, (a1, a3) for row g+8 (kchan)
+      uint2 b[NB];
 #pragma unroll
-          for (int nb = 0; nb < NB; ++nb) mma16(acc[m][nb], a0, a1, a2, a3, b[nb].x, b[nb].y);
+      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
+#pragma unroll
+      for (int m = 0; m < kMT; ++m) {
+        const uint2 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint2*>(rows[m][0]) + q) : make_uint2(0u, 0u);
+        const uint2 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint2*>(rows[m][1]) + q) : make_uint2(0u, 0u);
+#pragma unroll
+        for (int nb = 0; nb < NB; ++nb) mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b[nb].x, b[nb].y);
+      }
+    } else {
+      // k-steps in pairs: channels 32p + 8q .. 8q+7 of the row feed k-steps 2p and 2p+1 (kchan)
+#pragma unroll
+      for (int kp = 0; kp < KS / 2; ++kp) {
+        uint2 b0[NB], b1[NB];
+#pragma unroll
+        for (int nb = 0; nb < NB; ++nb) {
+          b0[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp) * NB + nb) * 32 + lane);
+          b1[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp + 1) * NB + nb) * 32 + lane);
+        }
+#pragma unroll
+        for (int m = 0; m < kMT; ++m) {
+          const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+          const uint4 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint4*>(rows[m][0]) + 4 * kp + q) : z4;
+          const uint4 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint4*>(rows[m][1]) + 4 * kp + q) : z4;
+#pragma unroll
+          for (int nb = 0; nb < NB; ++nb) {
+            mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b0[nb].x, b0[nb].y);
+            mma16(acc[m][nb], u0.z, u1.z, u0.w, u1.w, b1[nb].x, b1[nb].y);
+          }
         }
       }
     }
@@ -121,7 +160,7 @@ __global__ void __launch_bounds__(kWarps * 32) conv_fwd_kernel(ConvArgs a) {
   // voxels are consecutive in x, so they are staged in shared memory and
   // written as 16-byte vectors (a voxel's COUT channels are contiguous); UP
   // (its own kernel in the network) keeps per-thread stores.
-  __shared__ __align__(16) __nv_bfloat16 stile[KIND == UP ? 1 : kWarps][KIND == UP ? 8 : 16 * kMT * COUT];
+  __shared__ __align__(16) __nv_bfloat16 stile[KIND == UP ? 1 : WB][KIND == UP ? 8 : 16 * kMT * COUT];
   const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int m = 0; m < kMT; ++m)
@@ -276,10 +315,14 @@ __global__ void frag_kernel(int kind, int cin, int cout, const float* __restrict
                          : w[((size_t)t * cin + k) * cout + n];
       return __float2bfloat16(v);
     };
-    const int k0 = 16 * ks;
     uint2 f;
-    f.x = pack2(W(k0 + 2 * q), W(k0 + 2 * q + 1));
-    f.y = ci2 >= 16 ? pack2(W(k0 + 8 + 2 * q), W(k0 + 9 + 2 * q)) : 0u;
+    if (ci2 >= 16) {   // K index j of k-step ks stands for input channel kchan(ks, j, KS)
+      f.x = pack2(W(kchan(ks, 2 * q, KS)), W(kchan(ks, 2 * q + 1, KS)));
+      f.y = pack2(W(kchan(ks, 8 + 2 * q, KS)), W(kchan(ks, 9 + 2 * q, KS)));
+    } else {           // 8 input channels: m16n8k8, K index j is channel j
+      f.x = pack2(W(2 * q), W(2 * q + 1));
+      f.y = 0u;
+    }
     frag[e] = f;
   }
 }
@@ -322,18 +365,20 @@ __global__ void __launch_bounds__(kWarps * 32) up_kernel(ConvArgs a) {
       const int x = x0 + 16 * m + g + 8 * h;
       rows[m][h] = x < nx ? reinterpret_cast<const uint32_t*>(a.in + vox(nx, x, y, z) * a.in_cs) : nullptr;
     }
+  static_assert(KS % 2 == 0, "the up-sampling layers have 32 or 64 input channels: k-steps in pairs");
 #pragma unroll
   for (int ks = 0; ks < KS; ++ks) {
+    // channels 32p + 8q .. 8q+7 of the row feed k-steps 2p and 2p+1 (kchan)
     uint32_t av[2][4];
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
-      const uint32_t* p0 = rows[m][0];
-      const uint32_t* p1 = rows[m][1];
-      const int o = 8 * ks;
-      av[m][0] = p0 ? __ldg(p0 + o + q) : 0u;
-      av[m][1] = p1 ? __ldg(p1 + o + q) : 0u;
-      av[m][2] = p0 ? __ldg(p0 + o + 4 + q) : 0u;
-      av[m][3] = p1 ? __ldg(p1 + o + 4 + q) : 0u;
+      const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+      const uint4 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint4*>(rows[m][0]) + 4 * (ks >> 1) + q) : z4;
+      const uint4 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint4*>(rows[m][1]) + 4 * (ks >> 1) + q) : z4;
+      av[m][0] = (ks & 1) ? u0.z : u0.x;
+      av[m][1] = (ks & 1) ? u1.z : u1.x;
+      av[m][2] = (ks & 1) ? u0.w : u0.y;
+      av[m][3] = (ks & 1) ? u1.w : u1.y;
     }
 #pragma unroll
     for (int px = 0; px < 2; ++px) {
@@ -398,7 +443,13 @@ cudaError_t fwd_t(cudaStream_t s, const ConvArgs& a) {
   const int nx = KIND == UP ? a.n_in : a.n_out;
   const long long ntask = (long long)((nx + 16 * kMT - 1) / (16 * kMT)) * nx * nx * (KIND == UP ? 8 : 1);
   const unsigned blocks = (unsigned)((ntask + kWarps - 1) / kWarps);
-  conv_fwd_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+  if (blocks < 2u * kNumSMs) {
+    // a small grid (the network's n/4 level): blocks of 2 warps spread it over every SM
+    constexpr int kSmall = 2;
+    conv_fwd_kernel<KIND, CIN, COUT, kSmall><<<(unsigned)((ntask + kSmall - 1) / kSmall), kSmall * 32, 0, s>>>(a);
+  } else {
+    conv_fwd_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -829,7 +829,10 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->ev_red, ctx->stream));
   double sf = 0.0, sf2 = 0.0, alpha = 0.0, fn2 = 0.0;
+  bool sums_read = false;
   auto read_sums = [&]() -> int {
+    if (sums_read) return BAOREC_OK;
+    sums_read = true;
     CK(cudaEventSynchronize(ctx->ev_red));
     for (int q = 0; q < kSumBlocks; ++q) { sf += ctx->hred[2 * q]; sf2 += ctx->hred[2 * q + 1]; }
     alpha = sf / (double)N;
@@ -867,8 +870,13 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       CKLAUNCH();
       // the first FFT correction needs only r: queue it before waiting for the sums
       if (spectral && ctx->cfg.max_cycles > 0) {
-        if (learned) CKS(guess_dispatch_apply(ctx, f, L0.v));
-        else CKS(spectral_correction(ctx, L0.f, L0.v));
+        if (learned) {
+          // the network's features reuse the partial-sum buffers that still hold Σf, Σf²
+          CKS(read_sums());
+          CKS(guess_dispatch_apply(ctx, f, L0.v));
+        } else {
+          CKS(spectral_correction(ctx, L0.f, L0.v));
+        }
         speculative = true;
       }
       CKS(read_sums());
@@ -940,7 +948,11 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       // go below that inconsistency (on the 256^3 lightcone the residual
       // stalls near 1e-3 after about four corrections; fewer leave a third
       // outer step, more are wasted against the stall).
-      int m = kSpectralFirst;
+      // With one line of sight the operator is symmetric (no first-derivative
+      // term): its left null vector is constant, α = mean(f) is already the
+      // consistent shift, and S⁻¹ is its exact inverse, so the first outer
+      // step is the FFT start alone and the next one sizes itself from it.
+      int m = ctx->cfg.los_mode == BAOREC_LOS_GLOBAL ? 1 : kSpectralFirst;
       if (m_last > 0) {
         const double r = std::min(std::max(rate, kSpectralRateFloor), 0.9);
         const double want = log((double)ctx->cfg.rtol / rho) / log(r);

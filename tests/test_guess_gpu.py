@@ -172,4 +172,5 @@ def test_learned_start_is_the_fft_start_for_a_fixed_line_of_sight():
     r_fft = guess.start_residual(ctx, fd.data_ptr(), "spectral")
     r_l = guess.start_residual(ctx, fd.data_ptr(), "learned")
     print("fixed line of sight: FFT start", r_fft, "learned", r_l)
-    assert r_l == r_fft and r_fft < 1e-5
+    # the FFT start is the exact inverse here: what is left is FP32 rounding of the transforms
+    assert r_l == r_fft and r_fft < 1e-4
