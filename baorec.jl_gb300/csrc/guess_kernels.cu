@@ -97,60 +97,108 @@ __global__ void __launch_bounds__(WB * 32) conv_fwd_kernel(ConvArgs a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[m][b][e] = 0.0f;
 
-  for (int t = 0; t < T; ++t) {
-    if (KIND == UP && t != par) continue;
-    const uint32_t* rows[kMT][2];
+  // 3x3x3 layers with 32+ input and at most 32 output channels: a software
+  // pipeline over (tap, pair of k-steps) loads the next step's operands into
+  // registers while this step's MMAs run (the operand order is that of the
+  // pair branch below, see kchan)
+  constexpr bool PIPE = KIND == C3 && !K8 && KS % 2 == 0 && NB <= 4;
+  if constexpr (PIPE) {
+    constexpr int KP = KS / 2, NSTEP = 27 * KP;
+    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+    uint4 ca0[kMT], ca1[kMT], na0[kMT], na1[kMT];
+    uint2 cb0[NB], cb1[NB], nb0[NB], nb1[NB];
+    auto fetch = [&](int st, uint4(&A0)[kMT], uint4(&A1)[kMT], uint2(&B0)[NB], uint2(&B1)[NB]) {
+      const int t = st / KP, kp = st - KP * t;
 #pragma unroll
-    for (int m = 0; m < kMT; ++m)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int x = x0 + 16 * m + g + 8 * h;
-        int xs, ys, zs;
-        const bool ok = x < nx && src_of<KIND>(t, x, y, z, a.n_in, xs, ys, zs);
-        rows[m][h] = ok ? reinterpret_cast<const uint32_t*>(a.in + vox(a.n_in, xs, ys, zs) * a.in_cs) : nullptr;
+      for (int nb = 0; nb < NB; ++nb) {
+        B0[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp) * NB + nb) * 32 + lane);
+        B1[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp + 1) * NB + nb) * 32 + lane);
       }
-    if (K8) {
-      uint2 b[NB];
 #pragma unroll
-      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
+      for (int m = 0; m < kMT; ++m)
 #pragma unroll
-      for (int m = 0; m < kMT; ++m) {
-        const uint32_t a0 = rows[m][0] ? __ldg(rows[m][0] + q) : 0u;
-        const uint32_t a1 = rows[m][1] ? __ldg(rows[m][1] + q) : 0u;
+        for (int h = 0; h < 2; ++h) {
+          const int x = x0 + 16 * m + g + 8 * h;
+          int xs, ys, zs;
+          const bool ok = x < nx && src_of<C3>(t, x, y, z, a.n_in, xs, ys, zs);
+          const uint4 v =
+              ok ? __ldg(reinterpret_cast<const uint4*>(a.in + vox(a.n_in, xs, ys, zs) * a.in_cs) + 4 * kp + q) : z4;
+          if (h == 0) A0[m] = v;
+          else A1[m] = v;
+        }
+    };
+    fetch(0, ca0, ca1, cb0, cb1);
+#pragma unroll 1
+    for (int st = 0; st < NSTEP; ++st) {
+      if (st + 1 < NSTEP) fetch(st + 1, na0, na1, nb0, nb1);
 #pragma unroll
-        for (int nb = 0; nb < NB; ++nb) mma8(acc[m][nb], a0, a1, b[nb].x);
-      }
-    } else if (KS == 1) {
-      // channels 4q .. 4q+3 of the row: (a0, a2) for row g, (a1, a3) for row g+8 (kchan)
-      uint2 b[NB];
-#pragma unroll
-      for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
-#pragma unroll
-      for (int m = 0; m < kMT; ++m) {
-        const uint2 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint2*>(rows[m][0]) + q) : make_uint2(0u, 0u);
-        const uint2 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint2*>(rows[m][1]) + q) : make_uint2(0u, 0u);
-#pragma unroll
-        for (int nb = 0; nb < NB; ++nb) mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b[nb].x, b[nb].y);
-      }
-    } else {
-      // k-steps in pairs: channels 32p + 8q .. 8q+7 of the row feed k-steps 2p and 2p+1 (kchan)
-#pragma unroll
-      for (int kp = 0; kp < KS / 2; ++kp) {
-        uint2 b0[NB], b1[NB];
+      for (int m = 0; m < kMT; ++m)
 #pragma unroll
         for (int nb = 0; nb < NB; ++nb) {
-          b0[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp) * NB + nb) * 32 + lane);
-          b1[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp + 1) * NB + nb) * 32 + lane);
+          mma16(acc[m][nb], ca0[m].x, ca1[m].x, ca0[m].y, ca1[m].y, cb0[nb].x, cb0[nb].y);
+          mma16(acc[m][nb], ca0[m].z, ca1[m].z, ca0[m].w, ca1[m].w, cb1[nb].x, cb1[nb].y);
         }
 #pragma unroll
-        for (int m = 0; m < kMT; ++m) {
-          const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-          const uint4 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint4*>(rows[m][0]) + 4 * kp + q) : z4;
-          const uint4 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint4*>(rows[m][1]) + 4 * kp + q) : z4;
+      for (int m = 0; m < kMT; ++m) { ca0[m] = na0[m]; ca1[m] = na1[m]; }
 #pragma unroll
+      for (int nb = 0; nb < NB; ++nb) { cb0[nb] = nb0[nb]; cb1[nb] = nb1[nb]; }
+    }
+  } else {
+    for (int t = 0; t < T; ++t) {
+      if (KIND == UP && t != par) continue;
+      const uint32_t* rows[kMT][2];
+  #pragma unroll
+      for (int m = 0; m < kMT; ++m)
+  #pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int x = x0 + 16 * m + g + 8 * h;
+          int xs, ys, zs;
+          const bool ok = x < nx && src_of<KIND>(t, x, y, z, a.n_in, xs, ys, zs);
+          rows[m][h] = ok ? reinterpret_cast<const uint32_t*>(a.in + vox(a.n_in, xs, ys, zs) * a.in_cs) : nullptr;
+        }
+      if (K8) {
+        uint2 b[NB];
+  #pragma unroll
+        for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
+  #pragma unroll
+        for (int m = 0; m < kMT; ++m) {
+          const uint32_t a0 = rows[m][0] ? __ldg(rows[m][0] + q) : 0u;
+          const uint32_t a1 = rows[m][1] ? __ldg(rows[m][1] + q) : 0u;
+  #pragma unroll
+          for (int nb = 0; nb < NB; ++nb) mma8(acc[m][nb], a0, a1, b[nb].x);
+        }
+      } else if (KS == 1) {
+        // channels 4q .. 4q+3 of the row: (a0, a2) for row g, (a1, a3) for row g+8 (kchan)
+        uint2 b[NB];
+  #pragma unroll
+        for (int nb = 0; nb < NB; ++nb) b[nb] = __ldg(a.w + ((size_t)t * NB + nb) * 32 + lane);
+  #pragma unroll
+        for (int m = 0; m < kMT; ++m) {
+          const uint2 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint2*>(rows[m][0]) + q) : make_uint2(0u, 0u);
+          const uint2 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint2*>(rows[m][1]) + q) : make_uint2(0u, 0u);
+  #pragma unroll
+          for (int nb = 0; nb < NB; ++nb) mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b[nb].x, b[nb].y);
+        }
+      } else {
+        // k-steps in pairs: channels 32p + 8q .. 8q+7 of the row feed k-steps 2p and 2p+1 (kchan)
+  #pragma unroll
+        for (int kp = 0; kp < KS / 2; ++kp) {
+          uint2 b0[NB], b1[NB];
+  #pragma unroll
           for (int nb = 0; nb < NB; ++nb) {
-            mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b0[nb].x, b0[nb].y);
-            mma16(acc[m][nb], u0.z, u1.z, u0.w, u1.w, b1[nb].x, b1[nb].y);
+            b0[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp) * NB + nb) * 32 + lane);
+            b1[nb] = __ldg(a.w + ((size_t)(t * KS + 2 * kp + 1) * NB + nb) * 32 + lane);
+          }
+  #pragma unroll
+          for (int m = 0; m < kMT; ++m) {
+            const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+            const uint4 u0 = rows[m][0] ? __ldg(reinterpret_cast<const uint4*>(rows[m][0]) + 4 * kp + q) : z4;
+            const uint4 u1 = rows[m][1] ? __ldg(reinterpret_cast<const uint4*>(rows[m][1]) + 4 * kp + q) : z4;
+  #pragma unroll
+            for (int nb = 0; nb < NB; ++nb) {
+              mma16(acc[m][nb], u0.x, u1.x, u0.y, u1.y, b0[nb].x, b0[nb].y);
+              mma16(acc[m][nb], u0.z, u1.z, u0.w, u1.w, b1[nb].x, b1[nb].y);
+            }
           }
         }
       }
