@@ -870,12 +870,27 @@ def run_gb300(args):
                        "frac": ach / peak, "peak_source": peak_src,
                        "traffic": traffic_per_launch(names[which].split()[0], N),
                        "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
+    # every form of the FP32 running residual (tune.pairs 0-3), timed the same way; the tuner's choice restored
+    if meas:
+        forms = {}
+        chosen = ctx.lib.baorec_tune_pairs(ctx.h)
+        for form in (0, 1, 2, 3):
+            ctx.call("baorec_set_tune_pairs", form)
+            avg, nbytes = C.c_float(), C.c_double()
+            ctx.call("baorec_profile_kernel", 3, 30, C.byref(avg), C.byref(nbytes))
+            forms[{0: "one cell per thread", 1: "two cells per thread", 2: "pairs streamed in z, 16-plane blocks",
+                   3: "pairs streamed in z, 32-plane blocks"}[form]] = {
+                "avg_launch_ms": avg.value, "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
+        ctx.call("baorec_set_tune_pairs", chosen)
+        meas["pair_forms"] = forms
     head = 0 if args.start == "zero" else (5 if tune.get("stream_residuals", -1) != 0 else 3)
     roofline, aux = None, {}
     if meas:
         roofline = dict(meas[head])
         roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
-        aux = {names[w]: meas[w] for w in meas if w != head}
+        aux = {names[w]: meas[w] for w in meas if w != head and w != "pair_forms"}
+        if "pair_forms" in meas:
+            aux["resid_pairs forms"] = meas["pair_forms"]
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
