@@ -68,7 +68,7 @@ inline size_t frag_count(int kind, int cin, int cout) {
   X(C3, 8, 16) X(C3, 16, 16) X(C3, 32, 32) X(C3, 64, 64) X(C3, 64, 32) X(C3, 32, 16) X(C3, 16, 32) \
   X(C3, 32, 64) X(DN, 16, 32) X(DN, 32, 64) X(UP, 64, 32) X(UP, 32, 16)
 
-// C3 shapes with a tcgen05 kernel (guess_tc.cu); grids with n % 128 == 0
+// C3 shapes with a tcgen05 kernel (guess_tc.cu); grids with n % 128 == 0 or n == 64
 #define BAOREC_GUESS_TC_SHAPES(X) X(8, 16) X(16, 16) X(32, 32) X(32, 16) X(16, 32) X(32, 64) X(64, 32)
 
 // BF16 entries of a tcgen05 weight image: one 16-wide K step per MMA of a

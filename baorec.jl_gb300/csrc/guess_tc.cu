@@ -319,7 +319,7 @@ struct Unit {
 
 // unit u = (x segment, group of yr rows, column of zc z planes), x fastest
 __device__ __forceinline__ Unit unit_of(long long u, int n, int zc, int yr) {
-  const int xsegs = n / kTM, ny = n / yr;
+  const int xsegs = (n + kTM - 1) / kTM, ny = n / yr;
   Unit t;
   t.x0 = (int)(u % xsegs) * kTM;
   const long long r = u / xsegs;
@@ -382,7 +382,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = a.n, zc = a.zc;
   constexpr int YR = P::YR;
-  const long long nunits = (long long)(n / kTM) * (n / YR) * (n / zc);
+  // a 64-voxel row is one tile whose upper half reads the TMA fill (zeros) and is not stored
+  const long long nunits = (long long)((n + kTM - 1) / kTM) * (n / YR) * (n / zc);
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
@@ -595,12 +596,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
 #pragma unroll
             for (int c = 0; c < COUT; c += 16) tmem_zero16(sh + (uint32_t)c);
           }
-          const size_t vo = ((size_t)(t.z0 + zl) * n + (t.y + yy)) * n + (t.x0 + m);
+          const bool inside = t.x0 + m < n;   // false only for the unused half of a 64-voxel row
+          const size_t vo = ((size_t)(t.z0 + zl) * n + (t.y + yy)) * n + (inside ? t.x0 + m : 0);
           if (a.bias) {
 #pragma unroll
             for (int c = 0; c < COUT; ++c) v[c] += __ldg(a.bias + c);
           }
-          if (a.add) {
+          if (a.add && inside) {
             const uint4* ap = reinterpret_cast<const uint4*>(a.add + vo * a.add_cs);
 #pragma unroll
             for (int g = 0; g < COUT / 8; ++g) {
@@ -621,7 +623,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           uint4* op = reinterpret_cast<uint4*>(a.out + vo * a.out_cs);
 #pragma unroll
           for (int g = 0; g < COUT / 8; ++g)
-            op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
+            if (inside)
+              op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
                                pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
         }
         tmem_wait_st();
@@ -763,12 +766,12 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
   long long best_rows = 0;
   for (int zc = 16; zc >= 4; zc /= 2) {
     if (n % zc) continue;
-    const long long units = (long long)(n / kTM) * (n / P::YR) * (n / zc);
+    const long long units = (long long)((n + kTM - 1) / kTM) * (n / P::YR) * (n / zc);
     const long long rows = ((units + ctas - 1) / ctas) * (zc + 2);   // slab loads of the busiest CTA
     if (!best || rows < best_rows) { best = zc; best_rows = rows; }
   }
   a.zc = best;
-  const long long units = (long long)(n / kTM) * (n / P::YR) * (n / best);
+  const long long units = (long long)((n + kTM - 1) / kTM) * (n / P::YR) * (n / best);
   const unsigned grid = (unsigned)(units < ctas ? units : ctas);
   conv_tc_kernel<CIN, COUT, LOADER><<<grid, kThreads, P::SMEM, s>>>(map, a);
   return cudaGetLastError();
@@ -777,7 +780,9 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
 }  // namespace
 
 bool tc_supported(int kind, int cin, int cout, int n) {
-  if (kind != C3 || n < kTM || n % kTM || n % 4) return false;
+  // rows of 128k voxels, or a 64-voxel row as one half-used tile (the n/2
+  // level of a 128^3 network)
+  if (kind != C3 || !(n % kTM == 0 || n == kTM / 2)) return false;
 #define X(I, O) if (cin == I && cout == O) return true;
   BAOREC_GUESS_TC_SHAPES(X)
 #undef X

@@ -430,8 +430,8 @@ int baorec_guess_train(baorec_ctx* ctx, const baorec_guess_train_config* tc, flo
 /* Convolution kernels of the network: tensor_core 1 (default) runs the 3x3x3
  * layers whose shape has one on the tcgen05 kernel (TMA-staged operands, TMEM
  * accumulators; the 3x3x3 shapes 8->16, 16->16, 16->32, 32->16, 32->32,
- * 32->64, 64->32 on grids with n % 128 == 0), 0 runs every layer on the
- * mma.sync kernels. */
+ * 32->64, 64->32 on grids with n % 128 == 0 or n == 64), 0 runs every
+ * layer on the mma.sync kernels. */
 int baorec_guess_set_conv_path(baorec_ctx* ctx, int32_t tensor_core);
 /* Convolutions of the last network forward that ran on tcgen05 (-1: no network). */
 int32_t baorec_guess_tc_layers(baorec_ctx* ctx);

@@ -64,16 +64,18 @@ def _conv_ref(xf, w, bias, add, relu, z, y, x):
     return out
 
 
+@pytest.mark.parametrize("n", [128, 64])
 @pytest.mark.parametrize("cin,cout", TC_SHAPES)
-def test_conv3_tcgen05_matches_fp64_and_mma(cin, cout):
-    """Every covered shape at n = 128, both slab loaders: the tcgen05 output
-    equals the FP64 convolution of the same BF16 operands to BF16 output
-    rounding, and the mma.sync kernel's output to within one BF16 step (the
-    two differ only in the FP32 summation order)."""
+def test_conv3_tcgen05_matches_fp64_and_mma(cin, cout, n):
+    """Every covered shape at n = 128 (one full tile per row) and n = 64 (one
+    half-used tile per row: the upper 64 slots read the TMA zero fill and are
+    not stored), both slab loaders: the tcgen05 output equals the FP64
+    convolution of the same BF16 operands to BF16 output rounding, and the
+    mma.sync kernel's output to within one BF16 step (the two differ only in
+    the FP32 summation order)."""
     import torch
     from baorec import guess
-    n = 128
-    rng = np.random.default_rng(cin * 100 + cout)
+    rng = np.random.default_rng(cin * 100 + cout + n)
     ctx = _ctx(n)
     xb = _bf16(rng.normal(size=(n, n, n, cin)))
     wq = _bf16(rng.normal(scale=1.0 / np.sqrt(27 * cin), size=(27, cin, cout))).to(torch.float32)
@@ -129,25 +131,28 @@ def test_conv3_tcgen05_rejects_uncovered():
     silent fallback."""
     import torch
     from baorec import _lib, guess
-    ctx = _ctx(64)
-    x = torch.zeros((64, 64, 64, 16), dtype=torch.bfloat16, device="cuda")
+    ctx = _ctx(96)
+    x = torch.zeros((96, 96, 96, 16), dtype=torch.bfloat16, device="cuda")
     w = torch.zeros((27, 16, 16), device="cuda")
     with pytest.raises(_lib.BaorecError):
-        guess.conv3(ctx, x, w, path="tcgen05")       # n = 64 is not a multiple of 128
+        guess.conv3(ctx, x, w, path="tcgen05")       # n = 96: neither a multiple of 128 nor 64
+    ctx = _ctx(128)
     x = torch.zeros((128, 128, 128, 64), dtype=torch.bfloat16, device="cuda")
     w = torch.zeros((27, 64, 64), device="cuda")
     with pytest.raises(_lib.BaorecError):
         guess.conv3(ctx, x, w, path="tcgen05")       # 64 -> 64 channels: mma.sync only
 
 
-def test_network_tcgen05_matches_mma_forward_and_gradients():
-    """The whole network at n = 256 with the trained weights: output and
-    parameter gradients with the tcgen05 layers on and off agree to the BF16
-    noise of the activations; the forward ran the eight covered layers (four
-    at 256^3, four at 128^3) on tcgen05."""
+@pytest.mark.parametrize("n", [256, 128])
+def test_network_tcgen05_matches_mma_forward_and_gradients(n):
+    """The whole network with the trained weights at n = 256 and at n = 128
+    (the size it runs at on the first restriction of a 256^3 mesh): output
+    and parameter gradients with the tcgen05 layers on and off agree to the
+    BF16 noise of the activations; the forward ran the eight covered layers
+    (four at n^3, four at (n/2)^3; the 64->64 layers at (n/4)^3 have no
+    tcgen05 kernel) on tcgen05."""
     import torch
     from baorec import guess
-    n = 256
     ctx = _ctx(n)
     p = guess.load_params(guess.os.path.join(guess.WEIGHTS_DIR, "guess_lightcone.npy"))
     guess.set_params(ctx, p)
