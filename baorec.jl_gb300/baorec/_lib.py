@@ -136,6 +136,8 @@ _SIGS = {
     "baorec_set_tune_stream": (C.c_int, [P, C.c_int]),
     "baorec_tune_pairs": (C.c_int, [P]),
     "baorec_set_tune_pairs": (C.c_int, [P, C.c_int]),
+    "baorec_tune_acc": (C.c_int, [P]),
+    "baorec_set_tune_acc": (C.c_int, [P, C.c_int]),
     "baorec_tune_zpass": (C.c_int, [P]),
     "baorec_set_tune_zpass": (C.c_int, [P, C.c_int]),
     "baorec_tune_xy": (C.c_int, [P]),
@@ -277,6 +279,7 @@ class Context:
         return {"paint_tile": pt.value, "tile16_per_level": list(bt),
                 "stream_residuals": int(self.lib.baorec_tune_stream(self.h)),
                 "pair_residual": int(self.lib.baorec_tune_pairs(self.h)),
+                "acc_residual": int(self.lib.baorec_tune_acc(self.h)),
                 "fft_zpass": int(self.lib.baorec_tune_zpass(self.h)),
                 "fft_xy_fused": int(self.lib.baorec_tune_xy(self.h))}
 

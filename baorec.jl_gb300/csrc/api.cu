@@ -52,7 +52,7 @@ int finish(baorec_ctx* ctx, uint32_t flags) {
     if (e & kErrOOB)
       return set_error(ctx, BAOREC_ERR_OOB, "particle outside the mesh (the reference raises BoundsError)");
     if (e & kErrTimeout)
-      return set_error(ctx, BAOREC_ERR_CUDA, "a device-side wait timed out (tensor-core convolution pipeline)");
+      return set_error(ctx, BAOREC_ERR_CUDA, "a device-side wait timed out (TMA-fed pipeline)");
   }
   return BAOREC_OK;
 }

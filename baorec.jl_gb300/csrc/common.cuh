@@ -106,7 +106,8 @@ struct baorec_ctx {
   struct Tune {                        // launch shapes (defaults, or chosen by baorec_autotune)
     int paint_tile = 8;                // tile edge of the deterministic paint
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming
-    int pairs = 1;                     // running residual on 32x16x16 tiles: 1 packed z-pairs, 0 one cell per thread
+    int pairs = 1;                     // form of the FP32 running residual (baorec_set_tune_pairs)
+    int acc = 0;                       // form of the accurate residual (baorec_set_tune_acc)
     int zpass = 1;                     // FFT preconditioner: 1 (2: capped registers) xy transforms + fused z pass where n3 = 256, 0 3-D transforms
     int xy = 0;                        // xy transforms of the z-pass paths: 0 cuFFT, 1 fused kernels (256 x 256 planes)
     int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1

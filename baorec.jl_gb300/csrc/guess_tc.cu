@@ -63,10 +63,13 @@
 
 #include "common.cuh"
 #include "guess.cuh"
+#include "tma_util.cuh"
 
 namespace baorec {
 namespace guess {
 namespace {
+
+using namespace ::baorec::tma;
 
 typedef __nv_bfloat16 bf16;
 
@@ -80,8 +83,6 @@ constexpr int kThreads = 32 * (kEpiWarp0 + 8);
 enum Loader { kLoadCpAsync = 0, kLoadTma = 1 };
 constexpr int kSmemMax = 232448;         // opt-in dynamic shared memory per block
 constexpr int kSmemBudget = kSmemMax - 1024 - 512;
-constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait
-constexpr uint32_t kSuspendNs = 20000;   // suspend hint of one try_wait
 constexpr int kRing = 6;                 // TMEM accumulators (output rows in flight) per output-row ring
 constexpr int kShadow = 2;               // shadow slots past a ring's end: the MMA never wraps
 constexpr int kCols = kRing + kShadow;   // slots of TMEM columns per ring
@@ -140,81 +141,6 @@ struct TcArgs {
 
 // ---- PTX wrappers -----------------------------------------------------------
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t gtimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// try_wait that may suspend the thread in hardware (up to the hint) until
-// the phase completes, leaving the issue slots to the other warps
-__device__ __forceinline__ bool mbar_try_suspend(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity), "r"(kSuspendNs)
-      : "memory");
-  return ok != 0;
-}
-
-// Wait for the phase of the given parity; false after limit_ns or when
-// another role has given up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                          unsigned long long limit_ns) {
-  if (mbar_try(bar, parity)) return true;
-  const uint64_t t0 = gtimer();
-  for (;;) {
-    if (mbar_try_suspend(bar, parity)) return true;
-    if (*abort_flag || gtimer() - t0 > limit_ns) return false;
-  }
-}
-
-// Wait for copies or MMAs this block has issued before it frees their
-// shared memory or TMEM: not cut short when another role gives up, bounded
-// by kWaitNs whatever the pipeline's own limit.
-__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
-  if (mbar_try(bar, parity)) return true;
-  const uint64_t t0 = gtimer();
-  for (;;) {
-    if (mbar_try_suspend(bar, parity)) return true;
-    if (gtimer() - t0 > kWaitNs) return false;
-  }
-}
-
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
-                                            int c2, int c3) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], "
-      "[%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
-      : "memory");
-}
-
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
@@ -230,8 +156,6 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
-// generic-proxy writes of this thread -> visible to the tensor core's async proxy
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // shared-memory matrix descriptor: no swizzle, fixed field 0b001 at bit 46
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -397,7 +321,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       mbar_init(smem_u32(&bar_accf[b]), 1);
       mbar_init(smem_u32(&bar_acce[b]), 128);
     }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
   }
   // the 32-byte pad after each chunk of a slab is never loaded; an 8-channel
   // MMA reads it (times zero weights), so it must hold finite values
@@ -683,23 +607,6 @@ __global__ void image_kernel(int cin, int cout, const float* __restrict__ w, bf1
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  }
-  return fn;
-}
 
 // Input activations as a 4-D tensor {channels, x, y, z} (channels fastest,
 // voxel pitch in_cs elements); box {8, 130, yr + 2, 1}.

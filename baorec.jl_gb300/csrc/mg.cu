@@ -372,6 +372,8 @@ LG level_geom(const baorec_ctx* ctx, int l, float clamp) {
   G.clamp = clamp;
   G.tile16 = l < 16 ? ctx->tune.big_tiles[l] : -1;
   G.pairs = ctx->tune.pairs;
+  G.accf = ctx->tune.acc;
+  G.err = ctx->derr;
   return G;
 }
 

@@ -16,7 +16,9 @@ struct LG {                           // level geometry passed to kernels
   int local;
   float clamp;                        // > 0: clamp derivative coefficients
   int tile16;                         // tile kernels: -1 heuristic, 0 = 32x8x8, 1 = 32x16x16 tiles
-  int pairs;                          // running residual on 32x16x16 tiles: 1 = two z-cells per thread, packed
+  int pairs;                          // form of the running residual (0-5, see baorec_set_tune_pairs)
+  int accf = 0;                       // accurate residual: 0 512-thread blocks, 1 / 2 256-thread blocks (32x8x8 / 32x8x16)
+  unsigned* err = nullptr;            // device error word of the context (bounded waits report here)
 };
 
 struct Coef {
@@ -147,6 +149,48 @@ cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, c
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts,
                              const float* ed = nullptr);
 int tile_blocks(const LG& G);
+// ---- packed FP32x2 arithmetic: two cells per instruction ---------------------
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 P2(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void U2(f2 r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ f2 B2(float a) { return P2(a, a); }
+#define BAOREC_F2OP(name, op)                                                 \
+  __device__ __forceinline__ f2 name(f2 a, f2 b) {                            \
+    f2 d;                                                                     \
+    asm(op ".rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));               \
+    return d;                                                                 \
+  }
+BAOREC_F2OP(add2, "add")
+BAOREC_F2OP(sub2, "sub")
+BAOREC_F2OP(mul2, "mul")
+#undef BAOREC_F2OP
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 rcp2(f2 a) {
+  float x, y;
+  U2(a, x, y);
+  return P2(__frcp_rn(x), __frcp_rn(y));
+}
+
+// c_x^2 p_x^2 + c_y^2 p_y^2 of the fast coefficients, in one fixed rounding
+// order (no contraction), so that the running-residual forms that pair
+// cells differently produce the same bits.
+__device__ __forceinline__ float coef_dxy(const LG& G, float px2, float py2) {
+  return __fadd_rn(__fmul_rn(G.cell2[0], px2), __fmul_rn(G.cell2[1], py2));
+}
+
+// the running residual with TMA-staged operands, blocks of tz planes (mg_tma.cu)
+bool resid_tma_ok(const LG& G, int tz);
+cudaError_t launch_resid_diff_tma(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
+                                  float* acc, int tz);
+
 // streaming (2.5-D, cp.async-pipelined) forms of the finest-level residuals (mg_stream.cu)
 bool stream_ok(const int n[3]);
 int stream_blocks(const int n[3]);

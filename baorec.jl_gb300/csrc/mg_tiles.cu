@@ -27,19 +27,19 @@ constexpr int CH = WX / 4;                         // 16-byte chunks per window 
 // cells, no wrap) is read through a ring of PF registers filled PF rows
 // ahead, so those loads overlap the window loads and the stencil work
 // instead of stalling the row that consumes them.
-template <int TY, int TZ>
+template <int TY, int TZ, int NW = NWARP>
 struct RowPrefetch {
-  static constexpr int RPW = (TY * TZ + NWARP - 1) / NWARP;   // rows per warp
+  static constexpr int RPW = (TY * TZ + NW - 1) / NW;   // rows per warp
   static constexpr int PF = RPW < 4 ? RPW : 4;
   float v[PF];
   __device__ __forceinline__ static int offset(int i, int warp, int lane, int x0, int y0, int z0, const int* n) {
-    const int row = warp + i * NWARP;
+    const int row = warp + i * NW;
     const int ly = row % TY, lz = row / TY;
     return ((z0 + lz) * n[1] + (y0 + ly)) * n[0] + x0 + lane;
   }
   __device__ __forceinline__ void issue(int i, const float* __restrict__ src, int warp, int lane, int x0, int y0,
                                         int z0, const int* n) {
-    if (i < RPW && warp + i * NWARP < TY * TZ) v[i % PF] = __ldg(src + offset(i, warp, lane, x0, y0, z0, n));
+    if (i < RPW && warp + i * NW < TY * TZ) v[i % PF] = __ldg(src + offset(i, warp, lane, x0, y0, z0, n));
   }
 };
 
@@ -47,10 +47,10 @@ __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >
 
 // Row offsets (ix = 0 of the row) of the periodic window rows
 // y in [y0-HY, y0+TY+HY), z in [z0-HY, z0+TZ+HY).
-template <int HY, int TY, int TZ>
+template <int HY, int TY, int TZ, int NTB = NT>
 __device__ __forceinline__ void row_table(int* __restrict__ ro, int y0, int z0, const int n[3]) {
   constexpr int SY = TY + 2 * HY, SZ = TZ + 2 * HY;
-  for (int r = threadIdx.x; r < SY * SZ; r += NT) {
+  for (int r = threadIdx.x; r < SY * SZ; r += NTB) {
     const int ly = r % SY, lz = r / SY;
     ro[r] = n[0] * (wrapi(y0 - HY + ly, n[1]) + n[1] * wrapi(z0 - HY + lz, n[2]));
   }
@@ -79,11 +79,11 @@ __device__ __forceinline__ void load_rows(float* __restrict__ s, const int* __re
   }
 }
 
-template <int HY, int TY, int TZ>
+template <int HY, int TY, int TZ, int NTB = NT>
 __device__ __forceinline__ void load_ptab(float* __restrict__ sp, const LG& G, int x0, int y0, int z0) {
-  for (int q = threadIdx.x; q < WX; q += NT) sp[q] = G.P[0][wrapi(x0 - XH + q, G.n[0])];
-  for (int q = threadIdx.x; q < TY + 2 * HY; q += NT) sp[WX + q] = G.P[1][wrapi(y0 - HY + q, G.n[1])];
-  for (int q = threadIdx.x; q < TZ + 2 * HY; q += NT) sp[2 * WX + q] = G.P[2][wrapi(z0 - HY + q, G.n[2])];
+  for (int q = threadIdx.x; q < WX; q += NTB) sp[q] = G.P[0][wrapi(x0 - XH + q, G.n[0])];
+  for (int q = threadIdx.x; q < TY + 2 * HY; q += NTB) sp[WX + q] = G.P[1][wrapi(y0 - HY + q, G.n[1])];
+  for (int q = threadIdx.x; q < TZ + 2 * HY; q += NTB) sp[2 * WX + q] = G.P[2][wrapi(z0 - HY + q, G.n[2])];
 }
 
 // Operator coefficients of one cell (approximate division: smoother and
@@ -194,36 +194,6 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
   }
 }
 
-// ---- packed FP32x2 arithmetic: two cells per instruction ---------------------
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 P2(float a, float b) {
-  f2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void U2(f2 r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
-__device__ __forceinline__ f2 B2(float a) { return P2(a, a); }
-#define BAOREC_F2OP(name, op)                                                 \
-  __device__ __forceinline__ f2 name(f2 a, f2 b) {                            \
-    f2 d;                                                                     \
-    asm(op ".rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));               \
-    return d;                                                                 \
-  }
-BAOREC_F2OP(add2, "add")
-BAOREC_F2OP(sub2, "sub")
-BAOREC_F2OP(mul2, "mul")
-#undef BAOREC_F2OP
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-  f2 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2 rcp2(f2 a) {
-  float x, y;
-  U2(a, x, y);
-  return P2(__frcp_rn(x), __frcp_rn(y));
-}
-
 // Gauss-Seidel values of two cells (shared indices qa, qb) that share p_y:
 // (rhs + neighbours) / diagonal, clamped operator, fast reciprocals.
 template <bool LOCAL, bool CLAMP, int SXY>
@@ -329,7 +299,7 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
       qa[k] = lxa + WX * ly + SXY * lza;
       qb[k] = lxb + WX * ly + SXY * lzb;
       const f2 Px = P2(ea ? pxe : pxo, ea ? pxo : pxe);
-      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : 0;
+      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : B2(0.0f);
       const float py = LOCAL ? sp[WX + ly] : 0.0f;
       const f2 fr = sub2(P2(__ldg(rhs + ro[ly + SY * lza] + (ea ? gxe : gxo)),
                             __ldg(rhs + ro[ly + SY * lzb] + (ea ? gxo : gxe))), sh2);
@@ -360,7 +330,7 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
       const int lx = 4 + ((ly + lza + 1) & 1) + 2 * (int)tb;
       qc[k] = lx + WX * ly + SXY * lza;
       const float px = LOCAL ? sp[lx] : 0.0f, py = LOCAL ? sp[WX + ly] : 0.0f;
-      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : 0;
+      const f2 Pz = LOCAL ? P2(sp[2 * WX + lza], sp[2 * WX + lzb]) : B2(0.0f);
       const int gx = x0 - XH + lx;
       const f2 fr = sub2(P2(__ldg(rhs + ro[ly + SY * lza] + gx), __ldg(rhs + ro[ly + SY * lzb] + gx)), sh2);
       nb[k] = gs_two<LOCAL, CLAMP, SXY>(sv, qc[k], qc[k] + HB * SXY, fr, B2(px), py, Pz, cu, G);
@@ -397,16 +367,17 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
 // hold every value of both stencils: the z-1 and z+1 values of (A, B) are
 // the pairs themselves, the in-plane values one register move from a pair.
 // Warp w computes window row y = 1 + w, lane l column x = XH + l.
-template <bool LOCAL>
-__global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restrict__ e, const float* __restrict__ rhs,
-                                                          float* __restrict__ r, LG G, float shift,
-                                                          float* __restrict__ acc) {
-  constexpr int TY = 16, TZ = 16, SY = TY + 2, SZ = TZ + 2;
+template <bool LOCAL, int TY>
+__global__ void __launch_bounds__(32 * TY, 32 / TY) resid_pairs_kernel(const float* __restrict__ e,
+                                                                     const float* __restrict__ rhs,
+                                                                     float* __restrict__ r, LG G, float shift,
+                                                                     float* __restrict__ acc) {
+  constexpr int NTH = 32 * TY;       // one warp per output row
+  constexpr int TZ = 16, SY = TY + 2, SZ = TZ + 2;
   constexpr int NPR = SZ / 2;        // plane pairs in the window
   constexpr int PR = 2 * WX;         // floats per row of a plane pair
   constexpr int PP = SY * PR;        // floats per plane pair
   constexpr int NK = TZ / 2;         // output pairs per thread
-  static_assert(NWARP == TY, "one warp per output row");
   extern __shared__ __align__(16) float smem[];
   float* sw = smem;
   int* ro = reinterpret_cast<int*>(sw + NPR * PP);
@@ -429,18 +400,18 @@ __global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restr
   };
   issue(0, r0, a0);
   issue(1, r1, a1);
-  row_table<1, TY, TZ>(ro, y0, z0, G.n);
-  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  row_table<1, TY, TZ, NTH>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<1, TY, TZ, NTH>(sp, G, x0, y0, z0);
   __syncthreads();
   {
     constexpr int TOT = NPR * SY * CH;
-    constexpr int K = (TOT + NT - 1) / NT, B = K;   // every chunk of the thread in flight at once
+    constexpr int K = (TOT + NTH - 1) / NTH, B = K;   // every chunk of the thread in flight at once
 #pragma unroll
     for (int k0 = 0; k0 < K; k0 += B) {
       float4 a[B], b[B];
 #pragma unroll
       for (int i = 0; i < B; ++i) {
-        const int t = threadIdx.x + (k0 + i) * NT;
+        const int t = threadIdx.x + (k0 + i) * NTH;
         if (k0 + i < K && t < TOT) {
           const int row = t / CH, c = t - CH * row;   // row = pair * SY + y
           const int j = row / SY, yy = row - SY * j;
@@ -451,7 +422,7 @@ __global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restr
       }
 #pragma unroll
       for (int i = 0; i < B; ++i) {
-        const int t = threadIdx.x + (k0 + i) * NT;
+        const int t = threadIdx.x + (k0 + i) * NTH;
         if (k0 + i < K && t < TOT) {
           const int row = t / CH, c = t - CH * row;
           float4* d = reinterpret_cast<float4*>(sw + row * PR + 8 * c);
@@ -464,7 +435,7 @@ __global__ void __launch_bounds__(NT, 2) resid_pairs_kernel(const float* __restr
   __syncthreads();
   const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1];
   const float px2 = px * px, py2 = py * py;
-  const float dxy = G.cell2[0] * px2 + G.cell2[1] * py2;
+  const float dxy = coef_dxy(G, px2, py2);
   auto L = [&](int q) { return *reinterpret_cast<const f2*>(sw + q); };
   // (second plane of pair a, first plane of pair b): the in-plane values of (A, B)
   auto C = [](f2 a, f2 b) {
@@ -604,7 +575,7 @@ __global__ void __launch_bounds__(NT, 2) resid_pairz_kernel(const float* __restr
   __syncthreads();
   const float px = LOCAL ? sp[lx] : G.pg[0], py = LOCAL ? sp[WX + ly] : G.pg[1];
   const float px2 = px * px, py2 = py * py;
-  const float dxy = G.cell2[0] * px2 + G.cell2[1] * py2;
+  const float dxy = coef_dxy(G, px2, py2);
   auto L = [&](int q) { return *reinterpret_cast<const f2*>(sw + q); };
   auto C = [](f2 a, f2 b) {
     float a0, a1, b0, b1;
@@ -672,8 +643,8 @@ __global__ void __launch_bounds__(NT, 2) resid_pairz_kernel(const float* __restr
 // operations in the reference's order.  Per-block (Σr, Σr²) to part.  The
 // solution pair is (hi, lo) + ec first; with HASD the correction is ec + ed,
 // added in FP32 as a separate e += d pass would.
-template <bool LOCAL, int TY, int TZ, bool HASD>
-__global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
+template <bool LOCAL, int TY, int TZ, bool HASD, int NTH = NT>
+__global__ void __launch_bounds__(NTH, 1024 / NTH) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
                                                         const float* __restrict__ ec, const float* __restrict__ ed,
                                                         const float* __restrict__ f,
                                                         float* __restrict__ ohi, float* __restrict__ olo,
@@ -686,22 +657,23 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
   float* sp = reinterpret_cast<float*>(ro + SY * SZ);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  using RP = RowPrefetch<TY, TZ>;
+  constexpr int NW = NTH / 32;
+  using RP = RowPrefetch<TY, TZ, NW>;
   RP pf;
 #pragma unroll
   for (int i = 0; i < RP::PF; ++i) pf.issue(i, f, warp, lane, x0, y0, z0, G.n);
-  row_table<1, TY, TZ>(ro, y0, z0, G.n);
-  if (LOCAL) load_ptab<1, TY, TZ>(sp, G, x0, y0, z0);
+  row_table<1, TY, TZ, NTH>(ro, y0, z0, G.n);
+  if (LOCAL) load_ptab<1, TY, TZ, NTH>(sp, G, x0, y0, z0);
   __syncthreads();
   {
     float4* sw4 = reinterpret_cast<float4*>(smem);
-    constexpr int TOT = SY * SZ * CH, K = (TOT + NT - 1) / NT, B = HASD ? 3 : 4;
+    constexpr int TOT = SY * SZ * CH, K = (TOT + NTH - 1) / NTH, B = HASD ? 3 : 4;
 #pragma unroll
     for (int k0 = 0; k0 < K; k0 += B) {
       float4 h[B], l[B], e[B], d[B];
 #pragma unroll
       for (int b = 0; b < B; ++b) {
-        const int t = threadIdx.x + (k0 + b) * NT;
+        const int t = threadIdx.x + (k0 + b) * NTH;
         if (k0 + b < K && t < TOT) {
           const int row = t / CH, c = t - CH * row;
           const int o = ro[row] + wrapi(x0 - XH + 4 * c, G.n[0]);
@@ -713,7 +685,7 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
       }
 #pragma unroll
       for (int b = 0; b < B; ++b) {
-        const int t = threadIdx.x + (k0 + b) * NT;
+        const int t = threadIdx.x + (k0 + b) * NTH;
         if (k0 + b < K && t < TOT) {
           if (HASD) {
             e[b].x = e[b].x + d[b].x;
@@ -738,7 +710,7 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
   constexpr int SX = WX;
 #pragma unroll
   for (int i = 0; i < RP::RPW; ++i) {
-    const int row = warp + i * NWARP;
+    const int row = warp + i * NW;
     if (row >= TY * TZ) break;
     const float fv = pf.v[i % RP::PF];
     pf.issue(i + RP::PF, f, warp, lane, x0, y0, z0, G.n);
@@ -781,12 +753,12 @@ __global__ void __launch_bounds__(NT, 2) resid_acc2_kernel(const float* __restri
     s1 += __shfl_xor_sync(0xffffffffu, s1, o);
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
-  __shared__ double red[2][NWARP];
+  __shared__ double red[2][NW];
   if (lane == 0) { red[0][warp] = s1; red[1][warp] = s2; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0.0, b = 0.0;
-    for (int k = 0; k < NWARP; ++k) { a += red[0][k]; b += red[1][k]; }
+    for (int k = 0; k < NW; ++k) { a += red[0][k]; b += red[1][k]; }
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     part[2 * bid] = a;
     part[2 * bid + 1] = b;
@@ -860,24 +832,24 @@ cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   return cudaGetLastError();
 }
 
-template <bool LOCAL>
+template <bool LOCAL, int TY = 16>
 cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
-  auto k = resid_pairs_kernel<LOCAL>;
-  constexpr size_t b = win_bytes<1, 16, 16>(1);
+  auto k = resid_pairs_kernel<LOCAL, TY>;
+  constexpr size_t b = win_bytes<1, TY, 16>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<16, 16>(G.n), NT, b, s>>>(ec, rhs, r, G, 0.0f, acc);
+  k<<<grid_of<TY, 16>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, 0.0f, acc);
   return cudaGetLastError();
 }
 
-template <bool LOCAL, int TY, int TZ>
+template <bool LOCAL, int TY, int TZ, int NTH = NT>
 cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* ed, const float* f,
                   float* ohi, float* olo, float* r, const LG& G, float alpha, double* part) {
-  auto k = (ed && ec) ? resid_acc2_kernel<LOCAL, TY, TZ, true> : resid_acc2_kernel<LOCAL, TY, TZ, false>;
+  auto k = (ed && ec) ? resid_acc2_kernel<LOCAL, TY, TZ, true, NTH> : resid_acc2_kernel<LOCAL, TY, TZ, false, NTH>;
   constexpr size_t b = win_bytes<1, TY, TZ>(2);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
+  k<<<grid_of<TY, TZ>(G.n), NTH, b, s>>>(hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
   return cudaGetLastError();
 }
 
@@ -885,8 +857,20 @@ cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float*
 
 bool tile_ok(const int n[3]) { return n[0] % TX == 0 && n[1] % 8 == 0 && n[2] % 8 == 0; }
 
+// accurate residual: 32 x 8 x 16 tiles of 256 threads (form 2), 32 x 8 x 8
+// tiles of 256 threads (form 1), else the level's tiles with 512 threads
+static int acc_form(const LG& G) {
+  const int* n = G.n;
+  if (G.accf == 2 && n[1] % 8 == 0 && n[2] % 16 == 0) return 2;
+  if (G.accf == 1 && n[1] % 8 == 0 && n[2] % 8 == 0) return 1;
+  return 0;
+}
+
 int tile_blocks(const LG& G) {
   const int* n = G.n;
+  const int f = acc_form(G);
+  if (f == 2) return (n[0] / TX) * (n[1] / 8) * (n[2] / 16);
+  if (f == 1) return (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
   return big_tiles(G) ? (n[0] / TX) * (n[1] / 16) * (n[2] / 16) : (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
 }
 
@@ -914,10 +898,17 @@ cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, floa
 }
 
 cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+  if (G.pairs == 6 && G.n[1] % 8 == 0 && G.n[2] % 16 == 0)   // the pair kernel on 32 x 8 x 16 tiles
+    return G.local ? pairs_t<true, 8>(s, ec, rhs, r, G, acc) : pairs_t<false, 8>(s, ec, rhs, r, G, acc);
+  if (G.pairs == 4 || G.pairs == 5) {   // TMA-staged operands, 64 x 16 columns of 32 (form 4) or 16 (form 5) planes
+    const int tz = G.pairs == 4 ? 32 : 16;
+    if (resid_tma_ok(G, tz) && ((uintptr_t)ec | (uintptr_t)rhs | (uintptr_t)acc) % 16 == 0)
+      return launch_resid_diff_tma(s, ec, rhs, r, G, acc, tz);
+  }
   const bool big = big_tiles(G);
   if (big && G.pairs == 3 && G.n[2] % 32 == 0)
     return G.local ? pairz_t<true, 32>(s, ec, rhs, r, G, acc) : pairz_t<false, 32>(s, ec, rhs, r, G, acc);
-  if (big && G.pairs >= 2)
+  if (big && (G.pairs == 2 || G.pairs == 3))
     return G.local ? pairz_t<true, 16>(s, ec, rhs, r, G, acc) : pairz_t<false, 16>(s, ec, rhs, r, G, acc);
   if (big && G.pairs) return G.local ? pairs_t<true>(s, ec, rhs, r, G, acc) : pairs_t<false>(s, ec, rhs, r, G, acc);
   if (!G.local)
@@ -931,6 +922,13 @@ cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, c
                              float* ohi, float* olo, float* r, const LG& G, float alpha, double* part, int* nparts,
                              const float* ed) {
   *nparts = tile_blocks(G);
+  const int form = acc_form(G);
+  if (form == 2)
+    return G.local ? acc_t<true, 8, 16, 256>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part)
+                   : acc_t<false, 8, 16, 256>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
+  if (form == 1)
+    return G.local ? acc_t<true, 8, 8, 256>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part)
+                   : acc_t<false, 8, 8, 256>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
   const bool big = big_tiles(G);
   if (G.local)
     return big ? acc_t<true, 16, 16>(s, hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part)

@@ -117,15 +117,19 @@ int tune_stencils(baorec_ctx* ctx) {
     ctx->tune.stream0 = ms[1] <= ms[0] ? 1 : 0;
   }
   // finest level: the tiled running residual with two z-adjacent cells per
-  // thread (packed FP32x2) against one cell per thread, and the packed form
-  // with its window streamed in z (blocks of 16 and 32 planes)
+  // thread (packed FP32x2) against one cell per thread, the packed form with
+  // its window streamed in z (blocks of 16 and 32 planes), and the form with
+  // TMA-staged operands and x-adjacent cell pairs (blocks of 32 and 16 planes)
   if (nl > 0 && tile_ok(L0.n)) {
     float* t = L0.r + L0.N;
-    float ms[4] = {0.0f, 0.0f, 1e30f, 1e30f};
-    const int nforms = (L0.n[1] % 16 == 0 && L0.n[2] % 16 == 0) ? 4 : 2;
-    for (int form = 0; form < nforms; ++form) {
+    float ms[7] = {0.0f, 0.0f, 1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+    const bool packed = L0.n[1] % 16 == 0 && L0.n[2] % 16 == 0;
+    for (int form = 0; form < 7; ++form) {
+      if (form >= 2 && form < 4 && !packed) continue;
+      if (form == 6 && (L0.n[1] % 8 || L0.n[2] % 16)) continue;
       ctx->tune.pairs = form;
       const LG G0 = level_geom_public(ctx, 0, 0.0f);
+      if (form >= 4 && !resid_tma_ok(G0, form == 4 ? 32 : 16)) continue;
       auto launch = [&]() -> int {
         CK(launch_resid_diff(ctx->stream, L0.v, L0.f, t, G0, L0.r));
         return BAOREC_OK;
@@ -134,9 +138,31 @@ int tune_stencils(baorec_ctx* ctx) {
       ctx->launches += 11;
     }
     int best = 0;
-    for (int form = 1; form < 4; ++form)
+    for (int form = 1; form < 7; ++form)
       if (ms[form] < ms[best]) best = form;
     ctx->tune.pairs = best;
+  }
+  // finest level: the accurate residual on 512-thread blocks (the level's
+  // tiles) against 256-thread blocks on 32x8x8 and 32x8x16 tiles
+  if (nl > 0 && tile_ok(L0.n)) {
+    float ms[3] = {0.0f, 1e30f, 1e30f};
+    for (int form = 0; form < 3; ++form) {
+      ctx->tune.acc = form;
+      const LG G0 = level_geom_public(ctx, 0, 0.0f);
+      if ((size_t)tile_blocks(G0) > kRedCapacity / 2) continue;
+      auto launch = [&]() -> int {
+        int np = 0;
+        CK(launch_resid_acc(ctx->stream, L0.v, ctx->phi_lo, nullptr, L0.f, ctx->phi_hi2, ctx->phi_lo2, L0.r, G0, 0.0f,
+                            ctx->dred, &np));
+        return BAOREC_OK;
+      };
+      CKS(time_ms(ctx, launch, 10, &ms[form]));
+      ctx->launches += 11;
+    }
+    int best = 0;
+    for (int form = 1; form < 3; ++form)
+      if (ms[form] < ms[best]) best = form;
+    ctx->tune.acc = best;
   }
   // FFT preconditioner: batched xy transforms around the fused z pass (two
   // register forms; xy transforms by cuFFT or, for 256 x 256 planes, by the
@@ -205,8 +231,16 @@ extern "C" int baorec_set_tune_stream(baorec_ctx* ctx, int stream) {
 extern "C" int baorec_tune_pairs(const baorec_ctx* ctx) { return ctx ? ctx->tune.pairs : -1; }
 
 extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
-  if (!ctx || pairs < 0 || pairs > 3) return BAOREC_ERR_ARG;
+  if (!ctx || pairs < 0 || pairs > 6) return BAOREC_ERR_ARG;
   ctx->tune.pairs = pairs;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_tune_acc(const baorec_ctx* ctx) { return ctx ? ctx->tune.acc : -1; }
+
+extern "C" int baorec_set_tune_acc(baorec_ctx* ctx, int acc) {
+  if (!ctx || acc < 0 || acc > 2) return BAOREC_ERR_ARG;
+  ctx->tune.acc = acc;
   return BAOREC_OK;
 }
 

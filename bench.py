@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-scale512", dest="scale512", action="store_false",
                     help="skip the 512^3 measurements (lightcone run! and solve, large box)")
     ap.add_argument("--set-tune", default="",
-                    help="after the autotuner, force choices: comma-separated key=value of pair_residual, "
+                    help="after the autotuner, force choices: comma-separated key=value of pair_residual, acc_residual, "
                          "fft_zpass, fft_xy_fused, stream_residuals, tiles (per level, 1:1:0:0) (a profiler "
                          "distorts the tuner's timings, "
                          "so a launch list under ncu pins the choices of the timed run)")
@@ -302,6 +302,17 @@ def run_batch(args, torch, np):
     return res
 
 
+RUNNING_RESIDUAL = {
+    0: "resid_kernel (difference form)",
+    1: "resid_pairs_kernel (FP32 running residual, two z-adjacent cells per thread)",
+    2: "resid_pairz_kernel (FP32 running residual, plane pairs streamed in z, 16-plane blocks)",
+    3: "resid_pairz_kernel (FP32 running residual, plane pairs streamed in z, 32-plane blocks)",
+    4: "resid_tma_kernel (FP32 running residual, TMA-staged, two x-adjacent cells per thread, 32-plane columns)",
+    5: "resid_tma_kernel (FP32 running residual, TMA-staged, two x-adjacent cells per thread, 16-plane columns)",
+    6: "resid_pairs_kernel (FP32 running residual, two z-adjacent cells per thread, 32x8x16 tiles)",
+}
+
+
 def traffic_per_launch(name, N):
     """DRAM bytes per launch of `name` from the committed ncu capture, scaled to N cells."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -471,8 +482,8 @@ def run_scale_512(args, torch, np, checks):
           "solver": {k: st[k] for k in ("cycles", "spectral_steps", "rel_residual")},
           "e2e": {"value": 1.0 / te, "unit": "recons/s", "ms_per_step": te * 1e3,
                   "h2d_bytes_per_step": 16 * (nd + nr) + 12 * nd + 12 * nr, "d2h_bytes_per_step": 12 * nd + 24 * nr},
-          "roofline": {"kernel": {3: "resid_pairs_kernel", 5: "resid_diff_stream_kernel"}.get(which, str(which)) +
-                       " (finest level 512^3)", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+          "roofline": {"kernel": (RUNNING_RESIDUAL[ctx.lib.baorec_tune_pairs(ctx.h)].split()[0] if which == 3
+                                  else "resid_diff_stream_kernel") + " (finest level 512^3)", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                        "frac": ach / peak, "peak_source": src, "avg_launch_ms": avg.value,
                        "algorithmic_bytes_per_launch": nbytes.value}}
     if checks:
@@ -772,7 +783,7 @@ def run_gb300(args):
     tune = ctx.autotune()
     for c_ in others.values():
         c_.autotune(paint=False)
-    setters = {"pair_residual": "baorec_set_tune_pairs", "fft_zpass": "baorec_set_tune_zpass",
+    setters = {"pair_residual": "baorec_set_tune_pairs", "acc_residual": "baorec_set_tune_acc", "fft_zpass": "baorec_set_tune_zpass",
                "fft_xy_fused": "baorec_set_tune_xy", "stream_residuals": "baorec_set_tune_stream"}
     for kv in filter(None, args.set_tune.split(",")):
         k, v = kv.split("=")
@@ -856,10 +867,7 @@ def run_gb300(args):
     # solve uses; the red-black sweep for the plain multigrid start
     peak, peak_src = measured_peak()
     N = int(np.prod(n))
-    pairs = tune.get("pair_residual", 0) == 1
-    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel",
-             3: "resid_pairs_kernel (FP32 running residual, two cells per thread)" if pairs
-             else "resid_kernel (difference form)",
+    names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: RUNNING_RESIDUAL[tune.get("pair_residual", 0)],
              4: "resid_acc_stream_kernel", 5: "resid_diff_stream_kernel"}
     meas = {}
     for which in (() if args.no_kernels else (0, 1, 3, 4, 5)):
@@ -870,16 +878,15 @@ def run_gb300(args):
                        "frac": ach / peak, "peak_source": peak_src,
                        "traffic": traffic_per_launch(names[which].split()[0], N),
                        "algorithmic_bytes_per_launch": nbytes.value, "avg_launch_ms": avg.value}
-    # every form of the FP32 running residual (tune.pairs 0-3), timed the same way; the tuner's choice restored
+    # every form of the FP32 running residual (tune.pairs 0-6), timed the same way; the tuner's choice restored
     if meas:
         forms = {}
         chosen = ctx.lib.baorec_tune_pairs(ctx.h)
-        for form in (0, 1, 2, 3):
+        for form in range(7):
             ctx.call("baorec_set_tune_pairs", form)
             avg, nbytes = C.c_float(), C.c_double()
             ctx.call("baorec_profile_kernel", 3, 30, C.byref(avg), C.byref(nbytes))
-            forms[{0: "one cell per thread", 1: "two cells per thread", 2: "pairs streamed in z, 16-plane blocks",
-                   3: "pairs streamed in z, 32-plane blocks"}[form]] = {
+            forms["%d: %s" % (form, RUNNING_RESIDUAL[form])] = {
                 "avg_launch_ms": avg.value, "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
         ctx.call("baorec_set_tune_pairs", chosen)
         meas["pair_forms"] = forms
@@ -890,7 +897,7 @@ def run_gb300(args):
         roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
         aux = {names[w]: meas[w] for w in meas if w != head and w != "pair_forms"}
         if "pair_forms" in meas:
-            aux["resid_pairs forms"] = meas["pair_forms"]
+            aux["running residual forms"] = meas["pair_forms"]
 
     # end to end through the C ABI with pinned host buffers
     e2e = None

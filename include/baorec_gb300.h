@@ -509,13 +509,22 @@ int baorec_set_tune(baorec_ctx* ctx, int32_t paint_tile, const int32_t* big_tile
  * cp.async-pipelined), 0 tiled, -1 not tuned (streaming where the mesh allows). */
 int baorec_tune_stream(const baorec_ctx* ctx);
 int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
-/* FP32 running residual of the FFT corrections on 32x16x16 tiles: 1 two
- * z-adjacent cells per thread in packed FP32x2 arithmetic (default), 0 one cell
+/* FP32 running residual of the FFT corrections: 1 two z-adjacent cells per
+ * thread in packed FP32x2 arithmetic on 32x16x16 tiles (default), 0 one cell
  * per thread, 2 and 3 the packed form with the window streamed through a ring
- * of plane pairs in blocks of 16 and 32 z planes (the same results as 1).
- * The stencil autotune times all four. */
+ * of plane pairs in blocks of 16 and 32 z planes, 4 and 5 two x-adjacent cells
+ * per thread on 64x16 columns of 32 and 16 z planes with every operand staged
+ * in shared memory by TMA (n[0] % 64 == 0, n[1] % 16 == 0; elsewhere form 1
+ * runs), 6 form 1 on 32x8x16 tiles of 256 threads (four blocks per SM).
+ * Forms 1-6 give the same bits.  The stencil autotune times all seven. */
 int baorec_tune_pairs(const baorec_ctx* ctx);
 int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
+/* Accurate residual (double-float solution update) of the residual-driven
+ * solve on the finest level: 0 blocks of 512 threads on the level's tiles
+ * (default), 1 and 2 blocks of 256 threads on 32x8x8 and 32x8x16 tiles.  The
+ * same results; the stencil autotune times all three. */
+int baorec_tune_acc(const baorec_ctx* ctx);
+int baorec_set_tune_acc(baorec_ctx* ctx, int acc);
 /* FFT preconditioner of the residual-driven solve where n[2] = 256: 1 batched
  * 2-D transforms of the xy planes around one kernel that transforms along z,
  * multiplies by S^-1(k) and transforms back (default), 2 the same with the

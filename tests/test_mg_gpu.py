@@ -287,13 +287,17 @@ def test_cycle_cap_returns_not_converged_with_the_last_iterate():
     assert st2["rel_residual_initial"] <= 1.05 * st["rel_residual"]
 
 
-@pytest.mark.parametrize("shape,los", [((64, 64, 64), None), ((32, 48, 96), [0.0, 0.6, 0.8]), ((64, 32, 48), None)])
+@pytest.mark.parametrize("shape,los", [((64, 64, 64), None), ((32, 48, 96), [0.0, 0.6, 0.8]), ((64, 32, 48), None),
+                                       ((128, 64, 64), None), ((64, 64, 32), [0.0, 0.0, 1.0])])
 def test_streamed_pair_running_residual_is_bit_identical(shape, los):
-    """The running residual with its window streamed through a ring of plane
+    """Every packed form of the running residual does the pair kernel's
+    arithmetic cell for cell: the window streamed through a ring of plane
     pairs (16- and 32-plane blocks; the 32-plane form falls back to 16 where
-    n3 is not a multiple of 32) does the packed pair kernel's arithmetic cell
-    for cell: the FFT start's residual, the solve history and the solution
-    are the same bits."""
+    n3 is not a multiple of 32), and the TMA-staged form with x-adjacent pairs
+    (32- and 16-plane columns; it falls back to the pair kernel where n1 is
+    not a multiple of 64, n2 not of 16 or n3 not of the column length), and
+    the pair kernel on 32x8x16 tiles of 256 threads.  The FFT start's
+    residual, the solve history and the solution are the same bits."""
     import ctypes as C
     import torch
     import baorec
@@ -306,7 +310,7 @@ def test_streamed_pair_running_residual_is_bit_identical(shape, los):
     ff = np.asfortranarray(f)
     fd = torch.from_numpy(np.ascontiguousarray(f.ravel(order="F"))).cuda()
     out = []
-    for pairs in (1, 2, 3):
+    for pairs in (1, 2, 3, 4, 5, 6):
         rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="spectral")
         ctx = baorec.setup_fft_(rec, shape)
         ctx.call("baorec_set_tune", 8, (C.c_int32 * 16)(*([1] * 16)))
@@ -322,3 +326,36 @@ def test_streamed_pair_running_residual_is_bit_identical(shape, los):
         assert rel == out[0][0]
         assert hist == out[0][1]
         np.testing.assert_array_equal(phi, out[0][2])
+
+
+@pytest.mark.parametrize("los", [None, [0.0, 0.6, 0.8]])
+def test_accurate_residual_block_shapes_agree(los):
+    """The accurate residual (double-float solution update) on 512-thread
+    blocks and on 256-thread blocks of 32x8x8 and 32x8x16 tiles: the same
+    per-cell arithmetic, so the solve takes the same steps and reaches the
+    same solution; only the per-block partial sums of the residual norm are
+    grouped differently: FP32 sums within a block's threads, so the history
+    agrees to FP32 rounding of those sums (1e-5 relative)."""
+    import ctypes as C
+    import baorec
+    f, bs, bm = _problem(n=64, seed=21)
+    ff = np.asfortranarray(f)
+    out = []
+    for acc in (0, 1, 2):
+        rec = _recon(bs, bm, los, mg_mode="convergent", rtol=1e-6, max_cycles=40, start="spectral")
+        ctx = baorec.setup_fft_(rec, f.shape)
+        ctx.call("baorec_set_tune", 8, (C.c_int32 * 16)(*([1] * 16)))
+        ctx.call("baorec_set_tune_stream", 0)
+        ctx.call("baorec_set_tune_acc", acc)
+        assert ctx.lib.baorec_tune_acc(ctx.h) == acc
+        phi = baorec.zeros_mesh(f.shape, device=False)
+        st = baorec.solve_(phi, ff, rec)
+        assert st["rel_residual"] <= 1e-6
+        out.append((ctx.solve_history(), np.asarray(phi, np.float64).copy()))
+    h0, p0 = out[0]
+    for h, p in out[1:]:
+        assert [k for _, k in h] == [k for _, k in h0]
+        for (r, _), (r0, _) in zip(h, h0):
+            assert abs(r - r0) <= 1e-5 * r0
+        assert np.max(np.abs(p - p0)) <= 1e-5 * np.max(np.abs(p0))
+    assert ctx.status("baorec_set_tune_acc", 3) == baorec._lib.ERR_ARG
