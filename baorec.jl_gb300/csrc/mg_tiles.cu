@@ -353,11 +353,8 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
   }
 }
 
-// Accurate residual with solution update: each window chunk of (hi, lo) + e
-// becomes the updated double-float pair as it is loaded, held as interleaved
-// (hi, lo) pairs (one 8-byte shared load per neighbour and one packed
-// subtraction give both parts of a difference); then
-// The FP32 running residual of the FFT corrections on 32 x 16 x 16 tiles, two
+// The FP32 running residual of the FFT corrections on 32 x TY x 16 tiles (TY =
+// 16: two blocks of 512 threads per SM; TY = 8: four of 256), two
 // z-adjacent cells per thread in packed FP32x2 arithmetic:
 //   r = (rhs - shift) + bracket(e_nb - e_0),  acc += e  (optional).
 // The window is stored as plane pairs: pair j interleaves window planes 2j
@@ -638,11 +635,16 @@ __global__ void __launch_bounds__(NT, 2) resid_pairz_kernel(const float* __restr
   }
 }
 
+// Accurate residual with solution update: each window chunk of (hi, lo) + e
+// becomes the updated double-float pair as it is loaded, held as interleaved
+// (hi, lo) pairs (one 8-byte shared load per neighbour and one packed
+// subtraction give both parts of a difference); then
 // r = (f - α) + bracket over differences D = v_nb - v_0 with the exact
 // operator, whose coefficients are evaluated with IEEE round-to-nearest
 // operations in the reference's order.  Per-block (Σr, Σr²) to part.  The
 // solution pair is (hi, lo) + ec first; with HASD the correction is ec + ed,
-// added in FP32 as a separate e += d pass would.
+// added in FP32 as a separate e += d pass would.  NTH threads per block
+// (512, or 256 for four blocks per SM on 32 x 8 x 8 / 32 x 8 x 16 tiles).
 template <bool LOCAL, int TY, int TZ, bool HASD, int NTH = NT>
 __global__ void __launch_bounds__(NTH, 1024 / NTH) resid_acc2_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
                                                         const float* __restrict__ ec, const float* __restrict__ ed,

@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--conv-only", action="store_true",
                     help="only time the learned guess's tensor-core convolutions, every shape on a --mesh grid "
                          "(a small case for profilers)")
+    ap.add_argument("--stencil-only", default="",
+                    help="only time finest-level stencil kernels on a --mesh grid (a small case for profilers): "
+                         "comma-separated kernel:pairs:acc, kernel 0 sweep, 1 accurate residual, 3 running "
+                         "residual, pairs and acc the forms of baorec_set_tune_pairs / baorec_set_tune_acc")
+    ap.add_argument("--stencil-reps", type=int, default=20)
     ap.add_argument("--start", default="spectral", choices=["zero", "spectral", "learned"],
                     help="start of the headline solve: zero (plain multigrid), spectral (FFT-preconditioned "
                          "corrections, V-cycles if they stall) or learned (CNN guess, then as spectral); "
@@ -746,6 +751,34 @@ def run_conv_only(args):
     return 0
 
 
+def run_stencil_only(args):
+    """Finest-level stencil kernels alone (baorec_profile_kernel) on a --mesh
+    grid with the lightcone workload's radial line of sight: one JSON line."""
+    import ctypes as C
+    import torch
+    from baorec import _lib
+    cfg = _lib.default_config()
+    cfg.method = _lib.MULTIGRID
+    cfg.mg_mode = _lib.MG_CONVERGENT
+    for a, lo in enumerate((500.0, 300.0, 200.0)):
+        cfg.n[a] = args.mesh
+        cfg.box_size[a] = 2000.0 * args.mesh / 256
+        cfg.box_min[a] = lo
+    ctx = _lib.Context(cfg)
+    torch.cuda.synchronize()
+    rows = []
+    for spec in filter(None, args.stencil_only.split(",")):
+        which, pairs, acc = (list(map(int, spec.split(":"))) + [1, 0])[:3]
+        ctx.call("baorec_set_tune_pairs", pairs)
+        ctx.call("baorec_set_tune_acc", acc)
+        avg, nbytes = C.c_float(), C.c_double()
+        ctx.call("baorec_profile_kernel", which, args.stencil_reps, C.byref(avg), C.byref(nbytes))
+        rows.append({"kernel": which, "pairs": pairs, "acc": acc, "avg_launch_us": avg.value * 1e3,
+                     "algorithmic_GBps": nbytes.value / (avg.value * 1e-3) / 1e9})
+    print(json.dumps({"metric": "stencil kernel time", "mesh": args.mesh, "kernels": rows}), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -754,6 +787,8 @@ def run_gb300(args):
     from baorec import _lib
     if args.conv_only:
         return run_conv_only(args)
+    if args.stencil_only:
+        return run_stencil_only(args)
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
