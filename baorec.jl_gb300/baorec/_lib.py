@@ -136,6 +136,8 @@ _SIGS = {
     "baorec_set_tune_stream": (C.c_int, [P, C.c_int]),
     "baorec_tune_pairs": (C.c_int, [P]),
     "baorec_set_tune_pairs": (C.c_int, [P, C.c_int]),
+    "baorec_tune_binned": (C.c_int, [P]),
+    "baorec_set_tune_binned": (C.c_int, [P, C.c_int]),
     "baorec_tune_acc": (C.c_int, [P]),
     "baorec_set_tune_acc": (C.c_int, [P, C.c_int]),
     "baorec_tune_zpass": (C.c_int, [P]),
@@ -276,7 +278,8 @@ class Context:
         pt = C.c_int32()
         bt = (C.c_int32 * 16)()
         self.call("baorec_autotune", (1 if stencil else 0) | (2 if paint else 0), C.byref(pt), bt)
-        return {"paint_tile": pt.value, "tile16_per_level": list(bt),
+        return {"paint_tile": pt.value, "paint_binned": int(self.lib.baorec_tune_binned(self.h)),
+                "tile16_per_level": list(bt),
                 "stream_residuals": int(self.lib.baorec_tune_stream(self.h)),
                 "pair_residual": int(self.lib.baorec_tune_pairs(self.h)),
                 "acc_residual": int(self.lib.baorec_tune_acc(self.h)),

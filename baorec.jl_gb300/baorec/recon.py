@@ -373,8 +373,9 @@ def setup_box(x, y, z, box_pad):
 # mass assignment — src/mas.jl
 # ----------------------------------------------------------------------------
 
-def _paint(name, rho, x, y, z, w, box_size, box_min, wrap, deterministic=False):
+def _paint(name, rho, x, y, z, w, box_size, box_min, wrap, deterministic=False, binned=None):
     ctx = _prim_ctx(rho.shape, box_size, box_min)
+    ctx.call("baorec_set_tune_binned", 0 if binned is None else int(bool(binned)))
     p = _Particles(x, y, z, w)
     flags = p.flags | (_lib.WRITEBACK if wrap else 0) | (_lib.DETERMINISTIC if deterministic else 0)
     with _Mesh(rho) as m:
@@ -385,14 +386,17 @@ def _paint(name, rho, x, y, z, w, box_size, box_min, wrap, deterministic=False):
     return rho
 
 
-def cic_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False):
-    """``cic!`` (``src/mas.jl:1-107``): add CIC weights to ``rho``."""
-    return _paint("baorec_cic", rho, x, y, z, w, box_size, box_min, wrap, deterministic)
+def cic_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False, binned=None):
+    """``cic!`` (``src/mas.jl:1-107``): add CIC weights to ``rho``.  ``binned``
+    picks the FP32 paint (None / False: one float atomic per weight, as the
+    reference's GPU kernel; True: tile counting sort and shared-memory tiles)."""
+    return _paint("baorec_cic", rho, x, y, z, w, box_size, box_min, wrap, deterministic, binned)
 
 
-def tsc_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False):
-    """Triangular-shaped-cloud paint (no reference counterpart)."""
-    return _paint("baorec_tsc", rho, x, y, z, w, box_size, box_min, wrap, deterministic)
+def tsc_(rho, x, y, z, w, box_size, box_min, wrap=True, deterministic=False, binned=None):
+    """Triangular-shaped-cloud paint (no reference counterpart); ``binned`` as
+    for :func:`cic_`."""
+    return _paint("baorec_tsc", rho, x, y, z, w, box_size, box_min, wrap, deterministic, binned)
 
 
 def cell_bins(x, y, z, box_size, box_min, dims, wrap=True):

@@ -282,8 +282,8 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
   cudaFree(ctx->derr);
   cudaFreeHost(ctx->herr);
   for (auto& b : ctx->stage) cudaFree(b.p);
-  for (DevBuf* b : {&ctx->sort_keys, &ctx->sort_perm, &ctx->sort_tiles, &ctx->fix_mesh, &ctx->pw_mesh, &ctx->pw_spec,
-                    &ctx->pw_part, &ctx->pw_nz})
+  for (DevBuf* b : {&ctx->sort_keys, &ctx->sort_perm, &ctx->sort_tiles, &ctx->fix_mesh, &ctx->bin_parts,
+                    &ctx->pw_mesh, &ctx->pw_spec, &ctx->pw_part, &ctx->pw_nz})
     cudaFree(b->p);
   if (ctx->ev_red) cudaEventDestroy(ctx->ev_red);
   for (int s = 0; s < 2; ++s)

@@ -102,9 +102,11 @@ struct baorec_ctx {
   cudaEvent_t ev_guess[2] = {nullptr, nullptr};
   // deterministic paint scratch: tile keys, permutation, tile counts/offsets, fixed-point mesh
   baorec::DevBuf sort_keys, sort_perm, sort_tiles, fix_mesh;
+  baorec::DevBuf bin_parts;            // binned paint: particles (x, y, z, w) ordered by mesh tile
   baorec::DevBuf pw_mesh, pw_spec, pw_part, pw_nz;   // power-spectrum scratch (power.cu)
   struct Tune {                        // launch shapes (defaults, or chosen by baorec_autotune)
     int paint_tile = 8;                // tile edge of the deterministic paint
+    int binned = 0;                    // FP32 paint: 0 global atomics, 1 binned (tile sort + shared-memory tiles)
     int stream0 = -1;                  // finest-level residuals: -1 default (streaming), 0 tile, 1 streaming
     int pairs = 1;                     // form of the FP32 running residual (baorec_set_tune_pairs)
     int acc = 0;                       // form of the accurate residual (baorec_set_tune_acc)
@@ -193,6 +195,10 @@ inline Geom geom_of(const baorec_ctx* c) {
 // ---- entry points implemented per translation unit ------------------------
 // paint.cu
 int paint_sorted(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w, int64_t n, int wrap,
+                 int mas, uint32_t flags);
+// FP32 paint by tile sort and shared-memory tiles (paint_sorted.cu)
+bool paint_binned_ok(const baorec_ctx* ctx, int64_t n);
+int paint_binned(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w, int64_t n, int wrap,
                  int mas, uint32_t flags);
 int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w,
           int64_t n, int wrap, int mas, uint32_t flags);

@@ -149,6 +149,7 @@ int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const floa
           int64_t n, int wrap, int mas, uint32_t flags) {
   if (n <= 0) return BAOREC_OK;
   if (flags & BAOREC_DETERMINISTIC) return paint_sorted(ctx, mesh, x, y, z, w, n, wrap, mas, flags);
+  if (ctx->tune.binned && paint_binned_ok(ctx, n)) return paint_binned(ctx, mesh, x, y, z, w, n, wrap, mas, flags);
   PaintGeom g = paint_geom(ctx, wrap);
   unsigned grid = grid_for((size_t)n, 256);
   if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;

@@ -12,6 +12,20 @@
 // mesh.  Integer addition is associative, so the painted mesh is the same
 // bits on every run.  The cell indices and the per-particle FP32 weights are
 // those of the atomic paint (shared arithmetic in paint_common.cuh).
+//
+// Binned FP32 paint (baorec_set_tune_binned; the reference's CIC kernel at
+// src/mas.jl:53-99, like this library's default paint, adds every weight to
+// the mesh with a float atomic): particles are bucketed by mesh tile with an
+// integer counting sort — per-block shared-memory histograms flushed to
+// global tile counts, an exclusive scan, and a scatter that reserves each
+// block's range of every tile with one atomic and writes the particles as
+// (x, y, z, w) records in tile order.  One block per tile then adds its
+// particles' weights in shared memory (FP32 atomics on shared memory) over
+// the tile plus its halo and writes the tile once: cells that only this
+// tile's particles reach with a plain read-add-store, the shared faces with
+// global atomics.  The per-particle weights are the atomic paint's; only the
+// order of the FP32 additions differs, as between two runs of the atomic
+// paint.
 #include "paint_common.cuh"
 
 namespace baorec {
@@ -199,7 +213,233 @@ __global__ void fix_to_mesh_kernel(const unsigned long long* __restrict__ fix, f
   }
 }
 
+// ---- binned FP32 paint ------------------------------------------------------
+
+constexpr int kBinChunk = 4096;   // particles per block of the count and scatter passes
+constexpr int kMaxBins = 4096;    // tiles: shared histogram of the count and scatter passes
+constexpr int kBinThreads = 256;
+static_assert(kBinChunk <= 4096 && kMaxBins <= (1 << 19), "key and rank packed in 31 bits");
+
+struct BinGeom {
+  int T, shift;   // tile edge (a power of two) and its log2
+  int nt[3];
+  int ntiles;
+};
+
+template <int MAS>
+__device__ __forceinline__ int bin_of(float px, float py, float pz, const PaintGeom& g, const BinGeom& bg) {
+  int b[3];
+  if (!base_cell<MAS>(px, py, pz, g, b)) return -1;
+  return (b[0] >> bg.shift) + bg.nt[0] * ((b[1] >> bg.shift) + bg.nt[1] * (b[2] >> bg.shift));
+}
+
+// Tile counts: a shared histogram per block of kBinChunk particles, flushed
+// with one global atomic per nonempty tile.  Wraps (and writes back) the
+// positions as the atomic paint does.
+template <int MAS>
+__global__ void __launch_bounds__(kBinThreads) bin_count_kernel(float* __restrict__ x, float* __restrict__ y,
+                                                                float* __restrict__ z, int64_t n, PaintGeom g,
+                                                                BinGeom bg, int writeback,
+                                                                int32_t* __restrict__ counts, unsigned* err) {
+  __shared__ int h[kMaxBins];
+  for (int b = threadIdx.x; b < bg.ntiles; b += kBinThreads) h[b] = 0;
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.x * kBinChunk;
+  const int64_t i1 = n < i0 + kBinChunk ? n : i0 + kBinChunk;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kBinThreads) {
+    float px = x[i], py = y[i], pz = z[i];
+    if (g.wrap) {
+      px = wrap_pos(px, g); py = wrap_pos(py, g); pz = wrap_pos(pz, g);
+      if (writeback) { x[i] = px; y[i] = py; z[i] = pz; }
+    }
+    const int k = bin_of<MAS>(px, py, pz, g, bg);
+    if (k < 0) atomicOr(err, kErrOOB);
+    else atomicAdd(&h[k], 1);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < bg.ntiles; b += kBinThreads)
+    if (h[b]) atomicAdd(counts + b, h[b]);
+}
+
+// Scatter: each particle's rank within its block and tile from a shared
+// atomic, one global atomic per (block, nonempty tile) to reserve the
+// block's range of the tile, then (x, y, z, w) to its place.
+template <int MAS>
+__global__ void __launch_bounds__(kBinThreads) bin_scatter_kernel(const float* __restrict__ x,
+                                                                  const float* __restrict__ y,
+                                                                  const float* __restrict__ z,
+                                                                  const float* __restrict__ w, int64_t n,
+                                                                  PaintGeom g, BinGeom bg,
+                                                                  int32_t* __restrict__ cursor,
+                                                                  float4* __restrict__ parts) {
+  __shared__ int h[kMaxBins];          // counts, then the block's base in each tile
+  __shared__ int kr[kBinChunk];        // tile << 12 | rank, -1 outside the mesh
+  for (int b = threadIdx.x; b < bg.ntiles; b += kBinThreads) h[b] = 0;
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.x * kBinChunk;
+  const int m = (int)((n < i0 + kBinChunk ? n : i0 + kBinChunk) - i0);
+  for (int j = threadIdx.x; j < m; j += kBinThreads) {
+    float px = x[i0 + j], py = y[i0 + j], pz = z[i0 + j];
+    if (g.wrap) { px = wrap_pos(px, g); py = wrap_pos(py, g); pz = wrap_pos(pz, g); }
+    const int k = bin_of<MAS>(px, py, pz, g, bg);
+    kr[j] = k < 0 ? -1 : (k << 12) | atomicAdd(&h[k], 1);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < bg.ntiles; b += kBinThreads)
+    if (h[b]) h[b] = atomicAdd(cursor + b, h[b]);
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += kBinThreads) {
+    const int v = kr[j];
+    if (v < 0) continue;
+    float px = x[i0 + j], py = y[i0 + j], pz = z[i0 + j];
+    if (g.wrap) { px = wrap_pos(px, g); py = wrap_pos(py, g); pz = wrap_pos(pz, g); }
+    parts[h[v >> 12] + (v & 4095)] = make_float4(px, py, pz, w[i0 + j]);
+  }
+}
+
+// One block per tile: the tile's particles into shared FP32 accumulators
+// over cells t0-1 .. t0+T per axis (local 0 .. T+1), then each nonzero cell
+// once into the mesh.  A cell that no other tile's particles reach (CIC:
+// t0+1 .. t0+T-1, TSC: t0+1 .. t0+T-2, short of the mesh's last cell or two
+// where a wrapped neighbour tile reaches) gets a plain read-add-store; the
+// shared faces get global atomics.
+template <int MAS>
+__global__ void __launch_bounds__(kBinThreads) bin_paint_kernel(const float4* __restrict__ parts,
+                                                                const int32_t* __restrict__ offsets, PaintGeom g,
+                                                                BinGeom bg, float* __restrict__ mesh) {
+  extern __shared__ float acc_f[];
+  const int T = bg.T, S = T + 2, S3 = S * S * S;
+  const int tile = blockIdx.x;
+  const int begin = offsets[tile], end = offsets[tile + 1];
+  if (begin == end) return;   // block-uniform
+  const int tx = tile % bg.nt[0], ty = (tile / bg.nt[0]) % bg.nt[1], tz = tile / (bg.nt[0] * bg.nt[1]);
+  const int t0[3] = {tx * T, ty * T, tz * T};
+  const int o[3] = {t0[0] - 1, t0[1] - 1, t0[2] - 1};   // mesh cell of local 0
+  for (int c = threadIdx.x; c < S3; c += kBinThreads) acc_f[c] = 0.0f;
+  __syncthreads();
+  for (int p = begin + threadIdx.x; p < end; p += kBinThreads) {
+    const float4 q = parts[p];
+    if (MAS == BAOREC_MAS_TSC) {
+      int ix[3], iy[3], iz[3];
+      float wx[3], wy[3], wz[3];
+      tsc_axis(q.x, g.bmin[0], g.fn[0], g.L[0], g.n[0], g.wrap, ix, wx);
+      tsc_axis(q.y, g.bmin[1], g.fn[1], g.L[1], g.n[1], g.wrap, iy, wy);
+      tsc_axis(q.z, g.bmin[2], g.fn[2], g.L[2], g.n[2], g.wrap, iz, wz);
+      const int lx = ix[1] - o[0] - 1, ly = iy[1] - o[1] - 1, lz = iz[1] - o[2] - 1;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+            atomicAdd(acc_f + (lx + a) + S * ((ly + b) + S * (lz + c)),
+                      __fmul_rn(__fmul_rn(__fmul_rn(q.w, wx[a]), wy[b]), wz[c]));
+    } else {
+      int x0, x1, y0, y1, z0, z1;
+      float wx1, wy1, wz1;
+      cic_axis(cic_coord(q.x, g.bmin[0], g.fn[0], g.L[0]), g.n[0], g.wrap, x0, x1, wx1);
+      cic_axis(cic_coord(q.y, g.bmin[1], g.fn[1], g.L[1]), g.n[1], g.wrap, y0, y1, wy1);
+      cic_axis(cic_coord(q.z, g.bmin[2], g.fn[2], g.L[2]), g.n[2], g.wrap, z0, z1, wz1);
+      const float wx0 = __fmul_rn(__fsub_rn(1.0f, wx1), q.w);
+      wx1 = __fmul_rn(wx1, q.w);
+      const float wy0 = __fsub_rn(1.0f, wy1), wz0 = __fsub_rn(1.0f, wz1);
+      const int l0 = (x0 - 1 - o[0]) + S * ((y0 - 1 - o[1]) + S * (z0 - 1 - o[2]));
+      atomicAdd(acc_f + l0, __fmul_rn(__fmul_rn(wx0, wy0), wz0));
+      atomicAdd(acc_f + l0 + 1, __fmul_rn(__fmul_rn(wx1, wy0), wz0));
+      atomicAdd(acc_f + l0 + S, __fmul_rn(__fmul_rn(wx0, wy1), wz0));
+      atomicAdd(acc_f + l0 + S * S, __fmul_rn(__fmul_rn(wx0, wy0), wz1));
+      atomicAdd(acc_f + l0 + 1 + S, __fmul_rn(__fmul_rn(wx1, wy1), wz0));
+      atomicAdd(acc_f + l0 + 1 + S * S, __fmul_rn(__fmul_rn(wx1, wy0), wz1));
+      atomicAdd(acc_f + l0 + S + S * S, __fmul_rn(__fmul_rn(wx0, wy1), wz1));
+      atomicAdd(acc_f + l0 + 1 + S + S * S, __fmul_rn(__fmul_rn(wx1, wy1), wz1));
+    }
+  }
+  __syncthreads();
+  const int reach = MAS == BAOREC_MAS_TSC ? 1 : 0;   // how far above a particle's tile its weights land, minus one
+  for (int c = threadIdx.x; c < S3; c += kBinThreads) {
+    const float v = acc_f[c];
+    if (v == 0.0f) continue;
+    const int l[3] = {c % S, (c / S) % S, c / (S * S)};
+    int m[3];
+    bool in = true, own = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int u = o[a] + l[a];   // unwrapped mesh cell
+      const int hi = min(t0[a] + T - 1, g.n[a] - 1) - reach;
+      own &= u >= t0[a] + 1 && u <= hi;
+      m[a] = u < 0 ? u + g.n[a] : (u >= g.n[a] ? u - g.n[a] : u);
+      in &= m[a] >= 0 && m[a] < g.n[a];
+    }
+    if (!in) continue;
+    float* cell = mesh + lin(m[0], m[1], m[2], g);
+    if (own) *cell = __fadd_rn(*cell, v);
+    else atomicAdd(cell, v);
+  }
+}
+
 }  // namespace
+
+// Tile edge of the binned paint: the smallest power of two >= 16 with at
+// most kMaxBins tiles; 0 when none fits the shared accumulators.
+static int bin_tile(const int n[3]) {
+  for (int T = 16; T <= 32; T *= 2) {
+    const long long nt = (long long)((n[0] + T - 1) / T) * ((n[1] + T - 1) / T) * ((n[2] + T - 1) / T);
+    if (nt <= kMaxBins) return T;
+  }
+  return 0;
+}
+
+bool paint_binned_ok(const baorec_ctx* ctx, int64_t n) {
+  const int nn[3] = {ctx->n1, ctx->n2, ctx->n3};
+  return n > 0 && n <= (int64_t)INT32_MAX && bin_tile(nn) > 0;
+}
+
+int paint_binned(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w, int64_t n, int wrap,
+                 int mas, uint32_t flags) {
+  if (n <= 0) return BAOREC_OK;
+  if (!paint_binned_ok(ctx, n)) return set_error(ctx, BAOREC_ERR_ARG, "binned paint: mesh or catalogue too large");
+  PaintGeom g = paint_geom(ctx, wrap);
+  BinGeom bg;
+  const int nn[3] = {ctx->n1, ctx->n2, ctx->n3};
+  bg.T = bin_tile(nn);
+  bg.shift = bg.T == 16 ? 4 : 5;
+  for (int a = 0; a < 3; ++a) bg.nt[a] = (g.n[a] + bg.T - 1) / bg.T;
+  bg.ntiles = bg.nt[0] * bg.nt[1] * bg.nt[2];
+  CKS(ensure(ctx, ctx->bin_parts, (size_t)n * sizeof(float4)));
+  CKS(ensure(ctx, ctx->sort_tiles, (size_t)(3 * bg.ntiles + 1) * 4));
+  int32_t* counts = (int32_t*)ctx->sort_tiles.p;
+  int32_t* offsets = counts + bg.ntiles;   // ntiles + 1
+  int32_t* cursor = offsets + bg.ntiles + 1;
+  float4* parts = (float4*)ctx->bin_parts.p;
+  CK(cudaMemsetAsync(counts, 0, (size_t)bg.ntiles * 4, ctx->stream));
+  const unsigned blocks = (unsigned)((n + kBinChunk - 1) / kBinChunk);
+  const int wb = (flags & BAOREC_WRITEBACK) ? 1 : 0;
+  const int S = bg.T + 2;
+  const size_t smem = (size_t)S * S * S * sizeof(float);
+  if (mas == BAOREC_MAS_TSC) {
+    bin_count_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr);
+    CKLAUNCH();
+    tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles);
+    CKLAUNCH();
+    bin_scatter_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts);
+    CKLAUNCH();
+    if (smem > 48 * 1024)
+      CK(cudaFuncSetAttribute(bin_paint_kernel<BAOREC_MAS_TSC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bin_paint_kernel<BAOREC_MAS_TSC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh);
+  } else {
+    bin_count_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr);
+    CKLAUNCH();
+    tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles);
+    CKLAUNCH();
+    bin_scatter_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts);
+    CKLAUNCH();
+    if (smem > 48 * 1024)
+      CK(cudaFuncSetAttribute(bin_paint_kernel<BAOREC_MAS_CIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bin_paint_kernel<BAOREC_MAS_CIC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh);
+  }
+  CKLAUNCH();
+  return BAOREC_OK;
+}
 
 int paint_sorted(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const float* w, int64_t n, int wrap,
                  int mas, uint32_t flags) {

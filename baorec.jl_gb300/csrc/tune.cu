@@ -210,6 +210,15 @@ int tune_paint(baorec_ctx* ctx) {
     if (st == BAOREC_OK && ms < best) { best = ms; pick = cand[c]; }
   }
   ctx->tune.paint_tile = pick;
+  // the FP32 paint: global float atomics against the binned paint
+  float ms_mode[2] = {1e30f, 1e30f};
+  const int keep = ctx->tune.binned;
+  for (int mode = 0; mode < 2 && st == BAOREC_OK; ++mode) {
+    ctx->tune.binned = mode;
+    auto launch = [&]() -> int { return paint(ctx, mesh, p, p + n, p + 2 * n, p + 3 * n, n, 1, ctx->cfg.mas, 0); };
+    st = time_ms(ctx, launch, 3, &ms_mode[mode]);
+  }
+  ctx->tune.binned = st == BAOREC_OK ? (ms_mode[1] <= ms_mode[0] ? 1 : 0) : keep;
   cudaStreamSynchronize(ctx->stream);
   cudaFree(p);
   return st;
@@ -233,6 +242,14 @@ extern "C" int baorec_tune_pairs(const baorec_ctx* ctx) { return ctx ? ctx->tune
 extern "C" int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs) {
   if (!ctx || pairs < 0 || pairs > 6) return BAOREC_ERR_ARG;
   ctx->tune.pairs = pairs;
+  return BAOREC_OK;
+}
+
+extern "C" int baorec_tune_binned(const baorec_ctx* ctx) { return ctx ? ctx->tune.binned : -1; }
+
+extern "C" int baorec_set_tune_binned(baorec_ctx* ctx, int binned) {
+  if (!ctx || binned < 0 || binned > 1) return BAOREC_ERR_ARG;
+  ctx->tune.binned = binned;
   return BAOREC_OK;
 }
 

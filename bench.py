@@ -68,6 +68,9 @@ def parse():
                          "comma-separated kernel:pairs:acc, kernel 0 sweep, 1 accurate residual, 3 running "
                          "residual, pairs and acc the forms of baorec_set_tune_pairs / baorec_set_tune_acc")
     ap.add_argument("--stencil-reps", type=int, default=20)
+    ap.add_argument("--paint-only", default="",
+                    help="only time the CIC paint of the lightcone randoms into the --mesh grid (a small case "
+                         "for profilers): comma-separated modes atomic, binned, deterministic")
     ap.add_argument("--start", default="spectral", choices=["zero", "spectral", "learned"],
                     help="start of the headline solve: zero (plain multigrid), spectral (FFT-preconditioned "
                          "corrections, V-cycles if they stall) or learned (CNN guess, then as spectral); "
@@ -779,6 +782,37 @@ def run_stencil_only(args):
     return 0
 
 
+def run_paint_only(args):
+    """The CIC paint of the workload's randoms alone, per mode: one JSON line."""
+    import torch
+    import baorec
+    from baorec import _lib
+    m, bs, bm = workload(args, args.seed)
+    rec = baorec.MultigridRecon(bias=2.0, f=0.8, smoothing_radius=15.0, box_size=bs, box_min=bm, los=None,
+                                mg_mode="convergent", rtol=1e-6)
+    ctx = baorec.setup_fft_(rec, (args.mesh,) * 3)
+    R = [torch.from_numpy(a).cuda() for a in (m.rx, m.ry, m.rz, m.rw)]
+    nr = int(m.rx.shape[0])
+    mesh = torch.zeros(args.mesh ** 3, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    torch.cuda.synchronize()
+    rows = []
+    for mode in filter(None, args.paint_only.split(",")):
+        fl = _lib.DETERMINISTIC if mode == "deterministic" else 0
+        ctx.call("baorec_set_tune_binned", 1 if mode == "binned" else 0)
+        run = lambda f: ctx.call("baorec_cic", mesh.data_ptr(), *[t.data_ptr() for t in R], nr, 0, f)
+        run(fl)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.stencil_reps):
+            run(fl | _lib.ASYNC)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rows.append({"mode": mode, "avg_ms": e0.elapsed_time(e1) / args.stencil_reps})
+    print(json.dumps({"metric": "paint time", "mesh": args.mesh, "particles": nr, "paints": rows}), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -789,6 +823,8 @@ def run_gb300(args):
         return run_conv_only(args)
     if args.stencil_only:
         return run_stencil_only(args)
+    if args.paint_only:
+        return run_paint_only(args)
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -957,11 +993,15 @@ def run_gb300(args):
                "h2d_bytes_per_step": 16 * (nd + nr) + 12 * nd + 12 * nr,
                "d2h_bytes_per_step": 12 * nd + 24 * nr, "ms_per_step": te * 1e3}
 
-    # particles painted/s: the 5e6 randoms into a 256^3 mesh, float-atomic and deterministic paints
+    # particles painted/s: the 5e6 randoms into a 256^3 mesh, float-atomic, binned and deterministic paints
     stream = torch.cuda.ExternalStream(ctx.stream)
     scratch = torch.zeros(N, device="cuda")
-    for label, fl in (() if args.no_kernels else
-                      (("cic_paint (atomic)", 0), ("cic_paint (deterministic, tile sort)", _lib.DETERMINISTIC))):
+    binned = ctx.lib.baorec_tune_binned(ctx.h)
+    for label, fl, mode in (() if args.no_kernels else
+                            (("cic_paint (atomic)", 0, 0),
+                             ("cic_paint (binned: tile sort + shared-memory tiles)", 0, 1),
+                             ("cic_paint (deterministic, tile sort)", _lib.DETERMINISTIC, binned))):
+        ctx.call("baorec_set_tune_binned", mode)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         reps = 10
         ctx.call("baorec_cic", scratch.data_ptr(), *ptr(R), nr, 0, fl)
@@ -975,6 +1015,7 @@ def run_gb300(args):
         aux[label] = {"particles_per_s": nr * 1e3 / pms, "avg_launch_ms": pms, "algorithmic_bytes": pbytes,
                       "achieved": pbytes / (pms * 1e-3) / 1e9, "unit": "GB/s", "peak": peak,
                       "frac": pbytes / (pms * 1e-3) / 1e9 / peak}
+    ctx.call("baorec_set_tune_binned", binned)
     del scratch
 
     if not args.no_kernels and args.mesh % 128 == 0:

@@ -519,6 +519,12 @@ int baorec_set_tune_stream(baorec_ctx* ctx, int stream);
  * Forms 1-6 give the same bits.  The stencil autotune times all seven. */
 int baorec_tune_pairs(const baorec_ctx* ctx);
 int baorec_set_tune_pairs(baorec_ctx* ctx, int pairs);
+/* FP32 paint (cic! / tsc! without BAOREC_DETERMINISTIC): 0 one float atomic
+ * per weight into the mesh (default), 1 binned (particles sorted by 16^3 or
+ * 32^3 mesh tile with an integer counting sort, each tile painted in shared
+ * memory and written once).  The same weights; the paint autotune times both. */
+int baorec_tune_binned(const baorec_ctx* ctx);
+int baorec_set_tune_binned(baorec_ctx* ctx, int binned);
 /* Accurate residual (double-float solution update) of the residual-driven
  * solve on the finest level: 0 blocks of 512 threads on the level's tiles
  * (default), 1 and 2 blocks of 256 threads on 32x8x8 and 32x8x16 tiles.  The

@@ -31,8 +31,9 @@ def test_cell_bins_bit_exact(n, npart):
     assert counts.sum() == npart
 
 
+@pytest.mark.parametrize("binned", [True, False])
 @pytest.mark.parametrize("wrap", [True, False])
-def test_cic_matches_oracle(wrap):
+def test_cic_matches_oracle(wrap, binned):
     import baorec
     n, npart = 32, 40000
     L = F32(500.0)
@@ -44,7 +45,7 @@ def test_cic_matches_oracle(wrap):
     bs = [L] * 3
     rho = baorec.zeros_mesh((n, n, n), device=False)
     gx, gy, gz = x.copy(), y.copy(), z.copy()
-    baorec.cic_(rho, gx, gy, gz, w, bs, bmin, wrap=wrap)
+    baorec.cic_(rho, gx, gy, gz, w, bs, bmin, wrap=wrap, binned=binned)
     orho = np.zeros((n, n, n), F32)
     orho, opos = O.cic(orho, x, y, z, w, bs, bmin, wrap=wrap)
     np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(np.abs(orho).max()))
@@ -122,20 +123,21 @@ def test_cic_vector_and_scalar_reductions(shape):
         p[p >= l] = F32(0.0)
     w = (0.5 + rng.random(npart)).astype(F32)
     rho = baorec.zeros_mesh(shape, device=False)
-    baorec.cic_(rho, x.copy(), y.copy(), z.copy(), w, L, [0.0] * 3, wrap=True)
+    baorec.cic_(rho, x.copy(), y.copy(), z.copy(), w, L, [0.0] * 3, wrap=True, binned=False)
     orho, _ = O.cic(np.zeros(shape, F32), x, y, z, w, L, [0.0] * 3, wrap=True)
     np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
 
 
+@pytest.mark.parametrize("binned", [True, False])
 @pytest.mark.parametrize("wrap", [True, False])
-def test_tsc_matches_oracle(wrap):
+def test_tsc_matches_oracle(wrap, binned):
     import baorec
     n, npart = 32, 30000
     L = F32(800.0)
     x, y, z, w = uniform_box(npart, L * F32(0.8), seed=5)
     x, y, z = [(a + F32(80)).astype(F32) for a in (x, y, z)]
     rho = baorec.zeros_mesh((n, n, n), device=False)
-    baorec.tsc_(rho, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=wrap)
+    baorec.tsc_(rho, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=wrap, binned=binned)
     orho, _ = O.tsc(np.zeros((n, n, n), F32), x, y, z, w, [L] * 3, [0.0] * 3, wrap=wrap)
     np.testing.assert_allclose(rho, orho, rtol=MESH_RTOL, atol=1e-5 * float(orho.max()))
     assert abs(float(rho.sum(dtype=np.float64)) - float(w.sum(dtype=np.float64))) < 1e-4 * float(w.sum())
@@ -186,3 +188,60 @@ def test_deterministic_paint_wraps_across_the_periodic_edge():
         paint(b, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=True)
         np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-5)
         assert abs(float(np.sum(a, dtype=np.float64)) - 3000.0) < 1e-2
+
+
+@pytest.mark.parametrize("mas", ["cic", "tsc"])
+@pytest.mark.parametrize("shape,wrap", [((40, 24, 72), True), ((40, 24, 72), False), ((18, 33, 16), True),
+                                        ((256, 256, 272), True)])
+def test_binned_paint_partial_tiles_edges_and_accumulation(mas, shape, wrap):
+    """The binned paint (tile counting sort, shared-memory tiles) against the
+    oracle: meshes that are not multiples of the 16-cell tile (partial last
+    tiles), one whose 16-cell tiles exceed the shared histogram (32-cell
+    tiles), particles on tile boundaries, on the last cell of every axis (their
+    upper weights wrap to cell 0) and on the upper box edge; the paint adds to
+    the mesh it is given, as cic! does."""
+    import baorec
+    npart = 120000 if np.prod(shape) < 1e6 else 200000
+    L = [F32(10.0 * s) for s in shape]
+    rng = np.random.default_rng(sum(shape) + (7 if wrap else 0))
+    lo = 0.0 if wrap else 25.0   # TSC / CIC weights stay inside the mesh without wrapping
+    x, y, z = [(lo + rng.random(npart) * (float(L[a]) - 2 * lo)).astype(F32) for a in range(3)]
+    # tile boundaries (cells 15/16, 31/32), the last cell, the upper edge
+    k = npart // 8
+    x[:k] = (F32(10.0) * rng.choice([15.5, 16.0, 31.99, 32.0], k)).astype(F32)
+    if wrap:
+        y[k:2 * k] = (L[1] - F32(10.0) * rng.random(k, dtype=np.float32)).astype(F32)
+        z[2 * k:2 * k + 50] = L[2]
+    w = (0.25 + rng.random(npart)).astype(F32)
+    paint, ofn = (baorec.cic_, O.cic) if mas == "cic" else (baorec.tsc_, O.tsc)
+    base = (rng.random(shape) - 0.5).astype(F32)
+    rho = baorec.zeros_mesh(shape, device=False)
+    rho[...] = base
+    paint(rho, x.copy(), y.copy(), z.copy(), w, L, [0.0] * 3, wrap=wrap, binned=True)
+    orho, _ = ofn(np.zeros(shape, F32), x.copy(), y.copy(), z.copy(), w, L, [0.0] * 3, wrap=wrap)
+    got = np.asarray(rho, np.float64) - base
+    np.testing.assert_allclose(got, orho, rtol=MESH_RTOL, atol=1e-5 * float(np.abs(orho).max()))
+    assert abs(float(got.sum()) - float(w.sum(dtype=np.float64))) < 1e-4 * float(w.sum())
+
+
+def test_binned_paint_out_of_bounds_raises_and_matches_atomic():
+    """Without wrapping, a particle whose weights leave the mesh is the
+    reference's BoundsError (IndexError) in both FP32 paints; the binned and
+    atomic meshes of a valid catalogue agree to FP32 rounding."""
+    import baorec
+    n = 32
+    L = F32(320.0)
+    x, y, z, w = uniform_box(50000, L * F32(0.9), seed=13)
+    x, y, z = [(a + F32(10)).astype(F32) for a in (x, y, z)]
+    meshes = []
+    for binned in (True, False):
+        rho = baorec.zeros_mesh((n, n, n), device=False)
+        baorec.cic_(rho, x.copy(), y.copy(), z.copy(), w, [L] * 3, [0.0] * 3, wrap=False, binned=binned)
+        meshes.append(np.array(rho))
+    np.testing.assert_allclose(meshes[0], meshes[1], rtol=1e-5, atol=1e-6 * float(np.abs(meshes[1]).max()))
+    bad = x.copy()
+    bad[7] = L - F32(1.0)   # last cell: its upper CIC weight would leave the mesh
+    for binned in (True, False):
+        with pytest.raises(IndexError):
+            baorec.cic_(baorec.zeros_mesh((n, n, n), device=False), bad, y.copy(), z.copy(), w, [L] * 3,
+                        [0.0] * 3, wrap=False, binned=binned)
