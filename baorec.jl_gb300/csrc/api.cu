@@ -224,6 +224,7 @@ extern "C" int baorec_create(const baorec_config* cfg, baorec_ctx** out) {
   CKC(cudaMalloc(&ctx->ck, ctx->Nk * sizeof(cufftComplex) * 6));
   for (int a = 0; a < 3; ++a) CKC(cudaMalloc(&ctx->xvec[a], (size_t)cfg->n[a] * 4));
   CKC(cudaMalloc(&ctx->dred, kRedCapacity * sizeof(double)));
+  CKC(cudaMalloc(&ctx->dfsum, 2 * kFsumBlocks * sizeof(double)));
   CKC(cudaMallocHost(&ctx->hred, kRedCapacity * sizeof(double)));
   CKC(cudaMalloc(&ctx->derr, sizeof(unsigned)));
   CKC(cudaMallocHost(&ctx->herr, sizeof(unsigned)));
@@ -278,6 +279,7 @@ extern "C" int baorec_destroy(baorec_ctx* ctx) {
     for (int a = 0; a < 3; ++a) cudaFree(ctx->lev[l].ax[a]);
   }
   cudaFree(ctx->dred);
+  cudaFree(ctx->dfsum);
   cudaFreeHost(ctx->hred);
   cudaFree(ctx->derr);
   cudaFreeHost(ctx->herr);
@@ -387,12 +389,13 @@ static int overdensity_data(baorec_ctx* ctx, float* delta, float* x, float* y, f
 // setup_overdensity! with randoms (src/recon.jl:60-91); `ran` is a scratch mesh.
 static int overdensity_randoms(baorec_ctx* ctx, float* delta, float* ran, const float* x, const float* y,
                                const float* z, const float* w, int64_t n, const float* rx, const float* ry,
-                               const float* rz, const float* rw, int64_t nr, uint32_t flags) {
+                               const float* rz, const float* rw, int64_t nr, uint32_t flags,
+                               double* fpart = nullptr) {
   CK(cudaMemsetAsync(ran, 0, ctx->N * 4, ctx->stream));
   CKS(paint(ctx, delta, (float*)x, (float*)y, (float*)z, w, n, 0, ctx->cfg.mas, flags & ~BAOREC_WRITEBACK));
   CKS(paint(ctx, ran, (float*)rx, (float*)ry, (float*)rz, rw, nr, 0, ctx->cfg.mas, flags & ~BAOREC_WRITEBACK));
   CKS(smooth_pair(ctx, delta, ran));
-  return normalize_randoms(ctx, delta, ran, nr);
+  return normalize_randoms(ctx, delta, ran, nr, fpart);
 }
 
 struct Staged {
@@ -585,10 +588,14 @@ static int recon_multigrid(baorec_ctx* ctx, const Staged& s, int64_t n, int64_t 
   float* B = A + ctx->N;          // δ
   float* C = B + ctx->N;          // randoms
   CK(cudaMemsetAsync(B, 0, ctx->N * 4, ctx->stream));
-  if (s.rx) CKS(overdensity_randoms(ctx, B, C, s.x, s.y, s.z, s.w, n, s.rx, s.ry, s.rz, s.rw, nr, flags));
+  // the normalisation pass also sums δ and δ² for the solve that follows
+  const bool sums = s.rx && ctx->cfg.mg_mode == BAOREC_MG_CONVERGENT;
+  if (s.rx)
+    CKS(overdensity_randoms(ctx, B, C, s.x, s.y, s.z, s.w, n, s.rx, s.ry, s.rz, s.rw, nr, flags,
+                            sums ? ctx->dfsum : nullptr));
   else CKS(overdensity_data(ctx, B, (float*)s.x, (float*)s.y, (float*)s.z, s.w, n, 1, flags));
   int st = BAOREC_OK;
-  if (ctx->cfg.mg_mode == BAOREC_MG_CONVERGENT) st = mg_solve(ctx, B, A, nullptr, nullptr);
+  if (ctx->cfg.mg_mode == BAOREC_MG_CONVERGENT) st = mg_solve(ctx, B, A, nullptr, nullptr, sums ? ctx->dfsum : nullptr);
   else st = mg_fmg(ctx, B, A);
   ctx->has_result = true;
   ctx->psi_valid = false;

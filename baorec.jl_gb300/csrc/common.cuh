@@ -117,6 +117,7 @@ struct baorec_ctx {
   } tune;
   // reductions
   double* dred = nullptr;              // device FP64 partial sums
+  double* dfsum = nullptr;             // per-block (Σf, Σf²) of the normalised overdensity, for the solve
   double* hred = nullptr;              // pinned host mirror
   unsigned* derr = nullptr;            // device error word
   unsigned* herr = nullptr;            // pinned host copy
@@ -207,7 +208,9 @@ int minmax3(baorec_ctx* ctx, const float* x, const float* y, const float* z, int
 // fft.cu
 int smooth(baorec_ctx* ctx, float* mesh);
 int normalize_data(baorec_ctx* ctx, float* delta);
-int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr);
+// fpart (optional, kFsumBlocks pairs): per-block (Σδ, Σδ²) of the normalised mesh
+constexpr int kFsumBlocks = 8 * kNumSMs;
+int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr, double* fpart = nullptr);
 int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter);
 int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi3);
 int spectral_correction(baorec_ctx* ctx, const float* r, float* e);
@@ -244,7 +247,9 @@ int mg_reduce(baorec_ctx* ctx, float* coarse, const float* fine, const int nl[3]
 int mg_prolong(baorec_ctx* ctx, float* fine, const float* coarse, const int nl[3], int add);
 int mg_vcycle_ref(baorec_ctx* ctx, int lvl, float* v, const float* f);
 int mg_fmg(baorec_ctx* ctx, const float* f, float* phi);
-int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st);
+// fpart (optional): kFsumBlocks per-block (Σf, Σf²) pairs of f already on the device
+int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st,
+             const double* fpart = nullptr);
 // readout.cu
 // mode 0: shifts, 1: shifted positions, 2: one plain mesh; with p0 set a
 // second field (field2) of the same gather goes to p0..p2

@@ -276,9 +276,12 @@ __global__ void norm_data_kernel(float* __restrict__ d, size_t N, const double* 
 }
 
 // setup_overdensity! with randoms (src/recon.jl:78-85).
+// With fpart, also the block's (Σδ, Σδ²) of the written mesh in FP64 (the
+// norm and the mean the residual-driven solve needs next, without a pass of
+// its own).
 __global__ void norm_randoms_kernel(float* __restrict__ d, const float* __restrict__ r, size_t N,
                                     const double* __restrict__ part, int nb, float bias, float ran_min,
-                                    float nrand) {
+                                    float nrand, double* __restrict__ fpart) {
   __shared__ float al_s, thr_s;
   double ta, tb;
   total2(part, nb, ta, tb);
@@ -289,10 +292,28 @@ __global__ void norm_randoms_kernel(float* __restrict__ d, const float* __restri
   __syncthreads();
   const float al = al_s, thr = thr_s;
   const float bal = __fmul_rn(bias, al);
+  double s1 = 0.0, s2 = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
     float rv = r[e];
     float dv = __fsub_rn(d[e], __fmul_rn(al, rv));
-    d[e] = rv > thr ? __fdiv_rn(dv, __fmul_rn(bal, rv)) : 0.0f;
+    const float out = rv > thr ? __fdiv_rn(dv, __fmul_rn(bal, rv)) : 0.0f;
+    d[e] = out;
+    s1 += (double)out;
+    s2 += (double)out * (double)out;
+  }
+  if (!fpart) return;   // grid-uniform
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double red[2][32];
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = s1; red[1][threadIdx.x >> 5] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0.0, t2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { t1 += red[0][k]; t2 += red[1][k]; }
+    fpart[2 * blockIdx.x] = t1;
+    fpart[2 * blockIdx.x + 1] = t2;
   }
 }
 
@@ -400,11 +421,12 @@ int normalize_data(baorec_ctx* ctx, float* delta) {
   return BAOREC_OK;
 }
 
-int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr) {
+int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr, double* fpart) {
+  static_assert(kElemBlocks == (unsigned)kFsumBlocks, "one (Σδ, Σδ²) pair per block of the normalisation");
   sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, ran, ctx->N, ctx->dred);
   CKLAUNCH();
   norm_randoms_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(
-      delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr);
+      delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr, fpart);
   CKLAUNCH();
   return BAOREC_OK;
 }

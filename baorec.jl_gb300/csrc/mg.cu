@@ -802,7 +802,8 @@ int start_residual(baorec_ctx* ctx, const float* f, int start, double* rel) {
   return BAOREC_OK;
 }
 
-int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st) {
+int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, baorec_solve_stats* st,
+             const double* fpart) {
   CKS(mg_setup(ctx));
   baorec::Level& L0 = ctx->lev[0];
   const size_t N = L0.N;
@@ -821,13 +822,18 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   const bool zero_start = !phi0;
   const bool learned = !phi0 && ctx->cfg.mg_start == BAOREC_START_LEARNED;
   CK(cudaMemsetAsync(loA, 0, N * 4, ctx->stream));
-  // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²), in one pass; the host reads
-  // them when it first needs them (a zero start forms its first residual and
-  // queues its first FFT correction on the device before that)
+  // Σf, Σf² for |f - α| = sqrt(Σf² - 2αΣf + Nα²), in one pass (or from the
+  // pass that produced f: fpart); the host reads them when it first needs
+  // them (a zero start forms its first residual and queues its first FFT
+  // correction on the device before that)
   constexpr int kSumBlocks = 8 * kNumSMs;
-  sum_sumsq_partial_kernel<<<kSumBlocks, 256, 0, ctx->stream>>>(f, N, ctx->dred);
-  CKLAUNCH();
-  CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kSumBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  static_assert(kSumBlocks == kFsumBlocks, "the producer's per-block sums stand in for this pass");
+  const double* fsums = fpart ? fpart : ctx->dred;
+  if (!fpart) {
+    sum_sumsq_partial_kernel<<<kSumBlocks, 256, 0, ctx->stream>>>(f, N, ctx->dred);
+    CKLAUNCH();
+  }
+  CK(cudaMemcpyAsync(ctx->hred, fsums, 2 * kSumBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->ev_red, ctx->stream));
   double sf = 0.0, sf2 = 0.0, alpha = 0.0, fn2 = 0.0;
@@ -864,12 +870,19 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   int nspec = 0, m_last = 0;
   double rho_prev = 0.0, rate = 0.0;
   const float* pending_d = nullptr;   // last FFT correction of an outer step, not yet added to e
+  // An FFT or learned start from zero never forms r = f - α as a mesh: its
+  // first correction transforms f itself (S⁻¹ f = S⁻¹ (f - α), the mean lying
+  // outside S⁻¹'s range) and the first running residual reads f and subtracts
+  // α as it loads it, the same FP32 subtraction.
+  const bool first_from_f = zero_start && spectral && ctx->cfg.max_cycles > 0 && (tile0 || stream0);
   for (int it = 0;; ++it) {
     double s1 = 0.0, s2 = 0.0;
     bool speculative = false;
     if (it == 0 && zero_start) {
-      shift_mean_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(f, L0.f, N, ctx->dred, kSumBlocks);
-      CKLAUNCH();
+      if (!first_from_f) {
+        shift_mean_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(f, L0.f, N, fsums, kSumBlocks);
+        CKLAUNCH();
+      }
       // the first FFT correction needs only r: queue it before waiting for the sums
       if (spectral && ctx->cfg.max_cycles > 0) {
         if (learned) {
@@ -877,7 +890,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
           CKS(read_sums());
           CKS(guess_dispatch_apply(ctx, f, L0.v));
         } else {
-          CKS(spectral_correction(ctx, L0.f, L0.v));
+          CKS(spectral_correction(ctx, first_from_f ? f : L0.f, L0.v));
         }
         speculative = true;
       }
@@ -967,11 +980,15 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       for (int q = 1; q < m; ++q) {
         const float* dprev = q == 1 ? L0.v : d;
         float* acc = q == 1 ? nullptr : L0.v;
+        // the first outer step of an FFT start from zero: r_0 = f - α formed on load
+        const bool from_f = first_from_f && it == 0 && q == 1;
+        const float* src = from_f ? f : rin;
+        const float shift = from_f ? (float)alpha : 0.0f;
         if (stream0) {
-          CK(launch_resid_diff_stream(ctx->stream, dprev, rin, rout, G, acc));
+          CK(launch_resid_diff_stream(ctx->stream, dprev, src, rout, G, acc, shift));
           ctx->launches++;
         } else if (tile0) {
-          CK(launch_resid_diff(ctx->stream, dprev, rin, rout, G, acc));
+          CK(launch_resid_diff(ctx->stream, dprev, src, rout, G, acc, shift));
           ctx->launches++;
         } else {
           residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(dprev, rin, rout, G, N, acc);

@@ -139,7 +139,9 @@ cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const
 // r = rhs - shift - Ã e (clamped operator).
 // r = rhs - A e in difference form (exact operator, no clamp), accurate for
 // smooth e; with acc != nullptr also acc += e
-cudaError_t launch_resid_diff(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float* acc);
+// r = (rhs - shift) + bracket(e_nb - e_0), acc += e (optional)
+cudaError_t launch_resid_diff(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float* acc,
+                              float shift = 0.0f);
 // r = rhs - shift - A e; with acc != nullptr also acc += e
 cudaError_t launch_resid(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float shift, bool clamp,
                          float* acc = nullptr);
@@ -189,7 +191,7 @@ __device__ __forceinline__ float coef_dxy(const LG& G, float px2, float py2) {
 // the running residual with TMA-staged operands, blocks of tz planes (mg_tma.cu)
 bool resid_tma_ok(const LG& G, int tz);
 cudaError_t launch_resid_diff_tma(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
-                                  float* acc, int tz);
+                                  float* acc, int tz, float shift = 0.0f);
 
 // streaming (2.5-D, cp.async-pipelined) forms of the finest-level residuals (mg_stream.cu)
 bool stream_ok(const int n[3]);
@@ -198,7 +200,7 @@ cudaError_t launch_resid_acc_stream(cudaStream_t s, const float* hi, const float
                                     float* ohi, float* olo, float* r, const LG& G, float alpha, double* part,
                                     int* nparts);
 cudaError_t launch_resid_diff_stream(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
-                                     float* acc);
+                                     float* acc, float shift = 0.0f);
 
 // ---- cooperative coarse tail (mg_tail.cu) -----------------------------------
 constexpr int kTailMaxCells = 64 * 64 * 64;   // levels at most this big run in the tail kernel

@@ -171,7 +171,7 @@ template <bool LOCAL>
 __global__ void __launch_bounds__(NTS) resid_diff_stream_kernel(const float* __restrict__ d,
                                                                 const float* __restrict__ rin,
                                                                 float* __restrict__ rout, LG G, int zseg,
-                                                                float* __restrict__ acc) {
+                                                                float* __restrict__ acc, float shift) {
   __shared__ __align__(16) float W[NSLOT][PLANE];
   const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SYT, z0 = blockIdx.z * zseg;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(NTS) resid_diff_stream_kernel(const float* __r
                  hg * (py * pz) * ((D(sp, q + WXS) + D(sm, q - WXS)) - (D(sp, q - WXS) + D(sm, q + WXS)));
       if (LOCAL) br += (g * px) * (xp - xm) + (g * py) * (yp - ym) + (g * pz) * (zp - zm);
       const size_t o = (size_t)x + (size_t)G.n[0] * ((size_t)y + (size_t)G.n[1] * (size_t)z);
-      rout[o] = __ldg(rin + o) + br;
+      rout[o] = (__ldg(rin + o) - shift) + br;
       if (acc) acc[o] += c0;
     }
     __syncthreads();
@@ -266,11 +266,11 @@ cudaError_t launch_resid_acc_stream(cudaStream_t s, const float* hi, const float
 }
 
 cudaError_t launch_resid_diff_stream(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
-                                     float* acc) {
+                                     float* acc, float shift) {
   const int zs = zseg_of(G.n);
   const dim3 grid(G.n[0] / SX, G.n[1] / SYT, G.n[2] / zs);
-  if (G.local) resid_diff_stream_kernel<true><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc);
-  else resid_diff_stream_kernel<false><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc);
+  if (G.local) resid_diff_stream_kernel<true><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift);
+  else resid_diff_stream_kernel<false><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift);
   return cudaGetLastError();
 }
 

@@ -825,22 +825,24 @@ cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
 }
 
 template <bool LOCAL, int TZ>
-cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc,
+                    float shift) {
   auto k = resid_pairz_kernel<LOCAL, TZ>;
   constexpr size_t b = sizeof(float) * (3 * (16 + 2) * 2 * WX + WX + (16 + 2) + TZ + 2) + sizeof(int) * (16 + 2);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<dim3(G.n[0] / TX, G.n[1] / 16, G.n[2] / TZ), NT, b, s>>>(ec, rhs, r, G, 0.0f, acc);
+  k<<<dim3(G.n[0] / TX, G.n[1] / 16, G.n[2] / TZ), NT, b, s>>>(ec, rhs, r, G, shift, acc);
   return cudaGetLastError();
 }
 
 template <bool LOCAL, int TY = 16>
-cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc,
+                    float shift) {
   auto k = resid_pairs_kernel<LOCAL, TY>;
   constexpr size_t b = win_bytes<1, TY, 16>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, 16>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, 0.0f, acc);
+  k<<<grid_of<TY, 16>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, shift, acc);
   return cudaGetLastError();
 }
 
@@ -899,25 +901,26 @@ cudaError_t launch_resid(cudaStream_t s, const float* ec, const float* rhs, floa
              : resid_t<true, false, 8, 8>(s, ec, rhs, r, G, shift, acc);
 }
 
-cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc) {
+cudaError_t launch_resid_diff(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc,
+                              float shift) {
   if (G.pairs == 6 && G.n[1] % 8 == 0 && G.n[2] % 16 == 0)   // the pair kernel on 32 x 8 x 16 tiles
-    return G.local ? pairs_t<true, 8>(s, ec, rhs, r, G, acc) : pairs_t<false, 8>(s, ec, rhs, r, G, acc);
+    return G.local ? pairs_t<true, 8>(s, ec, rhs, r, G, acc, shift) : pairs_t<false, 8>(s, ec, rhs, r, G, acc, shift);
   if (G.pairs == 4 || G.pairs == 5) {   // TMA-staged operands, 64 x 16 columns of 32 (form 4) or 16 (form 5) planes
     const int tz = G.pairs == 4 ? 32 : 16;
     if (resid_tma_ok(G, tz) && ((uintptr_t)ec | (uintptr_t)rhs | (uintptr_t)acc) % 16 == 0)
-      return launch_resid_diff_tma(s, ec, rhs, r, G, acc, tz);
+      return launch_resid_diff_tma(s, ec, rhs, r, G, acc, tz, shift);
   }
   const bool big = big_tiles(G);
   if (big && G.pairs == 3 && G.n[2] % 32 == 0)
-    return G.local ? pairz_t<true, 32>(s, ec, rhs, r, G, acc) : pairz_t<false, 32>(s, ec, rhs, r, G, acc);
+    return G.local ? pairz_t<true, 32>(s, ec, rhs, r, G, acc, shift) : pairz_t<false, 32>(s, ec, rhs, r, G, acc, shift);
   if (big && (G.pairs == 2 || G.pairs == 3))
-    return G.local ? pairz_t<true, 16>(s, ec, rhs, r, G, acc) : pairz_t<false, 16>(s, ec, rhs, r, G, acc);
-  if (big && G.pairs) return G.local ? pairs_t<true>(s, ec, rhs, r, G, acc) : pairs_t<false>(s, ec, rhs, r, G, acc);
+    return G.local ? pairz_t<true, 16>(s, ec, rhs, r, G, acc, shift) : pairz_t<false, 16>(s, ec, rhs, r, G, acc, shift);
+  if (big && G.pairs) return G.local ? pairs_t<true>(s, ec, rhs, r, G, acc, shift) : pairs_t<false>(s, ec, rhs, r, G, acc, shift);
   if (!G.local)
-    return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
-               : resid_t<false, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);
-  return big ? resid_t<true, false, 16, 16, true>(s, ec, rhs, r, G, 0.0f, acc)
-             : resid_t<true, false, 8, 8, true>(s, ec, rhs, r, G, 0.0f, acc);
+    return big ? resid_t<false, false, 16, 16, true>(s, ec, rhs, r, G, shift, acc)
+               : resid_t<false, false, 8, 8, true>(s, ec, rhs, r, G, shift, acc);
+  return big ? resid_t<true, false, 16, 16, true>(s, ec, rhs, r, G, shift, acc)
+             : resid_t<true, false, 8, 8, true>(s, ec, rhs, r, G, shift, acc);
 }
 
 cudaError_t launch_resid_acc(cudaStream_t s, const float* hi, const float* lo, const float* ec, const float* f,

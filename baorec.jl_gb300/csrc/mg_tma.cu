@@ -327,7 +327,7 @@ cudaError_t encode_mesh_map(CUtensorMap* m, const float* p, const int n[3], uint
 }
 
 template <bool LOCAL>
-cudaError_t tma_t(cudaStream_t s, const ResidMaps& maps, float* rout, float* acc, const LG& G, int tz) {
+cudaError_t tma_t(cudaStream_t s, const ResidMaps& maps, float* rout, float* acc, const LG& G, int tz, float shift) {
   auto k = resid_tma_kernel<LOCAL, kRing>;
   constexpr size_t bytes = (size_t)kRing * kSlotB + 128;
   static std::mutex mu;
@@ -344,7 +344,7 @@ cudaError_t tma_t(cudaStream_t s, const ResidMaps& maps, float* rout, float* acc
     }
   }
   const dim3 grid(G.n[0] / kTX, G.n[1] / kTY, G.n[2] / tz);
-  k<<<grid, kThreadsR, bytes, s>>>(maps, rout, acc, G, 0.0f, tz, G.err, kWaitNs);
+  k<<<grid, kThreadsR, bytes, s>>>(maps, rout, acc, G, shift, tz, G.err, kWaitNs);
   return cudaGetLastError();
 }
 
@@ -356,7 +356,7 @@ bool resid_tma_ok(const LG& G, int tz) {
 }
 
 cudaError_t launch_resid_diff_tma(cudaStream_t s, const float* d, const float* rin, float* rout, const LG& G,
-                                  float* acc, int tz) {
+                                  float* acc, int tz, float shift) {
   if (!resid_tma_ok(G, tz)) return cudaErrorInvalidValue;
   for (const float* p : {d, rin, (const float*)acc})
     if ((uintptr_t)p % 16) return cudaErrorInvalidValue;
@@ -372,7 +372,7 @@ cudaError_t launch_resid_diff_tma(cudaStream_t s, const float* d, const float* r
   } else {
     m.acc = m.rin;   // not read
   }
-  return G.local ? tma_t<true>(s, m, rout, acc, G, tz) : tma_t<false>(s, m, rout, acc, G, tz);
+  return G.local ? tma_t<true>(s, m, rout, acc, G, tz, shift) : tma_t<false>(s, m, rout, acc, G, tz, shift);
 }
 
 }  // namespace baorec
