@@ -364,13 +364,13 @@ __global__ void __launch_bounds__(NT, 2) rb_sweep2_kernel(const float* __restric
 // hold every value of both stencils: the z-1 and z+1 values of (A, B) are
 // the pairs themselves, the in-plane values one register move from a pair.
 // Warp w computes window row y = 1 + w, lane l column x = XH + l.
-template <bool LOCAL, int TY>
+template <bool LOCAL, int TY, int TZ = 16>
 __global__ void __launch_bounds__(32 * TY, 32 / TY) resid_pairs_kernel(const float* __restrict__ e,
                                                                      const float* __restrict__ rhs,
                                                                      float* __restrict__ r, LG G, float shift,
                                                                      float* __restrict__ acc) {
   constexpr int NTH = 32 * TY;       // one warp per output row
-  constexpr int TZ = 16, SY = TY + 2, SZ = TZ + 2;
+  constexpr int SY = TY + 2, SZ = TZ + 2;
   constexpr int NPR = SZ / 2;        // plane pairs in the window
   constexpr int PR = 2 * WX;         // floats per row of a plane pair
   constexpr int PP = SY * PR;        // floats per plane pair
@@ -402,7 +402,8 @@ __global__ void __launch_bounds__(32 * TY, 32 / TY) resid_pairs_kernel(const flo
   __syncthreads();
   {
     constexpr int TOT = NPR * SY * CH;
-    constexpr int K = (TOT + NTH - 1) / NTH, B = K;   // every chunk of the thread in flight at once
+    // every chunk of the thread in flight at once, or in rounds of four
+    constexpr int K = (TOT + NTH - 1) / NTH, B = K <= 4 ? K : 4;
 #pragma unroll
     for (int k0 = 0; k0 < K; k0 += B) {
       float4 a[B], b[B];
@@ -835,14 +836,14 @@ cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   return cudaGetLastError();
 }
 
-template <bool LOCAL, int TY = 16>
+template <bool LOCAL, int TY = 16, int TZ = 16>
 cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r, const LG& G, float* acc,
                     float shift) {
-  auto k = resid_pairs_kernel<LOCAL, TY>;
-  constexpr size_t b = win_bytes<1, TY, 16>(1);
+  auto k = resid_pairs_kernel<LOCAL, TY, TZ>;
+  constexpr size_t b = win_bytes<1, TY, TZ>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, 16>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, shift, acc);
+  k<<<grid_of<TY, TZ>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, shift, acc);
   return cudaGetLastError();
 }
 
