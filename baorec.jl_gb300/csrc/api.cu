@@ -595,10 +595,18 @@ static int recon_multigrid(baorec_ctx* ctx, const Staged& s, int64_t n, int64_t 
                             sums ? ctx->dfsum : nullptr));
   else CKS(overdensity_data(ctx, B, (float*)s.x, (float*)s.y, (float*)s.z, s.w, n, 1, flags));
   int st = BAOREC_OK;
-  if (ctx->cfg.mg_mode == BAOREC_MG_CONVERGENT) st = mg_solve(ctx, B, A, nullptr, nullptr, sums ? ctx->dfsum : nullptr);
-  else st = mg_fmg(ctx, B, A);
+  ctx->psi_ahead = false;
+  if (ctx->cfg.mg_mode == BAOREC_MG_CONVERGENT) {
+    ctx->want_psi_ahead = true;
+    st = mg_solve(ctx, B, A, nullptr, nullptr, sums ? ctx->dfsum : nullptr);
+    ctx->want_psi_ahead = false;
+  } else {
+    st = mg_fmg(ctx, B, A);
+  }
   ctx->has_result = true;
-  ctx->psi_valid = false;
+  // the solve's last step computed the displacement of the returned solution
+  ctx->psi_valid = st == BAOREC_OK && ctx->psi_ahead;
+  ctx->psi_ahead = false;
   return st;
 }
 

@@ -74,6 +74,10 @@ struct baorec_ctx {
   bool has_result = false;
   float* psi = nullptr;                // 6 real meshes (displacements / iterative parts)
   bool psi_valid = false;              // psi[0..2] hold the displacement of `result`
+  // set by the composed reconstruction: the solve computes the displacement
+  // of its last iterate while the host reads the final residual (psi_ahead:
+  // it did, and that iterate is the solution)
+  bool want_psi_ahead = false, psi_ahead = false;
   cudaEvent_t ev_red = nullptr;          // the solve's partial sums have reached the host
   // chunked host read-out: copy-in and copy-out streams beside `stream`, the
   // events that order them per staging slot, and the double-buffered staging

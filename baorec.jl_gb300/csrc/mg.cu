@@ -917,18 +917,31 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       // nothing the host decides (it writes only the correction lev[0].v; a
       // V-cycle zeroes that first).  Skipped when the last step's rate says
       // this residual is already below rtol.
+      bool predicted_done = false;
       if (spectral && nspec < ctx->cfg.max_cycles) {
         const double predicted = m_last > 0 ? rho_prev * pow(std::max(rate, 0.0), (double)m_last) : 1.0;
-        speculative = !(m_last > 0 && rate > 0.0 && predicted <= (double)ctx->cfg.rtol);
+        predicted_done = m_last > 0 && rate > 0.0 && predicted <= (double)ctx->cfg.rtol;
+        speculative = !predicted_done;
       }
+      bool psi_now = false;
       if (speculative) {
         if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
         CK(cudaEventRecord(ctx->ev_red, ctx->stream));
         CKS(spectral_correction(ctx, L0.f, L0.v));
         CK(cudaEventSynchronize(ctx->ev_red));
+      } else if (ctx->want_psi_ahead && predicted_done) {
+        // predicted converged: the displacement of this iterate (the hi part
+        // just written) runs while the host reads the residual; it stands if
+        // the solve stops here
+        if (!ctx->ev_red) CK(cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming));
+        CK(cudaEventRecord(ctx->ev_red, ctx->stream));
+        CKS(displacement_meshes(ctx, hiB, ctx->psi));
+        CK(cudaEventSynchronize(ctx->ev_red));
+        psi_now = true;
       } else {
         CK(cudaStreamSynchronize(ctx->stream));
       }
+      ctx->psi_ahead = psi_now;
       for (int q = 0; q < nparts; ++q) { s1 += ctx->hred[2 * q]; s2 += ctx->hred[2 * q + 1]; }
       { float* t = hiA; hiA = hiB; hiB = t; t = loA; loA = loB; loB = t; }
     }
