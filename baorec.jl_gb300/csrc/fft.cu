@@ -292,11 +292,26 @@ __global__ void norm_randoms_kernel(float* __restrict__ d, const float* __restri
   __syncthreads();
   const float al = al_s, thr = thr_s;
   const float bal = __fmul_rn(bias, al);
+  auto norm = [&](float dv0, float rv) {
+    const float dv = __fsub_rn(dv0, __fmul_rn(al, rv));
+    return rv > thr ? __fdiv_rn(dv, __fmul_rn(bal, rv)) : 0.0f;
+  };
+  // four cells per step (16-byte accesses); their sums in FP32, then FP64
   double s1 = 0.0, s2 = 0.0;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
-    float rv = r[e];
-    float dv = __fsub_rn(d[e], __fmul_rn(al, rv));
-    const float out = rv > thr ? __fdiv_rn(dv, __fmul_rn(bal, rv)) : 0.0f;
+  const size_t N4 = ((uintptr_t)d % 16 == 0 && (uintptr_t)r % 16 == 0) ? N / 4 : 0;
+  float4* d4 = reinterpret_cast<float4*>(d);
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
+    const float4 dv = d4[e], rv = r4[e];
+    const float4 o = make_float4(norm(dv.x, rv.x), norm(dv.y, rv.y), norm(dv.z, rv.z), norm(dv.w, rv.w));
+    d4[e] = o;
+    if (fpart) {
+      s1 += (double)((o.x + o.y) + (o.z + o.w));
+      s2 += (double)((o.x * o.x + o.y * o.y) + (o.z * o.z + o.w * o.w));
+    }
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    const float out = norm(d[e], r[e]);
     d[e] = out;
     s1 += (double)out;
     s2 += (double)out * (double)out;
