@@ -214,15 +214,23 @@ __global__ void sum2_partial_kernel(const float* __restrict__ a, const float* __
   const size_t N4 = vec ? N / 4 : 0;
   const float4* a4 = reinterpret_cast<const float4*>(a);
   const float4* b4 = reinterpret_cast<const float4*>(b);
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += (size_t)gridDim.x * blockDim.x) {
-    const float4 u = a4[e];
-    sa += (double)((u.x + u.y) + (u.z + u.w));
-    if (b) {
-      const float4 w = b4[e];
-      sb += (double)((w.x + w.y) + (w.z + w.w));
+  // four 16-byte loads per array in flight per thread before their sums join
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e0 < N4; e0 += 4 * stride) {
+    float4 u[4], w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const size_t e = e0 + k * stride;
+      u[k] = e < N4 ? a4[e] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      w[k] = (b && e < N4) ? b4[e] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      sa += (double)((u[k].x + u[k].y) + (u[k].z + u[k].w));
+      sb += (double)((w[k].x + w[k].y) + (w[k].z + w[k].w));
     }
   }
-  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += stride) {
     sa += (double)a[e];
     if (b) sb += (double)b[e];
   }
@@ -270,9 +278,16 @@ __global__ void norm_data_kernel(float* __restrict__ d, size_t N, const double* 
   total2(part, nb, ta, tb);
   if (threadIdx.x == 0) mean_s = (float)(ta / (double)N);
   __syncthreads();
-  float mean = mean_s;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    d[e] = __fdiv_rn(__fsub_rn(__fdiv_rn(d[e], mean), 1.0f), bias);
+  const float mean = mean_s;
+  auto norm = [&](float v) { return __fdiv_rn(__fsub_rn(__fdiv_rn(v, mean), 1.0f), bias); };
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t N4 = (uintptr_t)d % 16 == 0 ? N / 4 : 0;   // four cells per 16-byte access
+  float4* d4 = reinterpret_cast<float4*>(d);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N4; e += stride) {
+    const float4 v = d4[e];
+    d4[e] = make_float4(norm(v.x), norm(v.y), norm(v.z), norm(v.w));
+  }
+  for (size_t e = 4 * N4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += stride) d[e] = norm(d[e]);
 }
 
 // setup_overdensity! with randoms (src/recon.jl:78-85).
