@@ -594,9 +594,14 @@ int mg_jacobi(baorec_ctx* ctx, float* v, const float* f, const int nl[3], int ni
   size_t N = ctx->lev[l].N;
   float* a = v;
   float* b = tmp;
+  const bool tiled = tile_ok(ctx->lev[l].n) && (uintptr_t)v % 16 == 0 && (uintptr_t)tmp % 16 == 0;
   for (int s = 0; s < niter; ++s) {
-    jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, f, b, G, ctx->cfg.jacobi_damping_factor, N);
-    CKLAUNCH();
+    if (tiled) {
+      CK(launch_jacobi(ctx->stream, a, f, b, G, ctx->cfg.jacobi_damping_factor));
+    } else {
+      jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, f, b, G, ctx->cfg.jacobi_damping_factor, N);
+      CKLAUNCH();
+    }
     float* t = a; a = b; b = t;
   }
   if (a != v) CK(cudaMemcpyAsync(v, a, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -607,8 +612,12 @@ int mg_residual(baorec_ctx* ctx, float* r, const float* v, const float* f, const
   int l = level_of(ctx, nl);
   if (l < 0) return set_error(ctx, BAOREC_ERR_ARG, "residual: %dx%dx%d is not a level of this mesh", nl[0], nl[1], nl[2]);
   LG G = level_geom(ctx, l, 0.0f);
-  residual_kernel<<<blocks_for(ctx->lev[l].N), 256, 0, ctx->stream>>>(v, f, r, G, ctx->lev[l].N, 0.0f);
-  CKLAUNCH();
+  if (tile_ok(ctx->lev[l].n) && (uintptr_t)v % 16 == 0) {
+    CK(launch_ref_residual(ctx->stream, v, f, r, G, 0.0f));
+  } else {
+    residual_kernel<<<blocks_for(ctx->lev[l].N), 256, 0, ctx->stream>>>(v, f, r, G, ctx->lev[l].N, 0.0f);
+    CKLAUNCH();
+  }
   return BAOREC_OK;
 }
 
@@ -1072,11 +1081,18 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
       launch_resid_diff(ctx->stream, L.v, L.f, t, G, L.r);
     else if (which == 3)
       residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, N, L.r);
+    else if (which == 6)
+      vcycle_rb(ctx, 0, 0.0f);
+    else if (which == 7)
+      mg_vcycle_ref(ctx, 0, L.v, L.f);
+    else if (tile_ok(L.n))
+      launch_jacobi(ctx->stream, L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor);
     else
       jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
   };
-  if (which < 0 || which > 5) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
-  if (which >= 4 && !stream_ok(L.n)) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: no streaming form here");
+  if (which < 0 || which > 7) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  if ((which == 4 || which == 5) && !stream_ok(L.n))
+    return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: no streaming form here");
   launch();   // warm-up
   CK(cudaEventRecord(a, ctx->stream));
   for (int r = 0; r < reps; ++r) launch();
@@ -1095,5 +1111,15 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   // residual of the FFT corrections reads d, r, acc and writes r, acc (20 B/cell)
   *bytes = which == 0 ? (tile_ok(L.n) ? 12.0 : 6.0) * N : (which == 1 || which == 4) ? 28.0 * N
           : (which == 3 || which == 5) ? 20.0 * N : 12.0 * N;
+  if (which == 6 || which == 7) {
+    // a V-cycle: on every level its sweeps (12 B/cell each: read v and f,
+    // write v), the residual (12 B/cell), the restriction (4 B/cell read, 0.5
+    // written) and the prolongation (read 0.5, read and write v: 8.5 B/cell);
+    // the coarsest level's sweeps are counted like the others
+    const double sweeps = which == 6 ? ctx->cfg.nu1 + ctx->cfg.nu2 : 2.0 * ctx->cfg.jacobi_niterations;
+    double b = 0.0;
+    for (int l = 0; l < ctx->nlev; ++l) b += (double)ctx->lev[l].N * (12.0 * sweeps + 12.0 + 4.5 + 8.5);
+    *bytes = b;
+  }
   return BAOREC_OK;
 }

@@ -139,6 +139,10 @@ cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const
 // r = rhs - shift - Ã e (clamped operator).
 // r = rhs - A e in difference form (exact operator, no clamp), accurate for
 // smooth e; with acc != nullptr also acc += e
+// one damped-Jacobi sweep of the reference schedule on shared-memory tiles (tile_ok meshes)
+cudaError_t launch_jacobi(cudaStream_t s, const float* v, const float* f, float* out, const LG& G, float omega);
+// r = (f - shift) - A v of the reference schedule on shared-memory tiles (tile_ok meshes)
+cudaError_t launch_ref_residual(cudaStream_t s, const float* v, const float* f, float* r, const LG& G, float shift);
 // r = (rhs - shift) + bracket(e_nb - e_0), acc += e (optional)
 cudaError_t launch_resid_diff(cudaStream_t s, const float* e, const float* rhs, float* r, const LG& G, float* acc,
                               float shift = 0.0f);

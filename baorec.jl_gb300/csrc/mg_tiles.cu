@@ -57,16 +57,16 @@ __device__ __forceinline__ void row_table(int* __restrict__ ro, int y0, int z0, 
 }
 
 // Window chunks: s[row][4c .. 4c+3] = g[row offset + wrap(x0 - XH + 4c) ..].
-template <int HY, int TY, int TZ>
+template <int HY, int TY, int TZ, int NTB = NT>
 __device__ __forceinline__ void load_rows(float* __restrict__ s, const int* __restrict__ ro, const float* __restrict__ g,
                                           int x0, int n0) {
   constexpr int ROWS = (TY + 2 * HY) * (TZ + 2 * HY);
-  constexpr int K = (ROWS * CH + NT - 1) / NT;   // chunks per thread, all in flight together
+  constexpr int K = (ROWS * CH + NTB - 1) / NTB;   // chunks per thread, all in flight together
   float4* s4 = reinterpret_cast<float4*>(s);
   float4 v[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    const int t = threadIdx.x + k * NT;
+    const int t = threadIdx.x + k * NTB;
     if (t < ROWS * CH) {
       const int row = t / CH, c = t - CH * row;
       v[k] = __ldg(reinterpret_cast<const float4*>(g + ro[row] + wrapi(x0 - XH + 4 * c, n0)));
@@ -74,7 +74,7 @@ __device__ __forceinline__ void load_rows(float* __restrict__ s, const int* __re
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    const int t = threadIdx.x + k * NT;
+    const int t = threadIdx.x + k * NTB;
     if (t < ROWS * CH) s4[t] = v[k];
   }
 }
@@ -191,6 +191,59 @@ __global__ void __launch_bounds__(NT) resid_kernel(const float* __restrict__ e, 
     else
       r[o] = (rv - shift) - (cf.diag * sv[q] - nbr<LOCAL, SXY>(sv, q, cf));
     if (acc) acc[o] = av + sv[q];   // optional: accumulate the operand into a running sum
+  }
+}
+
+// The reference schedule's stencils on 32 x TY x TZ tiles of NTH threads, with
+// the per-cell arithmetic of jacobi_kernel / residual_kernel (coef_at, the
+// neighbours in gather's order, offdiag) and the neighbours read from the
+// tile window instead of global memory:
+//   JACOBI  one damped-Jacobi sweep (src/multigrid.jl:137-191, 207),
+//           out = (1-ω) v + ω (f + bracket(v)) / diag;
+//   else    the residual (src/multigrid.jl:328-376, 393),
+//           out = (f - shift) - (diag v - bracket(v)), shift passed as omega.
+template <int TY, int TZ, int NTH, bool JACOBI>
+__global__ void __launch_bounds__(NTH, 1024 / NTH) jacobi_tile_kernel(const float* __restrict__ v,
+                                                                     const float* __restrict__ f,
+                                                                     float* __restrict__ out, LG G, float omega) {
+  constexpr int SY = TY + 2, SZ = TZ + 2, SXY = WX * SY, NW = NTH / 32;
+  extern __shared__ __align__(16) float smem[];
+  float* sv = smem;
+  int* ro = reinterpret_cast<int*>(sv + WX * SY * SZ);
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  using RP = RowPrefetch<TY, TZ, NW>;
+  RP pf;
+#pragma unroll
+  for (int i = 0; i < RP::PF; ++i) pf.issue(i, f, warp, lane, x0, y0, z0, G.n);
+  row_table<1, TY, TZ, NTH>(ro, y0, z0, G.n);
+  __syncthreads();
+  load_rows<1, TY, TZ, NTH>(sv, ro, v, x0, G.n[0]);
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < RP::RPW; ++i) {
+    const int row = warp + i * NW;
+    if (row >= TY * TZ) break;
+    const float fv = pf.v[i % RP::PF];
+    pf.issue(i + RP::PF, f, warp, lane, x0, y0, z0, G.n);
+    const int ly = 1 + row % TY, lz = 1 + row / TY, lx = XH + lane;
+    const int q = lx + WX * ly + SXY * lz;
+    const Coef c = coef_at(G, x0 + lane, y0 + ly - 1, z0 + lz - 1);
+    Nb b;
+    b.xp = sv[q + 1]; b.xm = sv[q - 1];
+    b.yp = sv[q + WX]; b.ym = sv[q - WX];
+    b.zp = sv[q + SXY]; b.zm = sv[q - SXY];
+    b.pp0 = sv[q + 1 + WX]; b.mm0 = sv[q - 1 - WX]; b.mp0 = sv[q - 1 + WX]; b.pm0 = sv[q + 1 - WX];
+    b.p0p = sv[q + 1 + SXY]; b.m0m = sv[q - 1 - SXY]; b.m0p = sv[q - 1 + SXY]; b.p0m = sv[q + 1 - SXY];
+    b._pp = sv[q + WX + SXY]; b._mm = sv[q - WX - SXY]; b._mp = sv[q - WX + SXY]; b._pm = sv[q + WX - SXY];
+    if (JACOBI) {
+      float jac = fv + offdiag(c, b, G.local);
+      jac /= 2.0f * (c.gpx + c.gpy + c.gpz);
+      out[ro[ly + SY * lz] + x0 + lane] = (1.0f - omega) * sv[q] + omega * jac;
+    } else {
+      const float av = 2.0f * (c.gpx + c.gpy + c.gpz) * sv[q] - offdiag(c, b, G.local);
+      out[ro[ly + SY * lz] + x0 + lane] = (fv - omega) - av;
+    }
   }
 }
 
@@ -877,6 +930,27 @@ int tile_blocks(const LG& G) {
   if (f == 2) return (n[0] / TX) * (n[1] / 8) * (n[2] / 16);
   if (f == 1) return (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
   return big_tiles(G) ? (n[0] / TX) * (n[1] / 16) * (n[2] / 16) : (n[0] / TX) * (n[1] / 8) * (n[2] / 8);
+}
+
+template <bool JACOBI>
+cudaError_t ref_stencil_t(cudaStream_t s, const float* v, const float* f, float* out, const LG& G, float w) {
+  auto run = [&](auto k, dim3 grid, size_t b) {
+    cudaError_t e = allow_smem(k, b);
+    if (e != cudaSuccess) return e;
+    k<<<grid, 256, b, s>>>(v, f, out, G, w);
+    return cudaGetLastError();
+  };
+  if (G.n[2] % 16 == 0)
+    return run(jacobi_tile_kernel<8, 16, 256, JACOBI>, grid_of<8, 16>(G.n), win_bytes<1, 8, 16>(1));
+  return run(jacobi_tile_kernel<8, 8, 256, JACOBI>, grid_of<8, 8>(G.n), win_bytes<1, 8, 8>(1));
+}
+
+cudaError_t launch_jacobi(cudaStream_t s, const float* v, const float* f, float* out, const LG& G, float omega) {
+  return ref_stencil_t<true>(s, v, f, out, G, omega);
+}
+
+cudaError_t launch_ref_residual(cudaStream_t s, const float* v, const float* f, float* r, const LG& G, float shift) {
+  return ref_stencil_t<false>(s, v, f, r, G, shift);
 }
 
 cudaError_t launch_rb_sweep(cudaStream_t s, const float* vin, float* vout, const float* rhs, const LG& G, float shift,

@@ -961,6 +961,16 @@ def run_gb300(args):
                 "avg_launch_ms": avg.value, "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
         ctx.call("baorec_set_tune_pairs", chosen)
         meas["pair_forms"] = forms
+    # V-cycles/s: one V-cycle of the residual-driven solve (the plain start's
+    # step) and one of the reference's schedule (vcycle!), on the finest level
+    vcycles = {}
+    for which, label in (() if args.no_kernels else ((6, "residual-driven (red-black 2+2, every level)"),
+                                                     (7, "reference vcycle! (damped Jacobi 5+5, every level)"))):
+        avg, nbytes = C.c_float(), C.c_double()
+        ctx.call("baorec_profile_kernel", which, 10, C.byref(avg), C.byref(nbytes))
+        vcycles[label] = {"per_s": 1000.0 / avg.value, "ms": avg.value, "algorithmic_bytes": nbytes.value,
+                          "achieved": nbytes.value / (avg.value * 1e-3) / 1e9, "unit": "GB/s", "peak": peak,
+                          "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
     head = 0 if args.start == "zero" else (5 if tune.get("stream_residuals", -1) != 0 else 3)
     roofline, aux = None, {}
     if meas:
@@ -1077,6 +1087,7 @@ def run_gb300(args):
             "clocks": clk,
             "roofline": roofline,
             "kernels": aux,
+            "vcycles": vcycles,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "batch": batch,

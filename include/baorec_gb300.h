@@ -225,7 +225,13 @@ int baorec_mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* ph
  * algorithmic bytes per launch.  which: 0 = red-black sweep (both colours),
  * 1 = accurate residual with solution update, 2 = damped-Jacobi sweep
  * (reference schedule), 3 = FP32 difference-form running residual of the FFT
- * corrections.  Needs a multigrid context. */
+ * corrections, 4 and 5 = the streaming forms of 1 and 3, 6 = one V-cycle of
+ * the residual-driven solve (nu1 + nu2 red-black sweeps per level, the small
+ * levels in one cooperative kernel, FP64 coarsest solve), 7 = one V-cycle of
+ * the reference schedule (vcycle!: jacobi_niterations damped-Jacobi sweeps
+ * before and after on every level); for 6 and 7 the bytes are those of every
+ * level's sweeps, residual, restriction and prolongation.  Needs a multigrid
+ * context. */
 int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch);
 
 /* Statistics of the context's last residual-driven solve. */

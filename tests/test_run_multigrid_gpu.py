@@ -128,3 +128,43 @@ def test_run_reference_schedule_matches_fp32_oracle():
     worst64 = max(float(np.max(np.abs(g[a] - r[a]))) for g, r in zip(got, ref64) for a in range(3))
     print("reference-schedule run! max |dpos| vs FP32 oracle FMG", worst, "vs FP64 FMG", worst64)
     assert worst < 1e-3 and worst64 < 1e-3
+
+
+@pytest.mark.parametrize("start", ["spectral", "zero"])
+def test_displacement_of_the_solve_equals_recomputed(start):
+    """The composed reconstruction computes the displacement of its last
+    iterate while the host reads the final residual (FFT start, convergence
+    predicted); the positions read out with it through the C ABI are the bits
+    of the positions read out after the same potential is set again (the
+    displacement recomputed)."""
+    import torch
+    import baorec
+    from baorec import _lib
+    n = 64
+    m = small_lightcone(n_data=40000, rand_factor=5, n_grid=n, seed=33)
+    bs, bm = O.setup_box(m.rx, m.ry, m.rz, 25.0 * 256 / n)
+    rec = baorec.MultigridRecon(bias=BIAS, f=GROWTH, smoothing_radius=R, box_size=bs, box_min=bm, los=None,
+                                mg_mode="convergent", rtol=1e-6, start=start)
+    ctx = baorec.setup_fft_(rec, (n,) * 3)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    X = [d(a) for a in (m.x, m.y, m.z, m.w)]
+    Rr = [d(a) for a in (m.rx, m.ry, m.rz, m.rw)]
+    p = lambda ts: [t.data_ptr() for t in ts]
+    nd, nr = int(m.x.size), int(m.rx.size)
+    torch.cuda.synchronize()
+    assert ctx.status("baorec_reconstructed_potential", *p(X), nd, *p(Rr), nr, 0) == _lib.OK
+    assert ctx.solve_stats()["rel_residual"] <= 1e-6
+
+    def positions():
+        out = [torch.empty(nr, device="cuda") for _ in range(6)]
+        ctx.call("baorec_reconstructed_positions2", *p(Rr)[:3], nr, _lib.FIELD["sum"], *p(out[:3]),
+                 _lib.FIELD["disp"], *p(out[3:]), 0)
+        return [o.cpu().numpy() for o in out]
+
+    first = positions()
+    phi = torch.empty(n ** 3, device="cuda")
+    ctx.call("baorec_get_result", phi.data_ptr(), 0)
+    ctx.call("baorec_set_result", phi.data_ptr(), 0)   # the displacement is recomputed from the same φ
+    again = positions()
+    for u, v in zip(first, again):
+        np.testing.assert_array_equal(u.view(np.uint32), v.view(np.uint32))
