@@ -78,6 +78,23 @@ def parse():
     return ap.parse_args()
 
 
+def replica_seed(base, rank):
+    """Each replica reconstructs its own mock: the base seed plus its rank."""
+    return base + rank
+
+
+def replica_throughput(ms, ws, dist=None, device="cuda"):
+    """Replicas only (one reconstruction never shards): the slowest rank's
+    time per step, taken over all ranks, and the whole job's reconstructions
+    per second, ws of them per step.  Returns (ms_max, recons_per_s)."""
+    if dist is not None and ws > 1:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, ws * 1000.0 / ms
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -832,7 +849,7 @@ def run_gb300(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    m, bs, bm = workload(args, args.seed + rank)
+    m, bs, bm = workload(args, replica_seed(args.seed, rank))
     n = (args.mesh,) * 3
     weights = os.path.join(ROOT, "baorec.jl_gb300", "weights", "guess_lightcone.npy")
 
@@ -911,11 +928,8 @@ def run_gb300(args):
         torch.cuda.synchronize()
         clk = clocks.stop()
         launches = c.launches() - l0
-        ms = ev0.elapsed_time(ev1) / args.steps
+        ms, _ = replica_throughput(ev0.elapsed_time(ev1) / args.steps, ws, dist)
         if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
             dist.barrier()
         return ms, hist, clk, launches, c.solve_stats()
 
