@@ -94,6 +94,7 @@ _SIGS = {
     "baorec_get_box": (C.c_int, [P, F3, F3]),
     "baorec_stream": (P, [P]),
     "baorec_kernel_launches": (I64, [P]),
+    "baorec_total_kernel_launches": (I64, []),
     "baorec_result_ptr": (P, [P]),
     "baorec_setup_box": (C.c_int, [P, P, P, P, I64, C.c_float, U32, F3, F3]),
     "baorec_setup_box_noalloc": (C.c_int, [P, P, P, I64, C.c_float, P, F3, F3]),
@@ -262,6 +263,10 @@ class Context:
 
     def launches(self) -> int:
         return int(self.lib.baorec_kernel_launches(self.h))
+
+    def total_launches(self) -> int:
+        """This library's kernel launches in the process so far (every context)."""
+        return int(self.lib.baorec_total_kernel_launches())
 
     def box(self):
         bs, bm = F3(), F3()

@@ -1,5 +1,6 @@
 // C ABI: context lifetime, staging, error reporting and the reconstruction
 // drivers (run!, setup_overdensity!, read_shifts, ...) of src/recon.jl.
+#include <atomic>
 #include <math.h>
 #include <stdarg.h>
 
@@ -306,6 +307,15 @@ extern "C" const char* baorec_last_error(const baorec_ctx* ctx) { return ctx ? c
 extern "C" void* baorec_stream(baorec_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 extern "C" int64_t baorec_kernel_launches(const baorec_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+namespace baorec {
+static std::atomic<int64_t> g_kernel_launches{0};
+int64_t count_launch() { return g_kernel_launches.fetch_add(1, std::memory_order_relaxed) + 1; }
+}  // namespace baorec
+
+extern "C" int64_t baorec_total_kernel_launches(void) {
+  return baorec::g_kernel_launches.load(std::memory_order_relaxed);
+}
 
 extern "C" float* baorec_result_ptr(baorec_ctx* ctx) { return ctx && ctx->has_result ? ctx->result : nullptr; }
 

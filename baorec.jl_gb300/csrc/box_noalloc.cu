@@ -141,9 +141,9 @@ extern "C" int baorec_setup_box_noalloc(const float* x, const float* y, const fl
   float* part = nullptr;
   if (scratch_for_current_device(&part) != cudaSuccess) return BAOREC_ERR_CUDA;
   const int nblocks = (int)((n + (int64_t)kThreads * kItemsPerThread - 1) / ((int64_t)kThreads * kItemsPerThread));
-  box_partial_noalloc_kernel<<<nblocks, kThreads, 0, s>>>(x, y, z, n, part);
+  (box_partial_noalloc_kernel<<<nblocks, kThreads, 0, s>>>(x, y, z, n, part), ::baorec::count_launch());
   if (cudaGetLastError() != cudaSuccess) return BAOREC_ERR_CUDA;
-  box_final_noalloc_kernel<<<1, kThreads, 0, s>>>(part, nblocks);
+  (box_final_noalloc_kernel<<<1, kThreads, 0, s>>>(part, nblocks), ::baorec::count_launch());
   if (cudaGetLastError() != cudaSuccess) return BAOREC_ERR_CUDA;
   float h[6];
   if (cudaMemcpyAsync(h, part + kFinal, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return BAOREC_ERR_CUDA;

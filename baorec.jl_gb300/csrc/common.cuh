@@ -156,6 +156,11 @@ inline unsigned grid_for(size_t n, int block) {
 
 #define BAOREC_LAUNCHED(c) ((c)->launches++)
 
+// Process-wide count of this library's kernel launches (every context, the
+// launches captured into a batch graph counted once): each launch site is
+// the expression (kernel<<<...>>>(...), count_launch()).
+int64_t count_launch();
+
 #define CK(call)                                                         \
   do {                                                                   \
     cudaError_t _e = (call);                                             \

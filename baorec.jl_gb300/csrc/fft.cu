@@ -352,7 +352,7 @@ constexpr int kRedBlocks = 2 * kNumSMs;
 }  // namespace
 
 int sum_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
-  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, nullptr, N, ctx->dred);
+  (sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, nullptr, N, ctx->dred), ::baorec::count_launch());
   CKLAUNCH();
   CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * kRedBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -384,7 +384,7 @@ __global__ void sumsq_partial_kernel(const float* __restrict__ a, size_t N, doub
 }
 
 int sumsq_mesh(baorec_ctx* ctx, const float* m, size_t N, double* out) {
-  sumsq_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, N, ctx->dred);
+  (sumsq_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(m, N, ctx->dred), ::baorec::count_launch());
   CKLAUNCH();
   CK(cudaMemcpyAsync(ctx->hred, ctx->dred, kRedBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -421,7 +421,7 @@ int smooth(baorec_ctx* ctx, float* mesh) {
   KGeom g = kgeom_of(ctx);
   float R = ctx->cfg.smoothing_radius;
   CKFFT(cufftExecR2C(ctx->plan_r2c, mesh, ctx->ck));
-  gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 1, ctx->Nk, g, R * R);
+  (gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 1, ctx->Nk, g, R * R), ::baorec::count_launch());
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, mesh));
   return BAOREC_OK;
@@ -437,26 +437,26 @@ int smooth_pair(baorec_ctx* ctx, float* a, float* b) {
   KGeom g = kgeom_of(ctx);
   float R = ctx->cfg.smoothing_radius;
   CKFFT(cufftExecR2C(ctx->plan_r2c2, a, ctx->ck));
-  gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 2, ctx->Nk, g, R * R);
+  (gauss_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, 2, ctx->Nk, g, R * R), ::baorec::count_launch());
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r2, ctx->ck, a));
   return BAOREC_OK;
 }
 
 int normalize_data(baorec_ctx* ctx, float* delta) {
-  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, nullptr, ctx->N, ctx->dred);
+  (sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, nullptr, ctx->N, ctx->dred), ::baorec::count_launch());
   CKLAUNCH();
-  norm_data_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(delta, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias);
+  (norm_data_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(delta, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
 
 int normalize_randoms(baorec_ctx* ctx, float* delta, const float* ran, int64_t nr, double* fpart) {
   static_assert(kElemBlocks == (unsigned)kFsumBlocks, "one (Σδ, Σδ²) pair per block of the normalisation");
-  sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, ran, ctx->N, ctx->dred);
+  (sum2_partial_kernel<<<kRedBlocks, 256, 0, ctx->stream>>>(delta, ran, ctx->N, ctx->dred), ::baorec::count_launch());
   CKLAUNCH();
-  norm_randoms_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(
-      delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr, fpart);
+  (norm_randoms_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(
+      delta, ran, ctx->N, ctx->dred, kRedBlocks, ctx->cfg.bias, ctx->cfg.ran_min, (float)nr, fpart), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -476,8 +476,8 @@ int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter) {
       if (ctx->cfg.los[a] != 0.0f) { mask |= 1 << a; ++nprod; }
   }
   CKFFT(cufftExecR2C(ctx->plan_r2c, delta_r, ctx->ck));
-  hessian_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->ck, ctx->Nk, g, local ? 1 : 0,
-                                                                  los, nprod, mask);
+  (hessian_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck, ctx->ck, ctx->Nk, g, local ? 1 : 0,
+                                                                  los, nprod, mask), ::baorec::count_launch());
   CKLAUNCH();
   if (nprod == 6) {
     CKFFT(cufftExecC2R(ctx->plan_c2r6, ctx->ck, ctx->psi));
@@ -485,9 +485,9 @@ int iterate(baorec_ctx* ctx, float* delta_r, const float* delta_s, int iter) {
     for (int m = 0; m < nprod; ++m)
       CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck + (size_t)m * ctx->Nk, ctx->psi + (size_t)m * ctx->N));
   }
-  iterate_update_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(
+  (iterate_update_kernel<<<grid_for(ctx->N, 256), 256, 0, ctx->stream>>>(
       delta_r, delta_s, ctx->psi, ctx->N, ctx->n1, ctx->n2, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2],
-      local ? 1 : 0, nprod, fac_diag, fac_off);
+      local ? 1 : 0, nprod, fac_diag, fac_off), ::baorec::count_launch());
   CKLAUNCH();
   ctx->psi_valid = false;
   return BAOREC_OK;
@@ -530,8 +530,8 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
     const int n[3] = {ctx->n1, ctx->n2, ctx->n3};
     float c2[3];
     for (int a = 0; a < 3; ++a) c2[a] = (2.0f * ctx->cfg.box_size[a]) / (float)n[a];   // FP32, as T(2L)/n
-    fd_grad_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(field, reinterpret_cast<float4*>(psi4), n[0], n[1], n[2],
-                                                         c2[0], c2[1], c2[2]);
+    (fd_grad_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(field, reinterpret_cast<float4*>(psi4), n[0], n[1], n[2],
+                                                         c2[0], c2[1], c2[2]), ::baorec::count_launch());
     CKLAUNCH();
     return BAOREC_OK;
   }
@@ -541,17 +541,17 @@ int displacement_meshes(baorec_ctx* ctx, const float* field, float* psi4) {
     CKS(xy_forward(ctx, field, ctx->ck + 3 * ctx->Nk, 1));
     CKS(zgrad_launch(ctx, ctx->ck + 3 * ctx->Nk, inv_lap));
     CKS(xy_inverse(ctx, ctx->ck, planes, 3));
-    interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
+    (interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N), ::baorec::count_launch());
     CKLAUNCH();
     return BAOREC_OK;
   }
   KGeom g = kgeom_of(ctx);
   // cuFFT's R2C reads but does not modify its input
   CKFFT(cufftExecR2C(ctx->plan_r2c, (cufftReal*)field, ctx->ck + 3 * ctx->Nk));
-  grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g, inv_lap);
+  (grad_kernel<<<grid_for(ctx->Nk, 256), 256, 0, ctx->stream>>>(ctx->ck + 3 * ctx->Nk, ctx->ck, ctx->Nk, g, inv_lap), ::baorec::count_launch());
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r3, ctx->ck, planes));
-  interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N);
+  (interleave3_kernel<<<kElemBlocks, 256, 0, ctx->stream>>>(planes, reinterpret_cast<float4*>(psi4), ctx->N), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -939,7 +939,7 @@ int zpass_launch(baorec_ctx* ctx, cufftComplex* a, const M& m, int batch) {
   const int ncols = ctx->n1h * ctx->n2;
   const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
   auto k = ctx->tune.zpass == 2 ? zpass_kernel<3, M> : zpass_kernel<1, M>;
-  k<<<dim3((ncols + kZCols - 1) / kZCols, batch), 256, 0, ctx->stream>>>(a, m, tw, ncols);
+  (k<<<dim3((ncols + kZCols - 1) / kZCols, batch), 256, 0, ctx->stream>>>(a, m, tw, ncols), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -965,7 +965,7 @@ int zgrad_launch(baorec_ctx* ctx, const cufftComplex* src, int inv_lap) {
   const int ncols = ctx->n1h * ctx->n2;
   const float2* tw = reinterpret_cast<const float2*>(ctx->stab + 2 * (ctx->n1h + ctx->n2 + ctx->n3));
   auto k = ctx->tune.zpass == 2 ? zgrad_kernel<3> : zgrad_kernel<1>;
-  k<<<(ncols + kZCols - 1) / kZCols, 256, kZGradSmem, ctx->stream>>>(src, ctx->ck, kgeom_of(ctx), inv_lap, tw, ncols);
+  (k<<<(ncols + kZCols - 1) / kZCols, 256, kZGradSmem, ctx->stream>>>(src, ctx->ck, kgeom_of(ctx), inv_lap, tw, ncols), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -1130,7 +1130,7 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
     info.n1h = g.n1h; info.n2 = g.n2; info.n3 = g.n3;
     for (int a = 0; a < 3; ++a) { info.diag[a] = g.diag[a]; info.cross[a] = g.cross[a]; }
     info.invN = g.invN;
-    set_callback_info_kernel<<<1, 1, 0, ctx->stream>>>((SpecCallbackInfo*)ctx->spec_cb, info);
+    (set_callback_info_kernel<<<1, 1, 0, ctx->stream>>>((SpecCallbackInfo*)ctx->spec_cb, info), ::baorec::count_launch());
     CKLAUNCH();
     CKFFT(cufftExecC2R(ctx->plan_c2r_spec, ctx->ck, e));
     return BAOREC_OK;
@@ -1140,7 +1140,7 @@ int spectral_correction(baorec_ctx* ctx, const float* r, float* e) {
   const int rpb = std::max(1, 1024 / ctx->n1h);
   const size_t rows = (size_t)ctx->n2 * ctx->n3;
   const unsigned blocks = (unsigned)std::min<size_t>((rows + rpb - 1) / rpb, 16 * kNumSMs);
-  spectral_inverse_kernel<<<blocks, rpb * ctx->n1h, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, rpb);
+  (spectral_inverse_kernel<<<blocks, rpb * ctx->n1h, 0, ctx->stream>>>(ctx->ck, g, ctx->stab, rpb), ::baorec::count_launch());
   CKLAUNCH();
   CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, e));
   return BAOREC_OK;

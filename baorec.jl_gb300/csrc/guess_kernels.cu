@@ -482,7 +482,7 @@ cudaError_t up_t(cudaStream_t s, const ConvArgs& a) {
   const int nx = a.n_in;
   const long long ntask = (long long)((nx + 31) / 32) * nx * nx * 4;
   const unsigned blocks = (unsigned)((ntask + kWarps - 1) / kWarps);
-  up_kernel<CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+  (up_kernel<CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -494,9 +494,9 @@ cudaError_t fwd_t(cudaStream_t s, const ConvArgs& a) {
   if (blocks < 2u * kNumSMs) {
     // a small grid (the network's n/4 level): blocks of 2 warps spread it over every SM
     constexpr int kSmall = 2;
-    conv_fwd_kernel<KIND, CIN, COUT, kSmall><<<(unsigned)((ntask + kSmall - 1) / kSmall), kSmall * 32, 0, s>>>(a);
+    (conv_fwd_kernel<KIND, CIN, COUT, kSmall><<<(unsigned)((ntask + kSmall - 1) / kSmall), kSmall * 32, 0, s>>>(a), ::baorec::count_launch());
   } else {
-    conv_fwd_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a);
+    (conv_fwd_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a), ::baorec::count_launch());
   }
   return cudaGetLastError();
 }
@@ -509,7 +509,7 @@ cudaError_t wgrad_t(cudaStream_t s, const WgradArgs& a) {
   int per = (int)((nrows + target - 1) / target);
   if (per < 1) per = 1;
   const unsigned blocks = (unsigned)((nrows + per - 1) / per);
-  wgrad_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a, per);
+  (wgrad_kernel<KIND, CIN, COUT><<<blocks, kWarps * 32, 0, s>>>(a, per), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -535,7 +535,7 @@ cudaError_t conv_wgrad(cudaStream_t s, int kind, int cin, int cout, const WgradA
 }
 
 cudaError_t weight_frags(cudaStream_t s, int kind, int cin, int cout, const float* w, uint2* frag, bool backward) {
-  frag_kernel<<<64, 256, 0, s>>>(kind, cin, cout, w, frag, backward ? 1 : 0);
+  (frag_kernel<<<64, 256, 0, s>>>(kind, cin, cout, w, frag, backward ? 1 : 0), ::baorec::count_launch());
   return cudaGetLastError();
 }
 

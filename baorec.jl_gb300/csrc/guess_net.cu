@@ -552,8 +552,8 @@ int net_forward(baorec_ctx* ctx) {
     CK(guess::conv_forward(ctx->stream, L.kind, L.cin, L.cout, a));
     ctx->launches++;
   }
-  head_fwd_kernel<<<eblocks(nvox(g, 0)), 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->out,
-                                                                 nvox(g, 0));
+  (head_fwd_kernel<<<eblocks(nvox(g, 0)), 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->out,
+                                                                 nvox(g, 0)), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -566,12 +566,12 @@ int net_loss(baorec_ctx* ctx, int kind, double* loss) {
   const size_t N = nvox(g, 0);
   if (kind == 1) {
     float* q = ctx->lev[0].r + N;   // scratch mesh
-    lap_loss_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->out, g->tgt, q, g->n, g->part);
+    (lap_loss_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->out, g->tgt, q, g->n, g->part), ::baorec::count_launch());
     CKLAUNCH();
-    lap_grad_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(q, g->dout, g->n);
+    (lap_grad_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(q, g->dout, g->n), ::baorec::count_launch());
     CKLAUNCH();
   } else {
-    loss_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->out, g->tgt, g->dout, N, g->part);
+    (loss_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->out, g->tgt, g->dout, N, g->part), ::baorec::count_launch());
     CKLAUNCH();
   }
   if (loss) {
@@ -588,15 +588,15 @@ int net_loss(baorec_ctx* ctx, int kind, double* loss) {
 int net_backward(baorec_ctx* ctx) {
   GuessNet* g = ctx->net;
   const size_t N = nvox(g, 0);
-  head_bwd_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->dout,
-                                                         g->grad[T_C0], g->grads + kP.w[kLayers], N);
+  (head_bwd_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(g->act[T_C0], g->params + kP.w[kLayers], g->dout,
+                                                         g->grad[T_C0], g->grads + kP.w[kLayers], N), ::baorec::count_launch());
   CKLAUNCH();
   for (int l = kLayers - 1; l >= 0; --l) {
     const LayerDef& L = kNet[l];
     const int ocs = kTensors[L.out_t].ch, ics = kTensors[L.in_t].ch;
     const size_t nvo = nvox(g, kTensors[L.out_t].level);
     bf16* dy = g->grad[L.out_t] + L.out_off;
-    relu_bwd_kernel<<<eblocks(nvo * L.cout / 2), 256, 0, ctx->stream>>>(dy, g->act[L.out_t] + L.out_off, ocs, L.cout, nvo);
+    (relu_bwd_kernel<<<eblocks(nvo * L.cout / 2), 256, 0, ctx->stream>>>(dy, g->act[L.out_t] + L.out_off, ocs, L.cout, nvo), ::baorec::count_launch());
     CKLAUNCH();
     guess::WgradArgs w;
     w.in = g->act[L.in_t] + L.in_off;
@@ -608,7 +608,7 @@ int net_backward(baorec_ctx* ctx) {
     w.n_out = g->n >> kTensors[L.out_t].level;
     CK(guess::conv_wgrad(ctx->stream, L.kind, L.cin, L.cout, w));
     ctx->launches++;
-    bias_grad_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(dy, ocs, L.cout, nvo, g->grads + kP.b[l]);
+    (bias_grad_kernel<<<kRedBlocksG, 256, 0, ctx->stream>>>(dy, ocs, L.cout, nvo, g->grads + kP.b[l]), ::baorec::count_launch());
     CKLAUNCH();
     if (l == 0) break;
     guess::ConvArgs a;
@@ -652,8 +652,8 @@ int net_features(baorec_ctx* ctx, const float* f, float* phs, float* rs, float* 
   mean_los(ctx, l);
   G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
   for (int a = 0; a < 3; ++a) G.l[a] = (float)l[a];
-  features_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(f, phs, rs, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], G,
-                                                       g->act[T_X], N);
+  (features_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(f, phs, rs, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], G,
+                                                       g->act[T_X], N), ::baorec::count_launch());
   CKLAUNCH();
   *s_out = s;
   return BAOREC_OK;
@@ -665,8 +665,8 @@ int net_adam(baorec_ctx* ctx, float lr, float gscale) {
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = (float)(1.0 - pow((double)b1, (double)g->adam_t));
   const float c2 = (float)(1.0 - pow((double)b2, (double)g->adam_t));
-  adam_kernel<<<eblocks(kP.total), 256, 0, ctx->stream>>>(g->params, g->grads, g->adam_m, g->adam_v, kP.total, lr,
-                                                          gscale, b1, b2, c1, c2, 1e-8f);
+  (adam_kernel<<<eblocks(kP.total), 256, 0, ctx->stream>>>(g->params, g->grads, g->adam_m, g->adam_v, kP.total, lr,
+                                                          gscale, b1, b2, c1, c2, 1e-8f), ::baorec::count_launch());
   CKLAUNCH();
   g->frags_ok = false;
   return BAOREC_OK;
@@ -695,7 +695,7 @@ int make_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, uint64_t i
   NG.slope2 = 0.5f * tc->pk_slope;
   NG.R2h = 0.5f * ctx->cfg.smoothing_radius * ctx->cfg.smoothing_radius;
   NG.seed = mix64(((uint64_t)tc->seed << 20) + index);
-  noise_kernel<<<eblocks(ctx->Nk), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, NG);
+  (noise_kernel<<<eblocks(ctx->Nk), 256, 0, ctx->stream>>>(ctx->ck, ctx->Nk, NG), ::baorec::count_launch());
   CKLAUNCH();
   float* G = ctx->psi;   // scratch
   CKFFT(cufftExecC2R(ctx->plan_c2r, ctx->ck, G));
@@ -712,8 +712,8 @@ int make_sample(baorec_ctx* ctx, const baorec_guess_train_config* tc, uint64_t i
   W.sig_rms = rms > 0.0 ? (float)(tc->sigma_g / rms) : 0.0f;
   W.half_var = 0.5f * tc->sigma_g * tc->sigma_g;
   W.ib = 1.0f / ctx->cfg.bias;
-  lognormal_window_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(G, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], W, f,
-                                                                    ctx->N);
+  (lognormal_window_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(G, ctx->xvec[0], ctx->xvec[1], ctx->xvec[2], W, f,
+                                                                    ctx->N), ::baorec::count_launch());
   CKLAUNCH();
   const baorec_config saved = ctx->cfg;
   ctx->cfg.mg_start = BAOREC_START_SPECTRAL;
@@ -754,7 +754,7 @@ int guess_apply(baorec_ctx* ctx, const float* f, float* phi0) {
   float s = 1.0f;
   CKS(net_features(ctx, f, phi0, ctx->lev[0].r, &s));
   CKS(net_forward(ctx));
-  axpy_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(phi0, ctx->net->out, s, ctx->N);
+  (axpy_kernel<<<eblocks(ctx->N), 256, 0, ctx->stream>>>(phi0, ctx->net->out, s, ctx->N), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -820,7 +820,7 @@ static int guess_eval_impl(baorec_ctx* ctx, const float* features, const float* 
   CKS(mg_setup(ctx));
   GuessNet* g = ctx->net;
   const size_t N = ctx->N;
-  f32_to_bf16_kernel<<<eblocks(N * kFeat), 256, 0, ctx->stream>>>(features, g->act[T_X], N * kFeat);
+  (f32_to_bf16_kernel<<<eblocks(N * kFeat), 256, 0, ctx->stream>>>(features, g->act[T_X], N * kFeat), ::baorec::count_launch());
   CKLAUNCH();
   CKS(net_forward(ctx));
   CK(cudaMemcpyAsync(out, g->out, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -866,7 +866,7 @@ static int guess_train_impl(baorec_ctx* ctx, const baorec_guess_train_config* tc
       CKS(net_features(ctx, f, phs, ctx->lev[0].r, &s));
       double mphi = 0.0;
       CKS(sum_mesh(ctx, phi, N, &mphi));
-      target_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(phi, phs, (float)(mphi / (double)N), 1.0f / s, g->tgt, N);
+      (target_kernel<<<eblocks(N), 256, 0, ctx->stream>>>(phi, phs, (float)(mphi / (double)N), 1.0f / s, g->tgt, N), ::baorec::count_launch());
       CKLAUNCH();
       CKS(net_forward(ctx));
       double l = 0.0;
@@ -949,7 +949,7 @@ int guess_apply_coarse(baorec_ctx* ctx, const float* f, float* phi0) {
   float s = 1.0f;
   CKS(routed(ctx, c, net_features(c, fc, phs, c->lev[0].r, &s)));
   CKS(routed(ctx, c, net_forward(c)));
-  scale_kernel<<<eblocks(c->N), 256, 0, c->stream>>>(c->net->out, s, c->N);
+  (scale_kernel<<<eblocks(c->N), 256, 0, c->stream>>>(c->net->out, s, c->N), ::baorec::count_launch());
   CK(cudaGetLastError());
   c->launches++;
   CK(cudaEventRecord(ctx->ev_guess[1], c->stream));

@@ -680,7 +680,7 @@ cudaError_t launch_tc(cudaStream_t s, const ConvArgs& c, int n) {
   a.zc = best;
   const long long units = (long long)((n + kTM - 1) / kTM) * (n / P::YR) * (n / best);
   const unsigned grid = (unsigned)(units < ctas ? units : ctas);
-  conv_tc_kernel<CIN, COUT, LOADER><<<grid, kThreads, P::SMEM, s>>>(map, a);
+  (conv_tc_kernel<CIN, COUT, LOADER><<<grid, kThreads, P::SMEM, s>>>(map, a), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -707,7 +707,7 @@ cudaError_t conv_forward_tc(cudaStream_t s, int cin, int cout, const ConvArgs& c
 }
 
 cudaError_t weight_image(cudaStream_t s, int cin, int cout, const float* w, __nv_bfloat16* img, bool backward) {
-  image_kernel<<<64, 256, 0, s>>>(cin, cout, w, img, backward ? 1 : 0);
+  (image_kernel<<<64, 256, 0, s>>>(cin, cout, w, img, backward ? 1 : 0), ::baorec::count_launch());
   return cudaGetLastError();
 }
 

@@ -599,7 +599,7 @@ int mg_jacobi(baorec_ctx* ctx, float* v, const float* f, const int nl[3], int ni
     if (tiled) {
       CK(launch_jacobi(ctx->stream, a, f, b, G, ctx->cfg.jacobi_damping_factor));
     } else {
-      jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, f, b, G, ctx->cfg.jacobi_damping_factor, N);
+      (jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, f, b, G, ctx->cfg.jacobi_damping_factor, N), ::baorec::count_launch());
       CKLAUNCH();
     }
     float* t = a; a = b; b = t;
@@ -615,7 +615,7 @@ int mg_residual(baorec_ctx* ctx, float* r, const float* v, const float* f, const
   if (tile_ok(ctx->lev[l].n) && (uintptr_t)v % 16 == 0) {
     CK(launch_ref_residual(ctx->stream, v, f, r, G, 0.0f));
   } else {
-    residual_kernel<<<blocks_for(ctx->lev[l].N), 256, 0, ctx->stream>>>(v, f, r, G, ctx->lev[l].N, 0.0f);
+    (residual_kernel<<<blocks_for(ctx->lev[l].N), 256, 0, ctx->stream>>>(v, f, r, G, ctx->lev[l].N, 0.0f), ::baorec::count_launch());
     CKLAUNCH();
   }
   return BAOREC_OK;
@@ -626,7 +626,7 @@ int mg_reduce(baorec_ctx* ctx, float* coarse, const float* fine, const int nl[3]
   int3 nf = make_int3(nl[0], nl[1], nl[2]);
   int3 nc = make_int3(nl[0] / 2, nl[1] / 2, nl[2] / 2);
   size_t Nc = (size_t)nc.x * nc.y * nc.z;
-  reduce_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(fine, coarse, nf, nc, Nc);
+  (reduce_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(fine, coarse, nf, nc, Nc), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -636,7 +636,7 @@ int mg_prolong(baorec_ctx* ctx, float* fine, const float* coarse, const int nl[3
   int3 nf = make_int3(nl[0], nl[1], nl[2]);
   int3 nc = make_int3(nl[0] / 2, nl[1] / 2, nl[2] / 2);
   size_t Nc = (size_t)nc.x * nc.y * nc.z;
-  prolong_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(coarse, fine, nc, nf, Nc, add);
+  (prolong_kernel<<<blocks_for(Nc), 256, 0, ctx->stream>>>(coarse, fine, nc, nf, Nc, add), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -695,9 +695,9 @@ static int smooth_rb(baorec_ctx* ctx, int lvl, const LG& G, float shift, int nsw
       ctx->launches++;
       float* q = a; a = b; b = q;
     } else {
-      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, b, L.f, G, N, 0, shift);
+      (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(a, b, L.f, G, N, 0, shift), ::baorec::count_launch());
       CKLAUNCH();
-      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(b, a, L.f, G, N, 1, shift);
+      (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(b, a, L.f, G, N, 1, shift), ::baorec::count_launch());
       CKLAUNCH();
     }
   }
@@ -735,21 +735,21 @@ static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
   }
   if (lvl == ctx->dense_level || lvl + 1 == ctx->nlev) {
     if (ctx->coarse_M && lvl == ctx->dense_level) {
-      coarse_dense_kernel<<<(unsigned)((N + 255) / 256), 256, 0, ctx->stream>>>(ctx->coarse_M, L.f, v, (int)N);
+      (coarse_dense_kernel<<<(unsigned)((N + 255) / 256), 256, 0, ctx->stream>>>(ctx->coarse_M, L.f, v, (int)N), ::baorec::count_launch());
       CKLAUNCH();
       return BAOREC_OK;
     }
     if (N <= (size_t)kCoarseMaxCells) {
       // the shift only moves the mean, which the coarse solve removes
-      coarse_solve_kernel<<<1, 256, 2 * N * sizeof(double), ctx->stream>>>(L.f, v, G, kCoarseSweeps);
+      (coarse_solve_kernel<<<1, 256, 2 * N * sizeof(double), ctx->stream>>>(L.f, v, G, kCoarseSweeps), ::baorec::count_launch());
       CKLAUNCH();
       return BAOREC_OK;
     }
     CK(cudaMemsetAsync(v, 0, N * 4, ctx->stream));
     for (int s = 0; s < 50; ++s) {
-      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift);
+      (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, t, L.f, G, N, 0, shift), ::baorec::count_launch());
       CKLAUNCH();
-      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift);
+      (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(t, v, L.f, G, N, 1, shift), ::baorec::count_launch());
       CKLAUNCH();
     }
     return BAOREC_OK;
@@ -761,7 +761,7 @@ static int vcycle_rb(baorec_ctx* ctx, int lvl, float shift) {
     CK(launch_resid(ctx->stream, v, L.f, L.r, G, shift, L.needs_clamp));
     ctx->launches++;
   } else {
-    residual_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, L.f, L.r, G, N, shift);
+    (residual_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(v, L.f, L.r, G, N, shift), ::baorec::count_launch());
     CKLAUNCH();
   }
   CKS(mg_reduce(ctx, C.f, L.r, L.n));
@@ -783,7 +783,7 @@ int operator_residual(baorec_ctx* ctx, const float* v, const float* f, float* r)
     CK(launch_resid_diff(ctx->stream, v, f, r, G, nullptr));
     ctx->launches++;
   } else {
-    residual_diff_kernel<<<blocks_for(L0.N), 256, 0, ctx->stream>>>(v, f, r, G, L0.N, nullptr);
+    (residual_diff_kernel<<<blocks_for(L0.N), 256, 0, ctx->stream>>>(v, f, r, G, L0.N, nullptr), ::baorec::count_launch());
     CKLAUNCH();
   }
   return BAOREC_OK;
@@ -839,7 +839,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
   static_assert(kSumBlocks == kFsumBlocks, "the producer's per-block sums stand in for this pass");
   const double* fsums = fpart ? fpart : ctx->dred;
   if (!fpart) {
-    sum_sumsq_partial_kernel<<<kSumBlocks, 256, 0, ctx->stream>>>(f, N, ctx->dred);
+    (sum_sumsq_partial_kernel<<<kSumBlocks, 256, 0, ctx->stream>>>(f, N, ctx->dred), ::baorec::count_launch());
     CKLAUNCH();
   }
   CK(cudaMemcpyAsync(ctx->hred, fsums, 2 * kSumBlocks * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -889,7 +889,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
     bool speculative = false;
     if (it == 0 && zero_start) {
       if (!first_from_f) {
-        shift_mean_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(f, L0.f, N, fsums, kSumBlocks);
+        (shift_mean_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(f, L0.f, N, fsums, kSumBlocks), ::baorec::count_launch());
         CKLAUNCH();
       }
       // the first FFT correction needs only r: queue it before waiting for the sums
@@ -916,8 +916,8 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
         pending_d = nullptr;
         ctx->launches++;
       } else {
-        resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
-                                                              G, N, (float)alpha, ctx->dred);
+        (resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(hiA, loA, have_e ? L0.v : nullptr, f, hiB, loB, L0.f,
+                                                              G, N, (float)alpha, ctx->dred), ::baorec::count_launch());
         CKLAUNCH();
       }
       CK(cudaMemcpyAsync(ctx->hred, ctx->dred, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1013,7 +1013,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
           CK(launch_resid_diff(ctx->stream, dprev, src, rout, G, acc, shift));
           ctx->launches++;
         } else {
-          residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(dprev, rin, rout, G, N, acc);
+          (residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(dprev, rin, rout, G, N, acc), ::baorec::count_launch());
           CKLAUNCH();
         }
         std::swap(rin, rout);
@@ -1022,7 +1022,7 @@ int mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* phi0, bao
       if (m > 1 && tile0 && !stream0) {
         pending_d = d;   // the tiled accurate residual adds the last correction as it loads e
       } else if (m > 1) {
-        add_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L0.v, d, N);
+        (add_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L0.v, d, N), ::baorec::count_launch());
         CKLAUNCH();
       }
       nspec += m;
@@ -1067,12 +1067,12 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     if (which == 0 && tile_ok(L.n))
       launch_rb_sweep(ctx->stream, L.v, t, L.f, Gc, 0.0f, L.needs_clamp);
     else if (which == 0)
-      rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, t, L.f, Gc, N, 0, 0.0f);
+      (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, t, L.f, Gc, N, 0, 0.0f), ::baorec::count_launch());
     else if (which == 1 && tile_ok(L.n))
       launch_resid_acc(ctx->stream, L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, 0.0f, ctx->dred, &np);
     else if (which == 1)
-      resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, N,
-                                                            0.0f, ctx->dred);
+      (resid_acc_kernel<<<kResBlocks, 256, 0, ctx->stream>>>(L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, N,
+                                                            0.0f, ctx->dred), ::baorec::count_launch());
     else if (which == 4)
       launch_resid_acc_stream(ctx->stream, L.v, L.f, L.r, L.f, ctx->phi_hi2, ctx->phi_lo2, t, G, 0.0f, ctx->dred, &np);
     else if (which == 5)
@@ -1080,7 +1080,7 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else if (which == 3 && tile_ok(L.n))
       launch_resid_diff(ctx->stream, L.v, L.f, t, G, L.r);
     else if (which == 3)
-      residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, N, L.r);
+      (residual_diff_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, N, L.r), ::baorec::count_launch());
     else if (which == 6)
       vcycle_rb(ctx, 0, 0.0f);
     else if (which == 7)
@@ -1088,7 +1088,7 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else if (tile_ok(L.n))
       launch_jacobi(ctx->stream, L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor);
     else
-      jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N);
+      (jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N), ::baorec::count_launch());
   };
   if (which < 0 || which > 7) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
   if ((which == 4 || which == 5) && !stream_ok(L.n))

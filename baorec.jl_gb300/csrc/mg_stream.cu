@@ -261,7 +261,7 @@ cudaError_t launch_resid_acc_stream(cudaStream_t s, const float* hi, const float
   auto k = G.local ? resid_acc_stream_kernel<true> : resid_acc_stream_kernel<false>;
   cudaError_t e = smem_optin((const void*)k, bytes);
   if (e != cudaSuccess) return e;
-  k<<<grid, NTS, bytes, s>>>(hi, lo, ec, f, ohi, olo, r, G, alpha, zs, part);
+  (k<<<grid, NTS, bytes, s>>>(hi, lo, ec, f, ohi, olo, r, G, alpha, zs, part), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -269,8 +269,8 @@ cudaError_t launch_resid_diff_stream(cudaStream_t s, const float* d, const float
                                      float* acc, float shift) {
   const int zs = zseg_of(G.n);
   const dim3 grid(G.n[0] / SX, G.n[1] / SYT, G.n[2] / zs);
-  if (G.local) resid_diff_stream_kernel<true><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift);
-  else resid_diff_stream_kernel<false><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift);
+  if (G.local) (resid_diff_stream_kernel<true><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift), ::baorec::count_launch());
+  else (resid_diff_stream_kernel<false><<<grid, NTS, 0, s>>>(d, rin, rout, G, zs, acc, shift), ::baorec::count_launch());
   return cudaGetLastError();
 }
 

@@ -863,7 +863,7 @@ cudaError_t sweep_t(cudaStream_t s, const float* vin, float* vout, const float* 
   constexpr size_t b = win_bytes<2, TY, TZ>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(vin, vout, rhs, G, shift);
+  (k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(vin, vout, rhs, G, shift), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -874,7 +874,7 @@ cudaError_t resid_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   constexpr size_t b = win_bytes<1, TY, TZ>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(ec, rhs, r, G, shift, acc);
+  (k<<<grid_of<TY, TZ>(G.n), NT, b, s>>>(ec, rhs, r, G, shift, acc), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -885,7 +885,7 @@ cudaError_t pairz_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   constexpr size_t b = sizeof(float) * (3 * (16 + 2) * 2 * WX + WX + (16 + 2) + TZ + 2) + sizeof(int) * (16 + 2);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<dim3(G.n[0] / TX, G.n[1] / 16, G.n[2] / TZ), NT, b, s>>>(ec, rhs, r, G, shift, acc);
+  (k<<<dim3(G.n[0] / TX, G.n[1] / 16, G.n[2] / TZ), NT, b, s>>>(ec, rhs, r, G, shift, acc), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -896,7 +896,7 @@ cudaError_t pairs_t(cudaStream_t s, const float* ec, const float* rhs, float* r,
   constexpr size_t b = win_bytes<1, TY, TZ>(1);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, shift, acc);
+  (k<<<grid_of<TY, TZ>(G.n), 32 * TY, b, s>>>(ec, rhs, r, G, shift, acc), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -907,7 +907,7 @@ cudaError_t acc_t(cudaStream_t s, const float* hi, const float* lo, const float*
   constexpr size_t b = win_bytes<1, TY, TZ>(2);
   cudaError_t e = allow_smem(k, b);
   if (e != cudaSuccess) return e;
-  k<<<grid_of<TY, TZ>(G.n), NTH, b, s>>>(hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part);
+  (k<<<grid_of<TY, TZ>(G.n), NTH, b, s>>>(hi, lo, ec, ed, f, ohi, olo, r, G, alpha, part), ::baorec::count_launch());
   return cudaGetLastError();
 }
 
@@ -937,7 +937,7 @@ cudaError_t ref_stencil_t(cudaStream_t s, const float* v, const float* f, float*
   auto run = [&](auto k, dim3 grid, size_t b) {
     cudaError_t e = allow_smem(k, b);
     if (e != cudaSuccess) return e;
-    k<<<grid, 256, b, s>>>(v, f, out, G, w);
+    (k<<<grid, 256, b, s>>>(v, f, out, G, w), ::baorec::count_launch());
     return cudaGetLastError();
   };
   if (G.n[2] % 16 == 0)

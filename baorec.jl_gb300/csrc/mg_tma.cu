@@ -344,7 +344,7 @@ cudaError_t tma_t(cudaStream_t s, const ResidMaps& maps, float* rout, float* acc
     }
   }
   const dim3 grid(G.n[0] / kTX, G.n[1] / kTY, G.n[2] / tz);
-  k<<<grid, kThreadsR, bytes, s>>>(maps, rout, acc, G, shift, tz, G.err, kWaitNs);
+  (k<<<grid, kThreadsR, bytes, s>>>(maps, rout, acc, G, shift, tz, G.err, kWaitNs), ::baorec::count_launch());
   return cudaGetLastError();
 }
 

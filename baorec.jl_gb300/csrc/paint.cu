@@ -155,11 +155,11 @@ int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const floa
   if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;
   int wb = (flags & BAOREC_WRITEBACK) ? 1 : 0;
   if (mas == BAOREC_MAS_TSC)
-    tsc_paint_kernel<<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
+    (tsc_paint_kernel<<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr), ::baorec::count_launch());
   else if (g.n[0] % 4 == 0 && (uintptr_t)mesh % 16 == 0)
-    cic_paint_kernel<true><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
+    (cic_paint_kernel<true><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr), ::baorec::count_launch());
   else
-    cic_paint_kernel<false><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr);
+    (cic_paint_kernel<false><<<grid, 256, 0, ctx->stream>>>(mesh, x, y, z, w, n, g, wb, ctx->derr), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
@@ -167,7 +167,7 @@ int paint(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, const floa
 int minmax3(baorec_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
             float mn[3], float mx[3]) {
   const unsigned blocks = 2 * kNumSMs;   // 6 floats per block fit the FP64 partials buffer
-  minmax_partial_kernel<<<blocks, 256, 0, ctx->stream>>>(x, y, z, n, (float*)ctx->dred);
+  (minmax_partial_kernel<<<blocks, 256, 0, ctx->stream>>>(x, y, z, n, (float*)ctx->dred), ::baorec::count_launch());
   CKLAUNCH();
   float* h = (float*)ctx->hred;
   CK(cudaMemcpyAsync(h, ctx->dred, blocks * 6 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -206,7 +206,7 @@ extern "C" int baorec_cell_bins(baorec_ctx* ctx, const float* x, const float* y,
   if (n > 0) {
     unsigned grid = grid_for((size_t)n, 256);
     if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;
-    cell_bins_kernel<<<grid, 256, 0, ctx->stream>>>(dx, dy, dz, n, g, dkeys, dcounts, ctx->derr);
+    (cell_bins_kernel<<<grid, 256, 0, ctx->stream>>>(dx, dy, dz, n, g, dkeys, dcounts, ctx->derr), ::baorec::count_launch());
     CKLAUNCH();
   }
   int st = BAOREC_OK;

@@ -417,25 +417,25 @@ int paint_binned(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, con
   const int S = bg.T + 2;
   const size_t smem = (size_t)S * S * S * sizeof(float);
   if (mas == BAOREC_MAS_TSC) {
-    bin_count_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr);
+    (bin_count_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr), ::baorec::count_launch());
     CKLAUNCH();
-    tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles);
+    (tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles), ::baorec::count_launch());
     CKLAUNCH();
-    bin_scatter_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts);
+    (bin_scatter_kernel<BAOREC_MAS_TSC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts), ::baorec::count_launch());
     CKLAUNCH();
     if (smem > 48 * 1024)
       CK(cudaFuncSetAttribute(bin_paint_kernel<BAOREC_MAS_TSC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bin_paint_kernel<BAOREC_MAS_TSC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh);
+    (bin_paint_kernel<BAOREC_MAS_TSC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh), ::baorec::count_launch());
   } else {
-    bin_count_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr);
+    (bin_count_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, n, g, bg, wb, counts, ctx->derr), ::baorec::count_launch());
     CKLAUNCH();
-    tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles);
+    (tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, bg.ntiles), ::baorec::count_launch());
     CKLAUNCH();
-    bin_scatter_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts);
+    (bin_scatter_kernel<BAOREC_MAS_CIC><<<blocks, kBinThreads, 0, ctx->stream>>>(x, y, z, w, n, g, bg, cursor, parts), ::baorec::count_launch());
     CKLAUNCH();
     if (smem > 48 * 1024)
       CK(cudaFuncSetAttribute(bin_paint_kernel<BAOREC_MAS_CIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bin_paint_kernel<BAOREC_MAS_CIC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh);
+    (bin_paint_kernel<BAOREC_MAS_CIC><<<bg.ntiles, kBinThreads, smem, ctx->stream>>>(parts, offsets, g, bg, mesh), ::baorec::count_launch());
   }
   CKLAUNCH();
   return BAOREC_OK;
@@ -466,28 +466,28 @@ int paint_sorted(baorec_ctx* ctx, float* mesh, float* x, float* y, float* z, con
   if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;
   const int wb = (flags & BAOREC_WRITEBACK) ? 1 : 0;
   if (mas == BAOREC_MAS_TSC)
-    tile_keys_kernel<BAOREC_MAS_TSC><<<grid, 256, 0, ctx->stream>>>(x, y, z, n, g, tg, wb, keys, counts, ctx->derr);
+    (tile_keys_kernel<BAOREC_MAS_TSC><<<grid, 256, 0, ctx->stream>>>(x, y, z, n, g, tg, wb, keys, counts, ctx->derr), ::baorec::count_launch());
   else
-    tile_keys_kernel<BAOREC_MAS_CIC><<<grid, 256, 0, ctx->stream>>>(x, y, z, n, g, tg, wb, keys, counts, ctx->derr);
+    (tile_keys_kernel<BAOREC_MAS_CIC><<<grid, 256, 0, ctx->stream>>>(x, y, z, n, g, tg, wb, keys, counts, ctx->derr), ::baorec::count_launch());
   CKLAUNCH();
-  tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, tg.ntiles);
+  (tile_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts, offsets, cursor, tg.ntiles), ::baorec::count_launch());
   CKLAUNCH();
-  tile_scatter_kernel<<<grid, 256, 0, ctx->stream>>>(keys, n, cursor, perm);
+  (tile_scatter_kernel<<<grid, 256, 0, ctx->stream>>>(keys, n, cursor, perm), ::baorec::count_launch());
   CKLAUNCH();
   const int S = tg.T + 2;
   const size_t smem = (size_t)S * S * S * sizeof(unsigned long long);
   if (mas == BAOREC_MAS_TSC) {
     if (smem > 48 * 1024) CK(cudaFuncSetAttribute(tile_accum_kernel<BAOREC_MAS_TSC>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    tile_accum_kernel<BAOREC_MAS_TSC><<<tg.ntiles, 256, smem, ctx->stream>>>(x, y, z, w, offsets, perm, g, tg, fix);
+    (tile_accum_kernel<BAOREC_MAS_TSC><<<tg.ntiles, 256, smem, ctx->stream>>>(x, y, z, w, offsets, perm, g, tg, fix), ::baorec::count_launch());
   } else {
     if (smem > 48 * 1024) CK(cudaFuncSetAttribute(tile_accum_kernel<BAOREC_MAS_CIC>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    tile_accum_kernel<BAOREC_MAS_CIC><<<tg.ntiles, 256, smem, ctx->stream>>>(x, y, z, w, offsets, perm, g, tg, fix);
+    (tile_accum_kernel<BAOREC_MAS_CIC><<<tg.ntiles, 256, smem, ctx->stream>>>(x, y, z, w, offsets, perm, g, tg, fix), ::baorec::count_launch());
   }
   CKLAUNCH();
-  fix_to_mesh_kernel<<<grid_for(ctx->N, 256) < 16u * kNumSMs ? grid_for(ctx->N, 256) : 16u * kNumSMs, 256, 0,
-                       ctx->stream>>>(fix, mesh, ctx->N);
+  (fix_to_mesh_kernel<<<grid_for(ctx->N, 256) < 16u * kNumSMs ? grid_for(ctx->N, 256) : 16u * kNumSMs, 256, 0,
+                       ctx->stream>>>(fix, mesh, ctx->N), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }

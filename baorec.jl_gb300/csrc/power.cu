@@ -298,10 +298,10 @@ extern "C" int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_confi
   double sd[3] = {0, 0, 0}, sr[3] = {0, 0, 0};
   {
     std::vector<double> h(6 * kPwBlocks);
-    pw_sums_kernel<<<kPwBlocks, 256, 0, ctx->stream>>>(dw, nullptr, n, part);
+    (pw_sums_kernel<<<kPwBlocks, 256, 0, ctx->stream>>>(dw, nullptr, n, part), ::baorec::count_launch());
     CKLAUNCH();
     if (nr > 0) {
-      pw_sums_kernel<<<kPwBlocks, 256, 0, ctx->stream>>>(ew, enz, nr, part + 3 * kPwBlocks);
+      (pw_sums_kernel<<<kPwBlocks, 256, 0, ctx->stream>>>(ew, enz, nr, part + 3 * kPwBlocks), ::baorec::count_launch());
       CKLAUNCH();
     }
     CK(cudaMemcpyAsync(h.data(), part, (nr > 0 ? 6 : 3) * kPwBlocks * sizeof(double), cudaMemcpyDeviceToHost,
@@ -345,21 +345,21 @@ extern "C" int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_confi
   auto paint_all = [&](float* mesh, float shift) -> int {
     CK(cudaMemsetAsync(mesh, 0, N * sizeof(float), ctx->stream));
     if (pc->mas == BAOREC_MAS_TSC) {
-      pw_paint_kernel<BAOREC_MAS_TSC><<<pgrid, 256, 0, ctx->stream>>>(mesh, dx, dy, dz, dw, n, g, shift, 1.0f,
-                                                                     survey, ctx->derr);
+      (pw_paint_kernel<BAOREC_MAS_TSC><<<pgrid, 256, 0, ctx->stream>>>(mesh, dx, dy, dz, dw, n, g, shift, 1.0f,
+                                                                     survey, ctx->derr), ::baorec::count_launch());
       CKLAUNCH();
       if (nr > 0) {
-        pw_paint_kernel<BAOREC_MAS_TSC><<<pgrid, 256, 0, ctx->stream>>>(mesh, ex, ey, ez, ew, nr, g, shift,
-                                                                       (float)-alpha, survey, ctx->derr);
+        (pw_paint_kernel<BAOREC_MAS_TSC><<<pgrid, 256, 0, ctx->stream>>>(mesh, ex, ey, ez, ew, nr, g, shift,
+                                                                       (float)-alpha, survey, ctx->derr), ::baorec::count_launch());
         CKLAUNCH();
       }
     } else {
-      pw_paint_kernel<BAOREC_MAS_CIC><<<pgrid, 256, 0, ctx->stream>>>(mesh, dx, dy, dz, dw, n, g, shift, 1.0f,
-                                                                     survey, ctx->derr);
+      (pw_paint_kernel<BAOREC_MAS_CIC><<<pgrid, 256, 0, ctx->stream>>>(mesh, dx, dy, dz, dw, n, g, shift, 1.0f,
+                                                                     survey, ctx->derr), ::baorec::count_launch());
       CKLAUNCH();
       if (nr > 0) {
-        pw_paint_kernel<BAOREC_MAS_CIC><<<pgrid, 256, 0, ctx->stream>>>(mesh, ex, ey, ez, ew, nr, g, shift,
-                                                                       (float)-alpha, survey, ctx->derr);
+        (pw_paint_kernel<BAOREC_MAS_CIC><<<pgrid, 256, 0, ctx->stream>>>(mesh, ex, ey, ez, ew, nr, g, shift,
+                                                                       (float)-alpha, survey, ctx->derr), ::baorec::count_launch());
         CKLAUNCH();
       }
     }
@@ -371,7 +371,7 @@ extern "C" int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_confi
   if (!survey && pc->interlace) {
     CKS(paint_all(M2, 0.5f));
     CKFFT(cufftExecR2C(ctx->plan_r2c, M2, S));
-    pw_interlace_kernel<<<eg, 256, 0, ctx->stream>>>(A0, S, kg, Nk);
+    (pw_interlace_kernel<<<eg, 256, 0, ctx->stream>>>(A0, S, kg, Nk), ::baorec::count_launch());
     CKLAUNCH();
   }
   if (survey) {
@@ -379,10 +379,10 @@ extern "C" int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_confi
     // quadrupole: the 6 index pairs i <= j, off-diagonal ones twice
     for (int i = 0; i < 3; ++i)
       for (int j = i; j < 3; ++j) {
-        pw_rhat_kernel<<<eg, 256, 0, ctx->stream>>>(F, M2, g, 2, i, j, 0, 0);
+        (pw_rhat_kernel<<<eg, 256, 0, ctx->stream>>>(F, M2, g, 2, i, j, 0, 0), ::baorec::count_launch());
         CKLAUNCH();
         CKFFT(cufftExecR2C(ctx->plan_r2c, M2, S));
-        pw_accum_kernel<<<eg, 256, 0, ctx->stream>>>(S, A2, kg, Nk, 2, i, j, 0, 0, i == j ? 1.0f : 2.0f);
+        (pw_accum_kernel<<<eg, 256, 0, ctx->stream>>>(S, A2, kg, Nk, 2, i, j, 0, 0, i == j ? 1.0f : 2.0f), ::baorec::count_launch());
         CKLAUNCH();
       }
     // hexadecapole: the 15 multisets i <= j <= k <= l with their 4!/(a! b! c!) orderings
@@ -397,17 +397,17 @@ extern "C" int baorec_power_multipoles(baorec_ctx* ctx, const baorec_power_confi
             cnt[k]++;
             cnt[l]++;
             const float c = (float)(24 / (fact[cnt[0]] * fact[cnt[1]] * fact[cnt[2]]));
-            pw_rhat_kernel<<<eg, 256, 0, ctx->stream>>>(F, M2, g, 4, i, j, k, l);
+            (pw_rhat_kernel<<<eg, 256, 0, ctx->stream>>>(F, M2, g, 4, i, j, k, l), ::baorec::count_launch());
             CKLAUNCH();
             CKFFT(cufftExecR2C(ctx->plan_r2c, M2, S));
-            pw_accum_kernel<<<eg, 256, 0, ctx->stream>>>(S, A4, kg, Nk, 4, i, j, k, l, c);
+            (pw_accum_kernel<<<eg, 256, 0, ctx->stream>>>(S, A4, kg, Nk, 4, i, j, k, l, c), ::baorec::count_launch());
             CKLAUNCH();
           }
   }
   const int nb = pc->nbins;
-  pw_bin_kernel<<<kPwBlocks, 256, 5 * nb * sizeof(double), ctx->stream>>>(
+  (pw_bin_kernel<<<kPwBlocks, 256, 5 * nb * sizeof(double), ctx->stream>>>(
       A0, A2, A4, kg, Nk, survey ? 1 : 0, (float)lv[0], (float)lv[1], (float)lv[2], pc->mas == BAOREC_MAS_TSC ? 3 : 2,
-      pc->kmin, pc->dk, nb, 1.0 / norm, shot, part);
+      pc->kmin, pc->dk, nb, 1.0 / norm, shot, part), ::baorec::count_launch());
   CKLAUNCH();
   std::vector<double> h((size_t)kPwBlocks * 5 * nb);
   CK(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -136,8 +136,8 @@ int readout(baorec_ctx* ctx, const float* psi3, const float* x, const float* y, 
   G.local = ctx->cfg.los_mode == BAOREC_LOS_LOCAL ? 1 : 0;
   unsigned grid = grid_for((size_t)n, 256);
   if (grid > 64u * kNumSMs) grid = 64u * kNumSMs;
-  readout_kernel<<<grid, 256, 0, ctx->stream>>>(psi3, ctx->N, x, y, z, n, G, field, mode, o0, o1, o2, field2, p0, p1,
-                                                 p2, ctx->derr);
+  (readout_kernel<<<grid, 256, 0, ctx->stream>>>(psi3, ctx->N, x, y, z, n, G, field, mode, o0, o1, o2, field2, p0, p1,
+                                                 p2, ctx->derr), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }

@@ -124,7 +124,7 @@ extern "C" int baorec_sky_to_cartesian(baorec_ctx* ctx, const float* ra, const f
   CKS(stage_out_alloc(ctx, 5, n, flags, y, &oy));
   CKS(stage_out_alloc(ctx, 6, n, flags, zc, &oz));
   if (n > 0) {
-    sky_to_cart_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dra, ddec, dz, n, t, h, ox, oy, oz, ctx->derr);
+    (sky_to_cart_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dra, ddec, dz, n, t, h, ox, oy, oz, ctx->derr), ::baorec::count_launch());
     CKLAUNCH();
   }
   CKS(stage_out_copy(ctx, x, ox, n, flags));
@@ -151,7 +151,7 @@ extern "C" int baorec_cartesian_to_sky(baorec_ctx* ctx, const float* x, const fl
   CKS(stage_out_alloc(ctx, 5, n, flags, dec, &o1));
   CKS(stage_out_alloc(ctx, 6, n, flags, red, &o2));
   if (n > 0) {
-    cart_to_sky_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dx, dy, dz, n, t, h, o0, o1, o2, ctx->derr);
+    (cart_to_sky_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dx, dy, dz, n, t, h, o0, o1, o2, ctx->derr), ::baorec::count_launch());
     CKLAUNCH();
   }
   CKS(stage_out_copy(ctx, ra, o0, n, flags));
@@ -168,7 +168,7 @@ extern "C" int baorec_fkp_weights(baorec_ctx* ctx, const float* nz, int64_t n, f
   float* dw;
   CKS(stage_out_alloc(ctx, 4, n, flags, w, &dw));
   if (n > 0) {
-    fkp_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dnz, n, P0, dw);
+    (fkp_kernel<<<grid_of_n(n), 256, 0, ctx->stream>>>(dnz, n, P0, dw), ::baorec::count_launch());
     CKLAUNCH();
   }
   CKS(stage_out_copy(ctx, w, dw, n, flags));

@@ -207,7 +207,7 @@ int tune_paint(baorec_ctx* ctx) {
   CK(cudaMalloc(&p, (size_t)n * 4 * sizeof(float)));
   float3 lo = make_float3(ctx->cfg.box_min[0], ctx->cfg.box_min[1], ctx->cfg.box_min[2]);
   float3 span = make_float3(ctx->cfg.box_size[0], ctx->cfg.box_size[1], ctx->cfg.box_size[2]);
-  uniform_particles_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(p, n, lo, span, 12345u);
+  (uniform_particles_kernel<<<8 * kNumSMs, 256, 0, ctx->stream>>>(p, n, lo, span, 12345u), ::baorec::count_launch());
   int st = cudaGetLastError() == cudaSuccess ? BAOREC_OK : set_error(ctx, BAOREC_ERR_CUDA, "autotune: particle kernel");
   float* mesh = ctx->psi;   // scratch
   ctx->psi_valid = false;

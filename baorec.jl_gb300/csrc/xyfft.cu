@@ -280,13 +280,13 @@ static const float2* w256_of(const baorec_ctx* ctx) {
 }
 
 int xy_r2c(baorec_ctx* ctx, const float* in, cufftComplex* out, int planes) {
-  xy_r2c_kernel<<<dim3(2, planes), kXT, kR2CSmem, ctx->stream>>>(in, out, w256_of(ctx));
+  (xy_r2c_kernel<<<dim3(2, planes), kXT, kR2CSmem, ctx->stream>>>(in, out, w256_of(ctx)), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
 
 int xy_c2r(baorec_ctx* ctx, const cufftComplex* in, float* out, int planes) {
-  xy_c2r_kernel<<<dim3(2, planes), kXT, kC2RSmem, ctx->stream>>>(in, out, w256_of(ctx));
+  (xy_c2r_kernel<<<dim3(2, planes), kXT, kC2RSmem, ctx->stream>>>(in, out, w256_of(ctx)), ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }

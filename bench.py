@@ -916,7 +916,7 @@ def run_gb300(args):
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
-        l0 = c.launches()
+        l0 = c.total_launches()
         clocks.start()
         ev0.record(stream)
         hist = []
@@ -927,7 +927,7 @@ def run_gb300(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         clk = clocks.stop()
-        launches = c.launches() - l0
+        launches = c.total_launches() - l0
         ms, _ = replica_throughput(ev0.elapsed_time(ev1) / args.steps, ws, dist)
         if dist:
             dist.barrier()

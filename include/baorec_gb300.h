@@ -125,6 +125,9 @@ int baorec_get_box(const baorec_ctx* ctx, float box_size[3], float box_min[3]);
 void* baorec_stream(baorec_ctx* ctx);
 /* Number of kernels this context has launched since creation. */
 int64_t baorec_kernel_launches(const baorec_ctx* ctx);
+/* This library's kernel launches in the process so far, every context (a
+ * batch graph's kernels counted once, when captured). */
+int64_t baorec_total_kernel_launches(void);
 /* Device pointer of the context's result field (result_cache), or NULL. */
 float* baorec_result_ptr(baorec_ctx* ctx);
 

@@ -152,8 +152,12 @@ def test_displacement_of_the_solve_equals_recomputed(start):
     p = lambda ts: [t.data_ptr() for t in ts]
     nd, nr = int(m.x.size), int(m.rx.size)
     torch.cuda.synchronize()
+    l0 = ctx.total_launches()
     assert ctx.status("baorec_reconstructed_potential", *p(X), nd, *p(Rr), nr, 0) == _lib.OK
     assert ctx.solve_stats()["rel_residual"] <= 1e-6
+    # every kernel of the library is counted (paints, smoothing, normalisation,
+    # the solve's passes, the displacement): dozens per reconstruction
+    assert ctx.total_launches() - l0 >= 20
 
     def positions():
         out = [torch.empty(nr, device="cuda") for _ in range(6)]
