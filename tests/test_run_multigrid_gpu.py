@@ -156,8 +156,9 @@ def test_displacement_of_the_solve_equals_recomputed(start):
     assert ctx.status("baorec_reconstructed_potential", *p(X), nd, *p(Rr), nr, 0) == _lib.OK
     assert ctx.solve_stats()["rel_residual"] <= 1e-6
     # every kernel of the library is counted (paints, smoothing, normalisation,
-    # the solve's passes, the displacement): dozens per reconstruction
-    assert ctx.total_launches() - l0 >= 20
+    # the solve's passes incl. the cooperative coarse-level kernel, the
+    # displacement)
+    assert ctx.total_launches() - l0 >= 10
 
     def positions():
         out = [torch.empty(nr, device="cuda") for _ in range(6)]
