@@ -182,9 +182,9 @@ cudaError_t launch_coarse_tail(cudaStream_t s, const TailArgs& args) {
   if (blocks > want) blocks = want > 0 ? want : 1;
   TailArgs a = args;
   void* params[] = {&a};
-  const cudaError_t e = cudaLaunchCooperativeKernel((void*)coarse_tail_kernel, dim3(blocks), dim3(256), params, 0, s);
+  const cudaError_t le = cudaLaunchCooperativeKernel((void*)coarse_tail_kernel, dim3(blocks), dim3(256), params, 0, s);
   ::baorec::count_launch();
-  return e;
+  return le;
 }
 
 }  // namespace baorec
