@@ -229,6 +229,7 @@ bool xy_fused_ok(const baorec_ctx* ctx);
 int xy_fused_prepare(baorec_ctx* ctx);
 int xy_r2c(baorec_ctx* ctx, const float* in, cufftComplex* out, int planes);
 int xy_c2r(baorec_ctx* ctx, const cufftComplex* in, float* out, int planes);
+int xy_profile(baorec_ctx* ctx, int inverse, const float* r, float* out);
 // Unit line of sight the FFT preconditioner uses (false: isotropic, l = 0).
 bool mean_los(const baorec_ctx* c, double l[3]);
 // r = f - A v with the finest level's exact operator (difference form, FP32).

@@ -930,7 +930,18 @@ bool xy_plans(baorec_ctx* ctx) {
 }
 
 int spectral_tables(baorec_ctx* ctx);
+}  // namespace
 
+// One batched xy transform of the finest mesh (the measurement hook): r ->
+// the spectrum buffer, or (inverse) the spectrum buffer -> out, by the
+// autotuner's current choice between the fused kernels and cuFFT.
+int xy_profile(baorec_ctx* ctx, int inverse, const float* r, float* out) {
+  if (ctx->n3 != kZLen || !ctx->ck || !xy_plans(ctx))
+    return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: no batched xy transforms for this mesh");
+  return inverse ? xy_inverse(ctx, ctx->ck, out, 1) : xy_forward(ctx, r, ctx->ck, 1);
+}
+
+namespace {
 // z pass over `batch` spectra of n3 = 256 planes at a, multiplier m; form 2
 // caps the registers for three resident blocks per SM instead of two.
 template <class M>

@@ -1062,9 +1062,11 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  int np = 0;
+  int np = 0, xst = BAOREC_OK;
   auto launch = [&]() {
-    if (which == 0 && tile_ok(L.n))
+    if (which == 8 || which == 9)
+      xst = xy_profile(ctx, which == 9, L.f, t);
+    else if (which == 0 && tile_ok(L.n))
       launch_rb_sweep(ctx->stream, L.v, t, L.f, Gc, 0.0f, L.needs_clamp);
     else if (which == 0)
       (rb_half_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, t, L.f, Gc, N, 0, 0.0f), ::baorec::count_launch());
@@ -1090,10 +1092,15 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     else
       (jacobi_kernel<<<blocks_for(N), 256, 0, ctx->stream>>>(L.v, L.f, t, G, ctx->cfg.jacobi_damping_factor, N), ::baorec::count_launch());
   };
-  if (which < 0 || which > 7) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
+  if (which < 0 || which > 9) return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: unknown kernel %d", which);
   if ((which == 4 || which == 5) && !stream_ok(L.n))
     return set_error(ctx, BAOREC_ERR_ARG, "profile_kernel: no streaming form here");
   launch();   // warm-up
+  if (xst != BAOREC_OK) {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return xst;
+  }
   CK(cudaEventRecord(a, ctx->stream));
   for (int r = 0; r < reps; ++r) launch();
   CK(cudaEventRecord(b, ctx->stream));
@@ -1121,5 +1128,8 @@ extern "C" int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float
     for (int l = 0; l < ctx->nlev; ++l) b += (double)ctx->lev[l].N * (12.0 * sweeps + 12.0 + 4.5 + 8.5);
     *bytes = b;
   }
+  // a batched xy transform reads the real mesh and writes the half spectrum
+  // (8 + 4 B per half-spectrum cell and real cell), or the reverse
+  if (which == 8 || which == 9) *bytes = 4.0 * N + 8.0 * (double)ctx->n1h * ctx->n2 * ctx->n3;
   return BAOREC_OK;
 }

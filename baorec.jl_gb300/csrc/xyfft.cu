@@ -1,28 +1,21 @@
 // Fused 2-D real transforms of 256 x 256 xy planes (the x and y passes of the
 // FFT preconditioner's, the smoothing's and the displacement's transforms),
-// one kernel per direction instead of cuFFT's two passes.
+// one kernel per direction instead of cuFFT's two passes: each plane is read
+// once and written once.
 //
-// Forward (R2C), two blocks per plane, block h keeping kx in [65h, 65h + 65 - h):
-//   x: each row of 256 reals is packed as 128 complex z[n] = x[2n] + i x[2n+1],
-//      transformed with a four-step 128 = 16 x 8 (a 16-point DFT in registers,
-//      the 128-point twiddles, an exchange in shared memory, two 8-point
-//      DFTs), and unpacked: X[k] = (Z[k] + Z*[128-k])/2
-//      - i/2 e^{-2πik/256} (Z[k] - Z*[128-k]), k = 0..128;
-//   y: each kept column (256 rows, in shared memory) is transformed with the
-//      four-step 256 = 16 x 16 of the z pass, in place, and written to the
-//      spectrum [plane][ky][kx] (row length 129) as cuFFT's batched 2-D R2C does.
-// Both blocks of a plane read the whole plane; the second read hits L2.
-// Inverse (C2R), two blocks per plane, block h producing rows [128h, 128h+128):
-//   y: every column is inverse-transformed (four-step, exchange in shared
-//      memory) and the block keeps its 128 rows;
-//   x: each kept row is packed, Z[k] = (X[k] + X*[128-k]) + i (X[k] - X*[128-k])
-//      e^{2πik/256}, inverse-transformed (four-step 128) and unpacked,
-//      x[2n] = Re z[n], x[2n+1] = Im z[n]; unnormalised like cuFFT's C2R.
-// The index algebra of both kernels was checked against numpy's FFT.  On a
-// GB300 one 256-plane transform takes 108.6 us forward and 104.2 us inverse
-// (one 200 KB block per SM, 16 warps, the row and column phases serialised
-// by barriers) against about 60 us for cuFFT's two passes, so the autotuner
-// keeps cuFFT; the kernels stay a timed candidate.
+// A plane runs on a cluster of four CTAs (two CTAs per SM): the row
+// transforms of the space side and the column transforms of the spectrum
+// side are split between the four, and the transposition between them is
+// a push of every value into the owning CTA's shared memory through the
+// cluster's distributed shared memory, so no CTA repeats another's row
+// transforms and no intermediate leaves the chip.
+//   rows: the 256 reals of a row packed as 128 complex values, a four-step
+//         128 = 16 x 8 (16-point DFT in registers, twiddles, an exchange in
+//         shared memory, 8-point DFTs) and the real-to-half-spectrum unpack
+//         X[k] = (Z[k] + Z*[128-k])/2 - i/2 e^{-2πik/256} (Z[k] - Z*[128-k]);
+//   columns: a four-step 256 = 16 x 16 per column.
+// The inverse mirrors it.  The index algebra was checked against numpy's
+// FFT by an emulation of both kernels' thread mappings.
 #include "common.cuh"
 
 namespace baorec {
@@ -31,9 +24,6 @@ namespace {
 constexpr int kXN = 256;         // points along x and y
 constexpr int kXH = kXN / 2;     // packed complex points of a row
 constexpr int kXC = kXN / 2 + 1; // half-spectrum length (129)
-constexpr int kXT = 512;         // threads per block
-constexpr int kXRows = kXT / 8;  // rows of one x-transform group (8 threads per row)
-constexpr int kYCols = kXT / 16; // columns of one y-transform round (16 threads per column)
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -110,160 +100,278 @@ __device__ __forceinline__ void dft8x(float2 (&v)[8]) {
   }
 }
 
-// Four-step 128-point transform of one packed row held by 8 threads (b =
-// lane-in-row): input values in[8a + b], a = 0..15 (already in registers v);
-// rb is the row's 128-value exchange buffer.  On return the thread holds
-// outputs k = c + 16 d for c in {b, b + 8} (d = 0..7) in o[2][8].
-template <bool INV>
-__device__ __forceinline__ void fft128_row(float2 (&v)[16], float2* __restrict__ rb, int b,
-                                           const float2* __restrict__ w256, float2 (&o)[2][8]) {
-  dft16x<INV>(v);   // over a: v[c]
-#pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    const float2 w = w256[2 * ((b * c) & 127)];   // e^{-2πi bc/128}
-    rb[8 * c + b] = INV ? cmulc(v[c], w) : cmul(v[c], w);
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const int c = b + 8 * q;
-#pragma unroll
-    for (int bb = 0; bb < 8; ++bb) o[q][bb] = rb[8 * c + bb];
-    dft8x<INV>(o[q]);   // over b: o[q][d] = out[c + 16 d]
-  }
+// ---- cluster plumbing -------------------------------------------------------
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_arrive_relaxed() { asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// store v at the shared-memory offset `local` of cluster CTA `rank`
+__device__ __forceinline__ void st_peer(uint32_t local, unsigned rank, float2 v) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(local), "r"(rank));
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
 }
 
-__global__ void __launch_bounds__(kXT, 1) xy_r2c_kernel(const float* __restrict__ in, cufftComplex* __restrict__ out,
-                                                       const float2* __restrict__ tw) {
+// ---- layout ---------------------------------------------------------------------
+// A plane's 256 x 256 transform runs on a cluster of kCl CTAs.  The packed
+// half spectrum of a row has 128 complex slots: slot 0 holds the two real
+// values (X[0], X[128]), slots 1..127 the complex X[1..127].  CTA q owns
+// rows [64q, 64q + 64) of the space side and packed columns [32q, 32q + 32)
+// of the spectrum side; the rows <-> columns exchange is a push of each
+// value into its owner's shared memory (distributed shared memory), fenced
+// by one cluster barrier.
+constexpr int kCl = 4;                  // CTAs per plane
+constexpr int kCT = 256;                // threads per CTA
+constexpr int kRows = kXN / kCl;        // 64 space rows per CTA
+constexpr int kCols = kXH / kCl;        // 32 packed columns per CTA
+constexpr int kXP = 136;                // float2 pitch of a row buffer: 1088 B, a 16-bank shift between rows
+static_assert(kCT == kXN, "one twiddle per thread");
+
+// Slot of value (c, bb) of a row's 16 x 8 four-step exchange: rotated so
+// that neither the writes (fixed c, 8 bb) nor the reads (8 c, fixed bb) of
+// the two rows sharing a half-warp meet in a bank.
+__device__ __forceinline__ int xslot(int c, int bb, int rot) { return 8 * c + ((bb + (c >> 1) + rot) & 7); }
+
+// Spectrum-side column buffer of the forward kernel: [256 rows][32 columns],
+// column index XOR 8 on odd rows (two rows of one half-warp's pushes land
+// in disjoint banks).
+__device__ __forceinline__ int ycell(int y, int lc) { return y * kCols + (lc ^ ((y & 1) << 3)); }
+
+__device__ __forceinline__ float2 r2c_unpack(float2 zk, float2 p, float2 wk) {   // p = Z[128 - k]
+  const float2 zm = conjf2(p);
+  const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
+  const float2 dd = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y - zm.y));
+  return addf2(e, cmul(make_float2(dd.y, -dd.x), wk));   // e - i dd W^k
+}
+
+// Forward: real planes [plane][y][x] -> half spectra [plane][ky][kx], row
+// length 129, as cuFFT's batched 2-D R2C.
+//   x: 8 threads per row; the row's 256 reals as 128 packed complex values
+//      z[8a + b] (thread b holds a = 0..15), a 16-point DFT over a, twiddles,
+//      an exchange through the row buffer, an 8-point DFT over b: Z[c + 16 d]
+//      for c in {b, b + 8}.  The partner Z[128 - k] of the unpack is in lane
+//      (8 - b) & 7 of the row (shuffles).  X[k] is pushed to CTA k / 32.
+//   y: 16 threads per column; four-step 256 = 16 x 16 in place in the column
+//      buffer; the packed column 0 (X[0] + i X[128], both real) is separated
+//      into the spectra of kx = 0 and kx = 128 with W[256 - ky].
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
+    xy_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, const float2* __restrict__ tw) {
   extern __shared__ __align__(16) float2 xsm[];
-  constexpr int HW = 65;                        // kept columns (block 1: 64)
-  float2* hs = xsm;                             // [256 rows][HW]
-  float2* rbuf = xsm + kXN * HW;                // [kXRows rows][128]
-  float2* w256 = rbuf + kXRows * kXH;           // e^{-2πi m/256}
+  float2* ys = xsm;                          // [256][32] (ycell)
+  float2* xb = ys + kXN * kCols;             // [32 rows][kXP]; later the separation buffer
+  float2* w = xb + 32 * kXP;                 // e^{-2πi m/256}
   const int t = threadIdx.x;
-  const int h = blockIdx.x, k0 = 65 * h, ncol = HW - h;
+  const unsigned rank = cluster_rank();
   const size_t plane = blockIdx.y;
-  const float* src = in + plane * (size_t)(kXN * kXN);
-  float2* dst = reinterpret_cast<float2*>(out) + plane * (size_t)(kXC * kXN);
-  if (t < kXN) w256[t] = __ldg(tw + t);
+  cluster_arrive_relaxed();                  // matched below, before the first push
+  w[t] = __ldg(tw + t);
+  const int rl = t >> 3, b = t & 7, rot = 4 * (rl & 1);
+  const float2* src = reinterpret_cast<const float2*>(in + plane * (size_t)(kXN * kXN));
+  const int y0 = kRows * (int)rank + rl;
+  float2 va[16], vb[16];
+#pragma unroll
+  for (int a = 0; a < 16; ++a) va[a] = __ldg(src + (size_t)y0 * kXH + 8 * a + b);
+#pragma unroll
+  for (int a = 0; a < 16; ++a) vb[a] = __ldg(src + (size_t)(y0 + 32) * kXH + 8 * a + b);
   __syncthreads();
-  const int rl = t >> 3, b = t & 7;             // row within the group, lane within the row
-  float2* rb = rbuf + rl * kXH;
-  for (int g = 0; g < kXN / kXRows; ++g) {
-    const int row = g * kXRows + rl;
-    float2 v[16];
-    const float2* xr = reinterpret_cast<const float2*>(src + (size_t)row * kXN);
+  cluster_wait();                            // every CTA of the cluster runs: pushes may start
+  const uint32_t ys0 = smem_addr(ys);
+  float2* rb = xb + rl * kXP;
+  const unsigned lane = t & 31, partner = (lane & ~7u) | ((8u - b) & 7u);
 #pragma unroll
-    for (int a = 0; a < 16; ++a) v[a] = __ldg(xr + 8 * a + b);   // z[8a + b] = (x[16a+2b], x[16a+2b+1])
-    float2 o[2][8];
-    fft128_row<false>(v, rb, b, w256, o);
-    __syncthreads();   // every thread of the row has read the exchange buffer
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-      for (int d = 0; d < 8; ++d) rb[b + 8 * q + 16 * d] = o[q][d];   // Z in natural order
-    __syncthreads();
-    // unpack X[k] = (Z[k] + Z*[128-k])/2 - i/2 W256^k (Z[k] - Z*[128-k]) for the kept k
-    for (int j = b; j < ncol; j += 8) {
-      const int k = k0 + j;
-      const float2 zk = rb[k & (kXH - 1)], zm = conjf2(rb[(kXH - k) & (kXH - 1)]);
-      const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
-      const float2 dd = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y - zm.y));
-      const float2 od = cmul(make_float2(dd.y, -dd.x), w256[k & (kXN - 1)]);   // -i dd W^k
-      hs[row * HW + j] = addf2(e, od);
-    }
-    __syncthreads();   // the exchange buffer is free for the next group
-  }
-  // y: four-step 256 = 16 x 16 per kept column, in place in hs, then out
-  const int cl = t & (kYCols - 1), r = t >> 5;
-  for (int c0 = 0; c0 < ncol; c0 += kYCols) {
-    const int col = c0 + cl;
-    const bool ok = col < ncol;
-    float2 v[16];
-#pragma unroll
-    for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? hs[(16 * n1 + r) * HW + col] : make_float2(0.0f, 0.0f);
+  for (int round = 0; round < 2; ++round) {
+    float2(&v)[16] = round ? vb : va;
+    const int y = y0 + 32 * round;
     dft16x<false>(v);
-    if (ok) {
 #pragma unroll
-      for (int k1 = 0; k1 < 16; ++k1) hs[(16 * k1 + r) * HW + col] = cmul(v[k1], w256[r * k1]);
+    for (int c = 0; c < 16; ++c) rb[xslot(c, b, rot)] = cmul(v[c], w[(2 * b * c) & 255]);   // W128^{bc}
+    __syncwarp();
+    float2 o[2][8];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int c = b + 8 * q;
+#pragma unroll
+      for (int bb = 0; bb < 8; ++bb) o[q][bb] = rb[xslot(c, bb, rot)];
+      dft8x<false>(o[q]);                    // o[q][d] = Z[c + 16 d]
     }
+    __syncwarp();                            // the row buffer is free for the next round
+    const int ysw = (y & 1) << 3;
+    {   // c = b: partner Z[128 - k] = lane (8 - b)'s o[1][7 - d]; b = 0: own o[0][8 - d]
+      float2 p[8];
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        const float2 s = o[1][7 - d];
+        p[d] = make_float2(__shfl_sync(0xffffffffu, s.x, partner), __shfl_sync(0xffffffffu, s.y, partner));
+      }
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        const int k = b + 16 * d;
+        float2 x = r2c_unpack(o[0][d], b == 0 ? o[0][(8 - d) & 7] : p[d], w[k]);
+        if (d == 0 && b == 0) x = make_float2(o[0][0].x + o[0][0].y, o[0][0].x - o[0][0].y);   // (X[0], X[128])
+        st_peer(ys0 + 8u * (uint32_t)(y * kCols + ((k & 31) ^ ysw)), (unsigned)(k >> 5), x);
+      }
+    }
+    {   // c = b + 8: partner = lane (8 - b)'s o[0][7 - d]; b = 0 (c = 8): own o[1][7 - d]
+      float2 p[8];
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        const float2 s = o[0][7 - d];
+        p[d] = make_float2(__shfl_sync(0xffffffffu, s.x, partner), __shfl_sync(0xffffffffu, s.y, partner));
+      }
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        const int k = b + 8 + 16 * d;
+        const float2 x = r2c_unpack(o[1][d], b == 0 ? o[1][7 - d] : p[d], w[k]);
+        st_peer(ys0 + 8u * (uint32_t)(y * kCols + ((k & 31) ^ ysw)), (unsigned)(k >> 5), x);
+      }
+    }
+  }
+  cluster_arrive_release();
+  cluster_wait_acquire();                    // the CTA's 32 columns are complete
+  float2* dst = out + plane * (size_t)(kXC * kXN);
+  float2* sep = xb;                          // W of the packed column (rank 0)
+  const int col = t & 15, r = t >> 4;
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    const int lc = 16 * g + col;
+    float2 v[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) v[n1] = ys[ycell(16 * n1 + r, lc)];
+    dft16x<false>(v);
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) ys[ycell(16 * k1 + r, lc)] = cmul(v[k1], w[r * k1]);
     __syncthreads();
 #pragma unroll
-    for (int n2 = 0; n2 < 16; ++n2) v[n2] = ok ? hs[(16 * r + n2) * HW + col] : make_float2(0.0f, 0.0f);
-    dft16x<false>(v);   // v[k2] = X[ky = r + 16 k2]
-    if (ok) {
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = ys[ycell(16 * r + n2, lc)];
+    dft16x<false>(v);                        // v[k2] = Y[ky = r + 16 k2]
+    const int kx = kCols * (int)rank + lc;
+    if (kx == 0) {
 #pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2) dst[(size_t)(r + 16 * k2) * kXC + k0 + col] = v[k2];
+      for (int k2 = 0; k2 < 16; ++k2) sep[r + 16 * k2] = v[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2) dst[(size_t)(r + 16 * k2) * kXC + kx] = v[k2];
     }
+  }
+  if (rank == 0) {                           // block-uniform
+    __syncthreads();
+    const float2 W = sep[t], Wm = conjf2(sep[(kXN - t) & (kXN - 1)]);
+    const float2 s = addf2(W, Wm), d = subf2(W, Wm);
+    dst[(size_t)t * kXC] = make_float2(0.5f * s.x, 0.5f * s.y);                 // Y0 = (W + W*[-ky]) / 2
+    dst[(size_t)t * kXC + kXH] = make_float2(0.5f * d.y, -0.5f * d.x);          // Y128 = (W - W*[-ky]) / 2i
   }
 }
 
-__global__ void __launch_bounds__(kXT, 1) xy_c2r_kernel(const cufftComplex* __restrict__ in, float* __restrict__ out,
-                                                       const float2* __restrict__ tw) {
+// Inverse: half spectra [plane][ky][kx] -> real planes [plane][y][x],
+// unnormalised as cuFFT's C2R.
+//   y: 16 threads per column; column kx = 0 is packed with kx = 128 as
+//      Y[0] + i Y[128], whose inverse is the packed slot (X[0], X[128]) of
+//      the rows directly (both real for Hermitian columns); four-step 256
+//      through a column exchange buffer; each value pushed to the CTA that
+//      owns its row.
+//   x: 8 threads per row; Z[k] = (X[k] + X*[128-k]) + i (X[k] - X*[128-k])
+//      e^{2πik/256} from the row buffer, an inverse four-step 128 with the
+//      exchange in the row buffer itself, x[2n] = Re z[n], x[2n+1] = Im z[n].
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
+    xy_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, const float2* __restrict__ tw) {
   extern __shared__ __align__(16) float2 xsm[];
-  constexpr int HP = kXC;                       // row length of the kept rows
-  constexpr int SP = kXN + 1;                   // padded column of the y exchange
-  float2* hr = xsm;                             // [128 rows][129]
-  float2* rbuf = xsm + kXH * HP;                // y exchange [kYCols][257], then x rows [kXRows][128]
-  float2* w256 = rbuf + kYCols * SP;
+  float2* xr = xsm;                          // [64 rows][kXP]
+  float2* eb = xr + kRows * kXP;             // [256][16] column exchange
+  float2* w = eb + kXN * 16;
   const int t = threadIdx.x;
-  const int h = blockIdx.x, y0 = kXH * h;
+  const unsigned rank = cluster_rank();
   const size_t plane = blockIdx.y;
-  const float2* src = reinterpret_cast<const float2*>(in) + plane * (size_t)(kXC * kXN);
-  float* dst = out + plane * (size_t)(kXN * kXN);
-  if (t < kXN) w256[t] = __ldg(tw + t);
-  __syncthreads();
-  // y: inverse four-step per column, the block's rows kept
-  const int cl = t & (kYCols - 1), r = t >> 5;
-  for (int c0 = 0; c0 < kXC; c0 += kYCols) {
-    const int col = c0 + cl;
-    const bool ok = col < kXC;
-    float2* s = rbuf + cl * SP;
-    float2 v[16];
+  cluster_arrive_relaxed();
+  w[t] = __ldg(tw + t);
+  const int col = t & 15, r = t >> 4;
+  const float2* src = in + plane * (size_t)(kXC * kXN);
+  float2 va[16], vb[16];
+  {
+    const int kx0 = kCols * (int)rank + col;
 #pragma unroll
-    for (int n1 = 0; n1 < 16; ++n1) v[n1] = ok ? __ldg(src + (size_t)(16 * n1 + r) * kXC + col) : make_float2(0.0f, 0.0f);
-    dft16x<true>(v);
-    __syncthreads();   // the previous round's reads of the exchange are done
-#pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) s[16 * k1 + r] = cmulc(v[k1], w256[r * k1]);
-    __syncthreads();
-#pragma unroll
-    for (int n2 = 0; n2 < 16; ++n2) v[n2] = s[16 * r + n2];
-    dft16x<true>(v);   // v[k2] = y[r + 16 k2]
-    if (ok) {
-#pragma unroll
-      for (int k2 = 0; k2 < 8; ++k2) hr[(r + 16 * (k2 + 8 * h) - y0) * HP + col] = v[k2 + 8 * h];
+    for (int n1 = 0; n1 < 16; ++n1) {
+      const float2* row = src + (size_t)(16 * n1 + r) * kXC;
+      float2 a = __ldg(row + kx0);
+      if (kx0 == 0) {                         // Y[0] + i Y[128]
+        const float2 h = __ldg(row + kXH);
+        a = make_float2(a.x - h.y, a.y + h.x);
+      }
+      va[n1] = a;
+      vb[n1] = __ldg(row + kx0 + 16);
     }
   }
   __syncthreads();
-  // x: pack, inverse four-step 128, unpack, per kept row
-  const int rl = t >> 3, b = t & 7;
-  float2* rb = rbuf + rl * kXH;
-  for (int g = 0; g < kXH / kXRows; ++g) {
-    const int row = g * kXRows + rl;
-    const float2* xr = hr + row * HP;
+  cluster_wait();
+  const uint32_t xr0 = smem_addr(xr);
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    float2(&v)[16] = g ? vb : va;
+    dft16x<true>(v);
+    if (g) __syncthreads();                  // the previous round's reads of eb are done
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) eb[(16 * k1 + r) * 16 + col] = cmulc(v[k1], w[r * k1]);
+    __syncthreads();
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = eb[(16 * r + n2) * 16 + col];
+    dft16x<true>(v);                         // v[k2] = X_kx[y = r + 16 k2]
+    const int kx = kCols * (int)rank + 16 * g + col;
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+      const int y = r + 16 * k2;
+      st_peer(xr0 + 8u * (uint32_t)((y & (kRows - 1)) * kXP + kx), (unsigned)(y >> 6), v[k2]);
+    }
+  }
+  cluster_arrive_release();
+  cluster_wait_acquire();                    // the CTA's 64 rows are complete
+  const int rl = t >> 3, b = t & 7, rot = 4 * (rl & 1);
+  float* dst = out + plane * (size_t)(kXN * kXN);
+#pragma unroll
+  for (int round = 0; round < 2; ++round) {
+    const int row = 32 * round + rl;
+    float2* xrow = xr + row * kXP;
     float2 v[16];
 #pragma unroll
     for (int a = 0; a < 16; ++a) {
-      const int k = 8 * a + b;   // packed index; Z[k] = (X[k] + X*[128-k]) + i (X[k] - X*[128-k]) W256^{-k}
-      const float2 xk = xr[k], xm = conjf2(xr[kXH - k]);
-      const float2 sdf = cmulc(subf2(xk, xm), w256[k]);
-      v[a] = make_float2(xk.x + xm.x - sdf.y, xk.y + xm.y + sdf.x);
+      const int k = 8 * a + b;
+      const float2 xk = xrow[k];
+      if (a == 0 && b == 0) {
+        v[0] = make_float2(xk.x + xk.y, xk.x - xk.y);   // (X[0] + X[128]) + i (X[0] - X[128])
+      } else {
+        const float2 xm = conjf2(xrow[kXH - k]);
+        const float2 sdf = cmulc(subf2(xk, xm), w[k]);
+        v[a] = make_float2(xk.x + xm.x - sdf.y, xk.y + xm.y + sdf.x);
+      }
     }
-    float2 o[2][8];
-    fft128_row<true>(v, rb, b, w256, o);
-    float2* xo = reinterpret_cast<float2*>(dst + (size_t)(y0 + row) * kXN);
+    __syncwarp();                            // the row's reads are done: it becomes the exchange
+    dft16x<true>(v);
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
+    for (int c = 0; c < 16; ++c) xrow[xslot(c, b, rot)] = cmulc(v[c], w[(2 * b * c) & 255]);
+    __syncwarp();
+    float2* xo = reinterpret_cast<float2*>(dst + (size_t)(kRows * (int)rank + row) * kXN);
 #pragma unroll
-      for (int d = 0; d < 8; ++d) xo[b + 8 * q + 16 * d] = o[q][d];   // (x[2n], x[2n+1]), n = c + 16 d
-    __syncthreads();   // the exchange buffer is free for the next group
+    for (int q = 0; q < 2; ++q) {
+      const int c = b + 8 * q;
+      float2 o[8];
+#pragma unroll
+      for (int bb = 0; bb < 8; ++bb) o[bb] = xrow[xslot(c, bb, rot)];
+      dft8x<true>(o);                        // o[d] = z[c + 16 d]
+#pragma unroll
+      for (int d = 0; d < 8; ++d) xo[c + 16 * d] = o[d];   // (x[2n], x[2n+1])
+    }
   }
 }
 
-constexpr size_t kR2CSmem = sizeof(float2) * (kXN * 65 + kXRows * kXH + kXN);
-constexpr size_t kC2RSmem = sizeof(float2) * (kXH * kXC + kYCols * (kXN + 1) + kXN);
-static_assert(kXRows * kXH <= kYCols * (kXN + 1), "the x rows fit the y exchange region");
+constexpr size_t kR2CSmem = sizeof(float2) * (kXN * kCols + 32 * kXP + kXN);
+constexpr size_t kC2RSmem = sizeof(float2) * (kRows * kXP + kXN * 16 + kXN);
+static_assert(kR2CSmem <= 113 * 1024 && kC2RSmem <= 113 * 1024, "two CTAs per SM");
 
 }  // namespace
 
@@ -280,13 +388,16 @@ static const float2* w256_of(const baorec_ctx* ctx) {
 }
 
 int xy_r2c(baorec_ctx* ctx, const float* in, cufftComplex* out, int planes) {
-  (xy_r2c_kernel<<<dim3(2, planes), kXT, kR2CSmem, ctx->stream>>>(in, out, w256_of(ctx)), ::baorec::count_launch());
+  (xy_r2c_kernel<<<dim3(kCl, planes), kCT, kR2CSmem, ctx->stream>>>(in, reinterpret_cast<float2*>(out), w256_of(ctx)),
+   ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }
 
 int xy_c2r(baorec_ctx* ctx, const cufftComplex* in, float* out, int planes) {
-  (xy_c2r_kernel<<<dim3(2, planes), kXT, kC2RSmem, ctx->stream>>>(in, out, w256_of(ctx)), ::baorec::count_launch());
+  (xy_c2r_kernel<<<dim3(kCl, planes), kCT, kC2RSmem, ctx->stream>>>(reinterpret_cast<const float2*>(in), out,
+                                                                    w256_of(ctx)),
+   ::baorec::count_launch());
   CKLAUNCH();
   return BAOREC_OK;
 }

@@ -65,8 +65,9 @@ def parse():
                          "(a small case for profilers)")
     ap.add_argument("--stencil-only", default="",
                     help="only time finest-level stencil kernels on a --mesh grid (a small case for profilers): "
-                         "comma-separated kernel:pairs:acc, kernel 0 sweep, 1 accurate residual, 3 running "
-                         "residual, pairs and acc the forms of baorec_set_tune_pairs / baorec_set_tune_acc")
+                         "comma-separated kernel:pairs:acc[:xy], kernel 0 sweep, 1 accurate residual, 3 running "
+                         "residual, 8 / 9 batched xy transform forward / inverse, pairs and acc the forms of "
+                         "baorec_set_tune_pairs / baorec_set_tune_acc, xy 0 cuFFT or 1 the fused kernels")
     ap.add_argument("--stencil-reps", type=int, default=20)
     ap.add_argument("--paint-only", default="",
                     help="only time the CIC paint of the lightcone randoms into the --mesh grid (a small case "
@@ -788,12 +789,13 @@ def run_stencil_only(args):
     torch.cuda.synchronize()
     rows = []
     for spec in filter(None, args.stencil_only.split(",")):
-        which, pairs, acc = (list(map(int, spec.split(":"))) + [1, 0])[:3]
+        which, pairs, acc, xy = (list(map(int, spec.split(":"))) + [1, 0, 1])[:4]
         ctx.call("baorec_set_tune_pairs", pairs)
         ctx.call("baorec_set_tune_acc", acc)
+        ctx.call("baorec_set_tune_xy", xy)
         avg, nbytes = C.c_float(), C.c_double()
         ctx.call("baorec_profile_kernel", which, args.stencil_reps, C.byref(avg), C.byref(nbytes))
-        rows.append({"kernel": which, "pairs": pairs, "acc": acc, "avg_launch_us": avg.value * 1e3,
+        rows.append({"kernel": which, "pairs": pairs, "acc": acc, "xy": xy, "avg_launch_us": avg.value * 1e3,
                      "algorithmic_GBps": nbytes.value / (avg.value * 1e-3) / 1e9})
     print(json.dumps({"metric": "stencil kernel time", "mesh": args.mesh, "kernels": rows}), flush=True)
     return 0
@@ -975,6 +977,22 @@ def run_gb300(args):
                 "avg_launch_ms": avg.value, "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
         ctx.call("baorec_set_tune_pairs", chosen)
         meas["pair_forms"] = forms
+        # the batched xy transforms of the FFT corrections: cuFFT's two passes
+        # against the fused cluster kernels, the tuner's choice restored
+        if n[2] == 256:
+            xyf = {}
+            chosen = ctx.lib.baorec_tune_xy(ctx.h)
+            for xy, label in ((0, "cuFFT"), (1, "fused cluster kernels")):
+                ctx.call("baorec_set_tune_xy", xy)
+                for which, d in ((8, "forward"), (9, "inverse")):
+                    avg, nbytes = C.c_float(), C.c_double()
+                    ctx.call("baorec_profile_kernel", which, 30, C.byref(avg), C.byref(nbytes))
+                    xyf["%s %s" % (label, d)] = {
+                        "avg_launch_ms": avg.value, "algorithmic_bytes_per_launch": nbytes.value,
+                        "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
+            ctx.call("baorec_set_tune_xy", chosen)
+            xyf["chosen"] = "fused cluster kernels" if chosen else "cuFFT"
+            meas["xy_transforms"] = xyf
     # V-cycles/s: one V-cycle of the residual-driven solve (the plain start's
     # step) and one of the reference's schedule (vcycle!), on the finest level
     vcycles = {}
@@ -990,9 +1008,11 @@ def run_gb300(args):
     if meas:
         roofline = dict(meas[head])
         roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
-        aux = {names[w]: meas[w] for w in meas if w != head and w != "pair_forms"}
+        aux = {names[w]: meas[w] for w in meas if w != head and w not in ("pair_forms", "xy_transforms")}
         if "pair_forms" in meas:
             aux["running residual forms"] = meas["pair_forms"]
+        if "xy_transforms" in meas:
+            aux["xy transforms"] = meas["xy_transforms"]
 
     # end to end through the C ABI with pinned host buffers
     e2e = None

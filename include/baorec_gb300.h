@@ -233,8 +233,11 @@ int baorec_mg_solve(baorec_ctx* ctx, const float* f, float* phi, const float* ph
  * levels in one cooperative kernel, FP64 coarsest solve), 7 = one V-cycle of
  * the reference schedule (vcycle!: jacobi_niterations damped-Jacobi sweeps
  * before and after on every level); for 6 and 7 the bytes are those of every
- * level's sweeps, residual, restriction and prolongation.  Needs a multigrid
- * context. */
+ * level's sweeps, residual, restriction and prolongation; 8 and 9 = the
+ * batched 2-D forward (real to half spectrum) and inverse transforms of the
+ * finest mesh's xy planes (meshes of 256 z planes), by the autotuner's
+ * current choice (baorec_set_tune_xy): the fused cluster kernels or cuFFT.
+ * Needs a multigrid context. */
 int baorec_profile_kernel(baorec_ctx* ctx, int which, int reps, float* avg_ms, double* bytes_per_launch);
 
 /* Statistics of the context's last residual-driven solve. */
