@@ -948,16 +948,23 @@ def run_gb300(args):
 
     # rooflines measured live (CUDA events on the context stream around a run
     # of launches on the finest level); the headline is the dominant kernel of
-    # the timed path (largest share of its launch list): the FP32 running
-    # residual of the FFT corrections for the FFT / learned starts (6 launches
-    # per reconstruction against the accurate residual's 2), in the form the
-    # solve uses; the red-black sweep for the plain multigrid start
+    # the timed path: the largest device time per reconstruction (launches per
+    # reconstruction of the last timed solve x the live per-launch time) among
+    # the FP32 running residual of the FFT corrections, the accurate residual
+    # and the batched xy transforms for the FFT / learned starts; the
+    # red-black sweep for the plain multigrid start
     peak, peak_src = measured_peak()
     N = int(np.prod(n))
+    xy_fused = bool(tune.get("fft_xy_fused", 0))
     names = {0: "rb_sweep2_kernel", 1: "resid_acc2_kernel", 3: RUNNING_RESIDUAL[tune.get("pair_residual", 0)],
-             4: "resid_acc_stream_kernel", 5: "resid_diff_stream_kernel"}
+             4: "resid_acc_stream_kernel", 5: "resid_diff_stream_kernel",
+             8: ("xy_r2c_kernel (fused xy forward transform, four-CTA clusters)" if xy_fused
+                 else "cuFFT xy forward transform (two passes)"),
+             9: ("xy_c2r_kernel (fused xy inverse transform, four-CTA clusters)" if xy_fused
+                 else "cuFFT xy inverse transform (two passes)")}
     meas = {}
-    for which in (() if args.no_kernels else (0, 1, 3, 4, 5)):
+    kinds = (0, 1, 3, 4, 5) + ((8, 9) if n[2] == 256 and tune.get("fft_zpass", 0) else ())
+    for which in (() if args.no_kernels else kinds):
         avg, nbytes = C.c_float(), C.c_double()
         ctx.call("baorec_profile_kernel", which, 30, C.byref(avg), C.byref(nbytes))
         ach = nbytes.value / (avg.value * 1e-3) / 1e9
@@ -1004,10 +1011,22 @@ def run_gb300(args):
                           "achieved": nbytes.value / (avg.value * 1e-3) / 1e9, "unit": "GB/s", "peak": peak,
                           "frac": nbytes.value / (avg.value * 1e-3) / 1e9 / peak}
     head = 0 if args.start == "zero" else (5 if tune.get("stream_residuals", -1) != 0 else 3)
+    device_ms = {}
+    if meas and args.start != "zero":
+        corr = int(stats["spectral_steps"])
+        n_acc = max(len(ctx.solve_history()) - 1, 0)   # one accurate residual after each outer step
+        units = {head: max(corr - n_acc, 0), 1: n_acc}
+        if 8 in meas:   # the corrections, the smoothing pair (two meshes) and the displacement (1 / 3 meshes)
+            units[8], units[9] = corr + 3, corr + 5
+        device_ms = {w: u * meas[w]["avg_launch_ms"] for w, u in units.items()}
+        head = max(device_ms, key=device_ms.get)
     roofline, aux = None, {}
     if meas:
         roofline = dict(meas[head])
         roofline["kernel"] = "%s (finest level %s)" % (names[head], "x".join(map(str, n)))
+        if device_ms:
+            roofline["device_ms_per_reconstruction"] = {names[w].split()[0] if w not in (8, 9) else names[w]: v
+                                                        for w, v in device_ms.items()}
         aux = {names[w]: meas[w] for w in meas if w != head and w not in ("pair_forms", "xy_transforms")}
         if "pair_forms" in meas:
             aux["running residual forms"] = meas["pair_forms"]
