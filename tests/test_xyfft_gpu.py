@@ -80,3 +80,42 @@ def test_preconditioner_256_fused_matches_cufft(los):
         assert max(rels) < 1e-3
     assert hists[0] == hists[1]
     assert rel_l2(phis[1] - phis[1].mean(), phis[0] - phis[0].mean()) < 1e-5
+
+
+def _mg_context(n):
+    from baorec import _lib
+    cfg = _lib.default_config()
+    cfg.method = _lib.MULTIGRID
+    cfg.mg_mode = _lib.MG_CONVERGENT
+    for a, lo in enumerate((500.0, 300.0, 200.0)):
+        cfg.n[a] = n
+        cfg.box_size[a] = 2000.0 * n / 256
+        cfg.box_min[a] = lo
+    return _lib.Context(cfg)
+
+
+def test_profile_hook_times_both_xy_transform_paths():
+    """baorec_profile_kernel 8 / 9 time the batched xy transforms of the
+    finest mesh by the current choice (cuFFT or the fused kernels) and report
+    their algorithmic bytes: the real mesh plus the half spectrum."""
+    import ctypes as C
+    from baorec import _lib
+    ctx = _mg_context(256)
+    want = 4.0 * 256 ** 3 + 8.0 * 129 * 256 * 256
+    for xy in (0, 1):
+        ctx.call("baorec_set_tune_xy", xy)
+        for which in (8, 9):
+            avg, nbytes = C.c_float(), C.c_double()
+            ctx.call("baorec_profile_kernel", which, 3, C.byref(avg), C.byref(nbytes))
+            assert nbytes.value == want
+            assert 0.0 < avg.value < 10.0
+
+
+def test_profile_hook_rejects_meshes_without_batched_xy_transforms():
+    import ctypes as C
+    from baorec import _lib
+    ctx = _mg_context(64)
+    avg, nbytes = C.c_float(), C.c_double()
+    with pytest.raises(_lib.BaorecError, match="xy") as e:
+        ctx.call("baorec_profile_kernel", 8, 3, C.byref(avg), C.byref(nbytes))
+    assert e.value.code == _lib.ERR_ARG
