@@ -113,7 +113,7 @@ __device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.c
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-// store v at the shared-memory offset `local` of cluster CTA `rank`
+// store v in cluster CTA `rank` at the position of this CTA's shared-memory address `local`
 __device__ __forceinline__ void st_peer(uint32_t local, unsigned rank, float2 v) {
   uint32_t a;
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(local), "r"(rank));
