@@ -140,6 +140,15 @@ static_assert(kCT == kXN, "one twiddle per thread");
 // the two rows sharing a half-warp meet in a bank.
 __device__ __forceinline__ int xslot(int c, int bb, int rot) { return 8 * c + ((bb + (c >> 1) + rot) & 7); }
 
+// Twiddles in shared memory: W256^m at [m], then the row transform's
+// W128^{bc} = W256^{2bc} at [256 + 8c + b] (eight consecutive entries per c,
+// so the eight lanes of a row read distinct banks).
+constexpr int kTw = kXN + 128;
+__device__ __forceinline__ void load_twiddles(float2* w, const float2* __restrict__ tw, int t) {
+  w[t] = __ldg(tw + t);
+  if (t < 128) w[kXN + t] = __ldg(tw + ((2 * (t & 7) * (t >> 3)) & (kXN - 1)));
+}
+
 // Spectrum-side column buffer of the forward kernel: [256 rows][32 columns],
 // column index XOR 8 on odd rows (two rows of one half-warp's pushes land
 // in disjoint banks).
@@ -172,7 +181,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
   const unsigned rank = cluster_rank();
   const size_t plane = blockIdx.y;
   cluster_arrive_relaxed();                  // matched below, before the first push
-  w[t] = __ldg(tw + t);
+  load_twiddles(w, tw, t);
   const int rl = t >> 3, b = t & 7, rot = 4 * (rl & 1);
   const float2* src = reinterpret_cast<const float2*>(in + plane * (size_t)(kXN * kXN));
   const int y0 = kRows * (int)rank + rl;
@@ -182,8 +191,8 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
 #pragma unroll
   for (int a = 0; a < 16; ++a) vb[a] = __ldg(src + (size_t)(y0 + 32) * kXH + 8 * a + b);
   __syncthreads();
-  cluster_wait();                            // every CTA of the cluster runs: pushes may start
   const uint32_t ys0 = smem_addr(ys);
+  const float2* twx = w + kXN;
   float2* rb = xb + rl * kXP;
   const unsigned lane = t & 31, partner = (lane & ~7u) | ((8u - b) & 7u);
 #pragma unroll
@@ -192,7 +201,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
     const int y = y0 + 32 * round;
     dft16x<false>(v);
 #pragma unroll
-    for (int c = 0; c < 16; ++c) rb[xslot(c, b, rot)] = cmul(v[c], w[(2 * b * c) & 255]);   // W128^{bc}
+    for (int c = 0; c < 16; ++c) rb[xslot(c, b, rot)] = cmul(v[c], twx[8 * c + b]);   // W128^{bc}
     __syncwarp();
     float2 o[2][8];
 #pragma unroll
@@ -204,6 +213,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
     }
     __syncwarp();                            // the row buffer is free for the next round
     const int ysw = (y & 1) << 3;
+    if (round == 0) cluster_wait();          // every CTA of the cluster runs: pushes may start
     {   // c = b: partner Z[128 - k] = lane (8 - b)'s o[1][7 - d]; b = 0: own o[0][8 - d]
       float2 p[8];
 #pragma unroll
@@ -290,7 +300,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
   const unsigned rank = cluster_rank();
   const size_t plane = blockIdx.y;
   cluster_arrive_relaxed();
-  w[t] = __ldg(tw + t);
+  load_twiddles(w, tw, t);
   const int col = t & 15, r = t >> 4;
   const float2* src = in + plane * (size_t)(kXC * kXN);
   float2 va[16], vb[16];
@@ -309,7 +319,6 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
     }
   }
   __syncthreads();
-  cluster_wait();
   const uint32_t xr0 = smem_addr(xr);
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
@@ -323,6 +332,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
     for (int n2 = 0; n2 < 16; ++n2) v[n2] = eb[(16 * r + n2) * 16 + col];
     dft16x<true>(v);                         // v[k2] = X_kx[y = r + 16 k2]
     const int kx = kCols * (int)rank + 16 * g + col;
+    if (g == 0) cluster_wait();              // every CTA of the cluster runs: pushes may start
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
       const int y = r + 16 * k2;
@@ -353,7 +363,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
     __syncwarp();                            // the row's reads are done: it becomes the exchange
     dft16x<true>(v);
 #pragma unroll
-    for (int c = 0; c < 16; ++c) xrow[xslot(c, b, rot)] = cmulc(v[c], w[(2 * b * c) & 255]);
+    for (int c = 0; c < 16; ++c) xrow[xslot(c, b, rot)] = cmulc(v[c], w[kXN + 8 * c + b]);
     __syncwarp();
     float2* xo = reinterpret_cast<float2*>(dst + (size_t)(kRows * (int)rank + row) * kXN);
 #pragma unroll
@@ -369,8 +379,8 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kCT, 2)
   }
 }
 
-constexpr size_t kR2CSmem = sizeof(float2) * (kXN * kCols + 32 * kXP + kXN);
-constexpr size_t kC2RSmem = sizeof(float2) * (kRows * kXP + kXN * 16 + kXN);
+constexpr size_t kR2CSmem = sizeof(float2) * (kXN * kCols + 32 * kXP + kTw);
+constexpr size_t kC2RSmem = sizeof(float2) * (kRows * kXP + kXN * 16 + kTw);
 static_assert(kR2CSmem <= 113 * 1024 && kC2RSmem <= 113 * 1024, "two CTAs per SM");
 
 }  // namespace
