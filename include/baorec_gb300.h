@@ -552,7 +552,11 @@ int baorec_tune_zpass(const baorec_ctx* ctx);
 int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass);
 /* The xy transforms of the z-pass paths (preconditioner, smoothing,
  * displacement) for 256 x 256 planes: 0 cuFFT's batched 2-D transforms
- * (default), 1 one fused kernel per direction.  The stencil autotune times both. */
+ * (default), 1 one fused kernel per direction (a cluster of four CTAs per
+ * plane, the rows <-> columns transposition through distributed shared
+ * memory: each plane read and written once).  The stencil autotune times
+ * both and keeps the faster (on a GB300 the fused kernels: about 49 / 52 us
+ * per 256-plane transform against 62 us). */
 int baorec_tune_xy(const baorec_ctx* ctx);
 int baorec_set_tune_xy(baorec_ctx* ctx, int xy);
 

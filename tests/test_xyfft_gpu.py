@@ -1,6 +1,7 @@
 """Fused 2-D real transforms of 256 x 256 xy planes (xyfft.cu: packed
-128-point row transforms and 256-point four-step column transforms, one
-kernel per direction) against cuFFT's batched 2-D transforms and the oracle,
+128-point row transforms and 256-point four-step column transforms on a
+four-CTA cluster per plane, one kernel per direction) against cuFFT's batched
+2-D transforms and the oracle,
 through the three paths that use them on meshes of 256 z planes: smoothing,
 the displacement spectra and the FFT preconditioner."""
 import numpy as np
