@@ -115,7 +115,7 @@ struct baorec_ctx {
     int pairs = 1;                     // form of the FP32 running residual (baorec_set_tune_pairs)
     int acc = 0;                       // form of the accurate residual (baorec_set_tune_acc)
     int zpass = 1;                     // FFT preconditioner: 1 (2: capped registers) xy transforms + fused z pass where n3 = 256, 0 3-D transforms
-    int xy = 0;                        // xy transforms of the z-pass paths: 0 cuFFT, 1 fused kernels (256 x 256 planes)
+    int xy = 1;                        // xy transforms of the z-pass paths: 0 cuFFT, 1 fused kernels (256 x 256 planes)
     int big_tiles[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};   // per level: -1 heuristic, 0/1
     bool tuned = false;
   } tune;

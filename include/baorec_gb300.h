@@ -551,8 +551,8 @@ int baorec_set_tune_acc(baorec_ctx* ctx, int acc);
 int baorec_tune_zpass(const baorec_ctx* ctx);
 int baorec_set_tune_zpass(baorec_ctx* ctx, int zpass);
 /* The xy transforms of the z-pass paths (preconditioner, smoothing,
- * displacement) for 256 x 256 planes: 0 cuFFT's batched 2-D transforms
- * (default), 1 one fused kernel per direction (a cluster of four CTAs per
+ * displacement) for 256 x 256 planes: 0 cuFFT's batched 2-D transforms,
+ * 1 (default) one fused kernel per direction (a cluster of four CTAs per
  * plane, the rows <-> columns transposition through distributed shared
  * memory: each plane read and written once).  The stencil autotune times
  * both and keeps the faster (on a GB300 the fused kernels: about 49 / 52 us
